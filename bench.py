@@ -1,0 +1,353 @@
+"""Benchmark of the GB300 reduce / scatter hot path on the MDRange +
+ScatterView workload:
+
+  step = MDRangePolicy<Rank<3>> MinLoc, MaxLoc and Sum over a LayoutLeft
+         View<float***> 512x512x256 of N(0,1) values (three reduces), plus a
+         ScatterView histogram of 2^26 int32 Zipf(s=1.1) keys over 2^16 bins
+         into int64 counts (bins zeroed, then contributed).
+  metric = algorithmic HBM bytes of the step / step time, in GB/s:
+           3 x 268,435,456 (reduces) + 268,435,456 + 524,288 (histogram).
+
+`value` times the device path (inputs resident in HBM; every input is
+268 MB, larger than the 129 MB L2, so no flush is needed).  `e2e` times the
+same step through the C ABI from pinned HOST buffers: deep_copy of the view
+and the keys to the device, the four operations, and the results copied
+back, every step.  `roofline` is the dominant kernel (the flat reduce
+kernel the contiguous MDRange box collapses to).  `cpu_baseline` is the
+oracle (CPU restatement of the reference OpenMP algorithms) on this host.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbk|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own
+GPU (the path does not shard across GPUs here); value = all ranks' bytes /
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N0, N1, N2 = 512, 512, 256
+NX = N0 * N1 * N2
+NKEYS = 1 << 26
+NBINS = 1 << 16
+RED_BYTES = NX * 4
+HIST_BYTES = NKEYS * 4 + NBINS * 8
+STEP_BYTES = 3 * RED_BYTES + HIST_BYTES
+WORKLOAD = ("MDRange<Rank<3>> MinLoc+MaxLoc+Sum over LayoutLeft View<float***> 512x512x256 N(0,1) "
+            "+ ScatterView histogram 2^26 int32 Zipf(1.1) keys -> 2^16 int64 bins")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in open(self.path):
+            c = [x.strip() for x in ln.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                mx.append(float(c[2]))
+                power.append(float(c[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, c[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": float(max(power)) if power else None}
+
+
+def cpu_baseline(budget_s=12.0):
+    """Oracle (CPU restatement of the reference OpenMP reduce and ScatterView
+    algorithms) over the same workload on this host's cores: full-size
+    inputs, as many whole steps as fit in the time budget (at least one)."""
+    import oracle
+    from kokkos_gb300 import datagen
+    P = oracle.max_threads()
+    x = datagen.normal_f32(NX, seed=0)
+    keys = datagen.zipf_i32(NKEYS, NBINS, 1.1, seed=0)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        # The full box of a LayoutLeft view is one contiguous range with
+        # loc = flat index, so the range reduce is the MDRange reduce.
+        oracle.reduce("minloc", x, P)
+        oracle.reduce("maxloc", x, P)
+        oracle.reduce("sum", x, P)
+        oracle.histogram(keys, NBINS, P)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 50:
+            break
+    gbs = steps * STEP_BYTES / el / 1e9
+    return {"value": round(gbs, 3), "unit": "GB/s", "cores": P, "kind": "port",
+            "sample": f"{steps} full-size steps ({el:.1f} s) of the same workload, OpenMP threads={P}"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU implementation of the path on
+    this host.  The reference build (oracle/_ref) is produced in a container
+    with the reference sources and is x86-only; on any other host the oracle
+    port of the same algorithms is timed."""
+    if rank != 0:
+        return
+    cb = cpu_baseline(budget_s=max(5.0, 2.0 * (args.steps + args.warmup)))
+    line = {"metric": "HBM GB/s (algorithmic bytes / step time)", "value": cb["value"], "unit": "GB/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(STEP_BYTES / (cb["value"] * 1e9) * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, seed 0)",
+            "config": {"workload": WORKLOAD, "step_bytes": STEP_BYTES}, "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbk", choices=["gbk", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+
+    from kokkos_gb300 import datagen, gbk
+    dist = init_dist(world)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    lib = gbk.lib
+
+    # ---- inputs (pinned host, seeded) and their device copies --------------
+    hx = torch.empty(NX, dtype=torch.float32, pin_memory=True)
+    hk = torch.empty(NKEYS, dtype=torch.int32, pin_memory=True)
+    datagen.normal_f32(NX, seed=0 + rank, out=hx.numpy())
+    datagen.zipf_i32(NKEYS, NBINS, 1.1, seed=0 + rank, out=hk.numpy())
+    dx = hx.to(dev, non_blocking=False)
+    dk = hk.to(dev, non_blocking=False)
+    dbins = torch.zeros(NBINS, dtype=torch.int64, device=dev)
+    dres = torch.zeros(256, dtype=torch.uint8, device=dev)
+    hres = torch.zeros(256, dtype=torch.uint8, pin_memory=True)
+    hbins = torch.zeros(NBINS, dtype=torch.int64, pin_memory=True)
+    torch.cuda.synchronize()
+
+    rk = 3
+    lo = (ctypes.c_int64 * rk)(0, 0, 0)
+    up = (ctypes.c_int64 * rk)(N0, N1, N2)
+    st = (ctypes.c_int64 * rk)(1, N0, N0 * N1)
+    X, K, B, R = (ctypes.c_void_p(t.data_ptr()) for t in (dx, dk, dbins, dres))
+    R0, R1, R2 = (ctypes.c_void_p(dres.data_ptr() + o) for o in (0, 64, 128))
+
+    def op_minloc():
+        gbk.check(lib.gbk_mdrange_reduce(8, 4, X, rk, lo, up, st, R0, sp, None), "minloc")
+
+    def op_maxloc():
+        gbk.check(lib.gbk_mdrange_reduce(9, 4, X, rk, lo, up, st, R1, sp, None), "maxloc")
+
+    def op_sum():
+        gbk.check(lib.gbk_mdrange_reduce(0, 4, X, rk, lo, up, st, R2, sp, None), "sum")
+
+    def op_hist():
+        gbk.check(lib.gbk_memset(B, 0, NBINS * 8, sp), "memset")
+        gbk.check(lib.gbk_histogram_i32_i64(K, NKEYS, B, NBINS, sp, None), "histogram")
+
+    ops = [("mdrange_minloc_f32", op_minloc, RED_BYTES), ("mdrange_maxloc_f32", op_maxloc, RED_BYTES),
+           ("mdrange_sum_f32", op_sum, RED_BYTES), ("histogram_zipf_2^16", op_hist, HIST_BYTES)]
+
+    def step(evs=None):
+        for i, (_, f, _) in enumerate(ops):
+            if evs is not None:
+                evs[i][0].record(stream)
+            f()
+            if evs is not None:
+                evs[i][1].record(stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    gbk.stream_check(stream)
+
+    # ---- timed region: device path ------------------------------------------
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in ops]
+           for _ in range(args.steps)]
+    clocks = Clocks(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    l0 = gbk.launch_count()
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        t_start.record(stream)
+        for s_ in range(args.steps):
+            step(evs[s_])
+        t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    launches = gbk.launch_count() - l0
+    clk = clocks.stop()
+    gbk.stream_check(stream)
+    ms_total = t_start.elapsed_time(t_end)
+    ms_total = max_over_ranks(dist, ms_total)
+    ms_step = ms_total / args.steps
+    value = world * STEP_BYTES * args.steps / (ms_total / 1e3) / 1e9
+
+    per_op = {}
+    hbm, peak_kind = peaks()
+    for i, (name, _, nbytes) in enumerate(ops):
+        ts = [evs[s_][i][0].elapsed_time(evs[s_][i][1]) for s_ in range(args.steps)]
+        avg = float(np.mean(ts))
+        gbs = nbytes / (avg / 1e3) / 1e9
+        per_op[name] = {"ms": round(avg, 5), "GB/s": round(gbs, 1), "frac_of_" + peak_kind + "_hbm": round(gbs / hbm, 4)}
+    red_ms = np.mean([per_op[n]["ms"] for n in ("mdrange_minloc_f32", "mdrange_maxloc_f32", "mdrange_sum_f32")])
+    red_gbs = RED_BYTES / (red_ms / 1e3) / 1e9
+
+    # ---- e2e: through the C ABI from pinned host buffers ---------------------
+    HX, HK = ctypes.c_void_p(hx.data_ptr()), ctypes.c_void_p(hk.data_ptr())
+    HR, HB = ctypes.c_void_p(hres.data_ptr()), ctypes.c_void_p(hbins.data_ptr())
+
+    def e2e_step():
+        gbk.check(lib.gbk_deep_copy(X, HX, NX * 4, sp), "h2d x")
+        gbk.check(lib.gbk_deep_copy(K, HK, NKEYS * 4, sp), "h2d keys")
+        step()
+        gbk.check(lib.gbk_deep_copy(HR, R, 192, sp), "d2h results")
+        gbk.check(lib.gbk_deep_copy(HB, B, NBINS * 8, sp), "d2h bins")
+        stream.synchronize()
+
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        e2e_step()
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e_ms = (time.perf_counter() - e0) * 1e3 / e2e_steps
+    e_ms = max_over_ranks(dist, e_ms)
+    e2e_val = world * STEP_BYTES / (e_ms / 1e3) / 1e9
+    gbk.stream_check(stream)
+
+    # correctness spot check of the last step's results (rank-local, cheap)
+    r = hres.numpy()
+    mn = gbk.decode_result(r[0:16], 8, 4)
+    hx_np = hx.numpy()
+    ok = bool(mn["val"] == hx_np.min() and int(hbins.numpy().sum()) == NKEYS)
+
+    line = {
+        "metric": "HBM GB/s (algorithmic bytes / step time) of MDRange reduce + ScatterView histogram",
+        "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded xoshiro256**, seed 0; N(0,1) floats, Zipf(1.1) keys)",
+        "config": {"workload": WORKLOAD, "step_bytes": STEP_BYTES, "l2": "inputs 268 MB each > 129 MB L2; no flush",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "k_reduce_flat (MinLoc/MaxLoc/Sum f32)",
+                     "achieved": round(red_gbs, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(red_gbs / hbm, 4), "peak_kind": peak_kind + " hbm_gbs (burst copy)",
+                     "traffic": None},
+        "ops": per_op,
+        "e2e": {"value": round(e2e_val, 1), "unit": "GB/s", "ms_per_step": round(e_ms, 3),
+                "h2d_bytes_per_step": NX * 4 + NKEYS * 4, "d2h_bytes_per_step": 192 + NBINS * 8},
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": launches / args.steps,
+        "clocks": clk,
+        "result_check": ok,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

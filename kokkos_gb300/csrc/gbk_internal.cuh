@@ -1,0 +1,297 @@
+// Internal device/host helpers shared by the libgbk translation units.
+//
+// Layout of the per-stream workspace (device memory owned by the library,
+// never by the caller):
+//   counters[64]  u32 slots, zero between launches (each kernel that takes a
+//                 ticket resets its slot before it exits)
+//   err           i32 device error bits (GBK_EBIT_*), read and cleared by
+//                 gbk_stream_check
+//   scratch       partials, tile status, sort temporaries (grown on demand
+//                 outside stream capture)
+//   stage         device copy of host inputs for the *_host entry points
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <mutex>
+
+#include "../../include/gbk.h"
+
+#define GBK_EBIT_TIMEOUT 1
+#define GBK_EBIT_KEY_RANGE 2
+#define GBK_EBIT_BAD_STATE 4
+
+namespace gbk {
+
+// ---------------------------------------------------------------------------
+// host runtime (gbk_runtime.cu)
+struct Workspace {
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  unsigned* counters = nullptr;  // 64 slots
+  int* err = nullptr;
+  char* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  char* stage = nullptr;
+  size_t stage_bytes = 0;
+  // Look-back status words, used only by kernels that tag them with `epoch`
+  // (bumped per launch), so no other kernel's data can look like a flag.
+  char* flags = nullptr;
+  size_t flags_bytes = 0;
+  uint32_t epoch = 0;
+  std::mutex mu;
+};
+
+Workspace* ws_get(cudaStream_t s, int* status);
+// Status-word buffer of at least `count` u32 and the next 30-bit epoch.
+unsigned* ws_flags(Workspace* w, size_t count, unsigned* epoch, int* status);
+// Ensure at least `bytes` of scratch; returns nullptr (and sets status) on
+// failure or when growth is needed while the stream is being captured.
+char* ws_scratch(Workspace* w, size_t bytes, int* status);
+char* ws_stage(Workspace* w, size_t bytes, int* status);
+int sm_count();
+int64_t wait_limit();
+void note_launch(int64_t k = 1);
+int cuda_status(cudaError_t e);
+// Counter slots
+enum { SLOT_REDUCE = 0, SLOT_SCAN_TILE = 1, SLOT_MISC = 2, SLOT_SEG = 3, SLOT_SORT = 8 };
+
+// ---------------------------------------------------------------------------
+// dtype mapping
+template <int DT> struct dtype_of;
+template <> struct dtype_of<GBK_I32> { using type = int32_t; };
+template <> struct dtype_of<GBK_I64> { using type = int64_t; };
+template <> struct dtype_of<GBK_U32> { using type = uint32_t; };
+template <> struct dtype_of<GBK_U64> { using type = uint64_t; };
+template <> struct dtype_of<GBK_F32> { using type = float; };
+template <> struct dtype_of<GBK_F64> { using type = double; };
+
+inline size_t dtype_size(int dt) { return (dt == GBK_I32 || dt == GBK_U32 || dt == GBK_F32) ? 4 : 8; }
+
+// ---------------------------------------------------------------------------
+// identities (core/src/Kokkos_ReductionIdentity.hpp)
+template <class T> struct lim;
+template <> struct lim<int32_t> { __host__ __device__ static constexpr int32_t hi() { return 2147483647; } __host__ __device__ static constexpr int32_t lo() { return -2147483647 - 1; } };
+template <> struct lim<uint32_t> { __host__ __device__ static constexpr uint32_t hi() { return 0xFFFFFFFFu; } __host__ __device__ static constexpr uint32_t lo() { return 0u; } };
+template <> struct lim<int64_t> { __host__ __device__ static constexpr int64_t hi() { return 9223372036854775807LL; } __host__ __device__ static constexpr int64_t lo() { return -9223372036854775807LL - 1; } };
+template <> struct lim<uint64_t> { __host__ __device__ static constexpr uint64_t hi() { return 0xFFFFFFFFFFFFFFFFull; } __host__ __device__ static constexpr uint64_t lo() { return 0ull; } };
+template <> struct lim<float> { __host__ __device__ static constexpr float hi() { return 3.402823466e+38F; } __host__ __device__ static constexpr float lo() { return -3.402823466e+38F; } };
+template <> struct lim<double> { __host__ __device__ static constexpr double hi() { return 1.7976931348623158e+308; } __host__ __device__ static constexpr double lo() { return -1.7976931348623158e+308; } };
+
+constexpr int64_t LOC_ID = 9223372036854775807LL;
+
+template <class T> struct ValLoc { T val; int64_t loc; };
+template <class T> struct MinMaxV { T min_val, max_val; };
+template <class T> struct MinMaxLocV { T min_val, max_val; int64_t min_loc, max_loc; };
+
+// ---------------------------------------------------------------------------
+// warp shuffles of the value types
+template <class T> __device__ __forceinline__ T shx(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+template <class T> __device__ __forceinline__ ValLoc<T> shx(ValLoc<T> v, int m) {
+  v.val = shx(v.val, m); v.loc = shx(v.loc, m); return v;
+}
+template <class T> __device__ __forceinline__ MinMaxV<T> shx(MinMaxV<T> v, int m) {
+  v.min_val = shx(v.min_val, m); v.max_val = shx(v.max_val, m); return v;
+}
+template <class T> __device__ __forceinline__ MinMaxLocV<T> shx(MinMaxLocV<T> v, int m) {
+  v.min_val = shx(v.min_val, m); v.max_val = shx(v.max_val, m);
+  v.min_loc = shx(v.min_loc, m); v.max_loc = shx(v.max_loc, m); return v;
+}
+
+// ---------------------------------------------------------------------------
+// Reducers.  update(v, x, loc) is the element functor of the typed entry
+// (v op= x); join(a, b) combines partial results.  ORDERED visits: a thread
+// sees its elements in increasing loc, so *Loc updates use a strict compare
+// (first occurrence wins, as the reference functor); unordered visits use
+// the (value, loc) order.
+template <class T> struct RSum {
+  using V = T;
+  __device__ static V init() { return T(0); }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) { v += x; }
+  __device__ static void join(V& a, const V& b) { a += b; }
+};
+template <class T> struct RProd {
+  using V = T;
+  __device__ static V init() { return T(1); }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) { v *= x; }
+  __device__ static void join(V& a, const V& b) { a *= b; }
+};
+template <class T> struct RMin {
+  using V = T;
+  __device__ static V init() { return lim<T>::hi(); }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) { v = (x < v) ? x : v; }
+  __device__ static void join(V& a, const V& b) { a = (b < a) ? b : a; }
+};
+template <class T> struct RMax {
+  using V = T;
+  __device__ static V init() { return lim<T>::lo(); }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) { v = (x > v) ? x : v; }
+  __device__ static void join(V& a, const V& b) { a = (b > a) ? b : a; }
+};
+template <class T> struct RLAnd {
+  using V = T;
+  __device__ static V init() { return T(1); }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) { v = (v && x) ? T(1) : T(0); }
+  __device__ static void join(V& a, const V& b) { a = (a && b) ? T(1) : T(0); }
+};
+template <class T> struct RLOr {
+  using V = T;
+  __device__ static V init() { return T(0); }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) { v = (v || x) ? T(1) : T(0); }
+  __device__ static void join(V& a, const V& b) { a = (a || b) ? T(1) : T(0); }
+};
+template <class T> struct RBAnd {
+  using V = T;
+  __device__ static V init() { return T(~T(0)); }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) { v &= x; }
+  __device__ static void join(V& a, const V& b) { a &= b; }
+};
+template <class T> struct RBOr {
+  using V = T;
+  __device__ static V init() { return T(0); }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) { v |= x; }
+  __device__ static void join(V& a, const V& b) { a |= b; }
+};
+template <class T> struct RMinLoc {
+  using V = ValLoc<T>;
+  __device__ static V init() { return V{lim<T>::hi(), LOC_ID}; }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t l) {
+    if (ORD) {
+      if (x < v.val) { v.val = x; v.loc = l; }
+    } else {
+      if (x < v.val || (x == v.val && v.loc != LOC_ID && l < v.loc)) { v.val = x; v.loc = l; }
+    }
+  }
+  __device__ static void join(V& a, const V& b) {
+    if (b.val < a.val || (b.val == a.val && b.loc < a.loc)) a = b;
+  }
+};
+template <class T> struct RMaxLoc {
+  using V = ValLoc<T>;
+  __device__ static V init() { return V{lim<T>::lo(), LOC_ID}; }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t l) {
+    if (ORD) {
+      if (x > v.val) { v.val = x; v.loc = l; }
+    } else {
+      if (x > v.val || (x == v.val && v.loc != LOC_ID && l < v.loc)) { v.val = x; v.loc = l; }
+    }
+  }
+  __device__ static void join(V& a, const V& b) {
+    if (b.val > a.val || (b.val == a.val && b.loc < a.loc)) a = b;
+  }
+};
+template <class T> struct RMinMax {
+  using V = MinMaxV<T>;
+  __device__ static V init() { return V{lim<T>::hi(), lim<T>::lo()}; }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t) {
+    v.min_val = (x < v.min_val) ? x : v.min_val;
+    v.max_val = (x > v.max_val) ? x : v.max_val;
+  }
+  __device__ static void join(V& a, const V& b) {
+    a.min_val = (b.min_val < a.min_val) ? b.min_val : a.min_val;
+    a.max_val = (b.max_val > a.max_val) ? b.max_val : a.max_val;
+  }
+};
+template <class T> struct RMinMaxLoc {
+  using V = MinMaxLocV<T>;
+  __device__ static V init() { return V{lim<T>::hi(), lim<T>::lo(), LOC_ID, LOC_ID}; }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t l) {
+    if (ORD) {
+      if (x < v.min_val) { v.min_val = x; v.min_loc = l; }
+      if (x > v.max_val) { v.max_val = x; v.max_loc = l; }
+    } else {
+      if (x < v.min_val || (x == v.min_val && v.min_loc != LOC_ID && l < v.min_loc)) { v.min_val = x; v.min_loc = l; }
+      if (x > v.max_val || (x == v.max_val && v.max_loc != LOC_ID && l < v.max_loc)) { v.max_val = x; v.max_loc = l; }
+    }
+  }
+  __device__ static void join(V& a, const V& b) {
+    if (b.min_val < a.min_val || (b.min_val == a.min_val && b.min_loc < a.min_loc)) { a.min_val = b.min_val; a.min_loc = b.min_loc; }
+    if (b.max_val > a.max_val || (b.max_val == a.max_val && b.max_loc < a.max_loc)) { a.max_val = b.max_val; a.max_loc = b.max_loc; }
+  }
+};
+
+// Warp tree.  32-bit integer Sum/Min/Max/BAnd/BOr use redux.sync (one
+// instruction); everything else a butterfly of shuffles.
+template <class R> struct WarpRed {
+  __device__ static typename R::V run(typename R::V v) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+      typename R::V o = shx(v, m);
+      R::join(v, o);
+    }
+    return v;
+  }
+};
+template <> struct WarpRed<RSum<int32_t>> { __device__ static int32_t run(int32_t v) { return (int32_t)__reduce_add_sync(0xffffffffu, (unsigned)v); } };
+template <> struct WarpRed<RSum<uint32_t>> { __device__ static uint32_t run(uint32_t v) { return __reduce_add_sync(0xffffffffu, v); } };
+template <> struct WarpRed<RMin<int32_t>> { __device__ static int32_t run(int32_t v) { return __reduce_min_sync(0xffffffffu, v); } };
+template <> struct WarpRed<RMin<uint32_t>> { __device__ static uint32_t run(uint32_t v) { return __reduce_min_sync(0xffffffffu, v); } };
+template <> struct WarpRed<RMax<int32_t>> { __device__ static int32_t run(int32_t v) { return __reduce_max_sync(0xffffffffu, v); } };
+template <> struct WarpRed<RMax<uint32_t>> { __device__ static uint32_t run(uint32_t v) { return __reduce_max_sync(0xffffffffu, v); } };
+template <> struct WarpRed<RBAnd<int32_t>> { __device__ static int32_t run(int32_t v) { return (int32_t)__reduce_and_sync(0xffffffffu, (unsigned)v); } };
+template <> struct WarpRed<RBAnd<uint32_t>> { __device__ static uint32_t run(uint32_t v) { return __reduce_and_sync(0xffffffffu, v); } };
+template <> struct WarpRed<RBOr<int32_t>> { __device__ static int32_t run(int32_t v) { return (int32_t)__reduce_or_sync(0xffffffffu, (unsigned)v); } };
+template <> struct WarpRed<RBOr<uint32_t>> { __device__ static uint32_t run(uint32_t v) { return __reduce_or_sync(0xffffffffu, v); } };
+
+// Block tree: result valid in thread 0.  `sm` holds BLOCK/32 values.
+template <class R, int BLOCK>
+__device__ __forceinline__ typename R::V block_reduce(typename R::V v, typename R::V* sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = WarpRed<R>::run(v);
+  if (lane == 0) sm[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = (lane < BLOCK / 32) ? sm[lane] : R::init();
+    v = WarpRed<R>::run(v);
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// 16-byte streaming load through the non-coherent path without L1
+// allocation, with a 256-byte L2 prefetch hint.  Only for data that no
+// thread writes during the kernel.
+__device__ __forceinline__ uint4 ld_stream16(const void* p) {
+  uint4 r;
+  asm("ld.global.nc.L1::no_allocate.L2::256B.v4.u32 {%0,%1,%2,%3}, [%4];"
+      : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+      : "l"(p));
+  return r;
+}
+
+template <class T>
+union Vec16 {
+  uint4 u;
+  T v[16 / sizeof(T)];
+};
+
+// Release store / acquire load at GPU scope (tile status words).
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_add_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+}  // namespace gbk
+
+#define GBK_CUDA_TRY(expr)                      \
+  do {                                          \
+    cudaError_t e_ = (expr);                    \
+    if (e_ != cudaSuccess) return gbk::cuda_status(e_); \
+  } while (0)

@@ -1,0 +1,287 @@
+// Reduce kernels: contiguous RangePolicy reduce and MDRange box reduce.
+//
+// Flat kernel (replaces the CUDA ParallelReduce<RangePolicy> of
+// core/src/Cuda/Kokkos_Cuda_Parallel_Range.hpp:191-368): a persistent grid
+// of SMs x ctas_per_sm CTAs walks tiles of BLOCK*UNROLL 16-byte vectors;
+// each thread keeps UNROLL independent 16-byte loads in flight
+// (ld.global.nc.L1::no_allocate with an L2 256-byte prefetch hint), folds
+// them into one running value with the reducer's element functor, then a
+// warp tree (redux.sync for 32-bit integer Sum/Min/Max/BAnd/BOr, shuffles
+// otherwise) and a CTA tree produce one partial per CTA.  The last CTA to
+// finish (ticket from one atomicAdd) combines the partials in CTA order and
+// writes the result: one launch, no second pass, no wait loop.  The
+// combine order is fixed by the grid, so results are deterministic for a
+// given configuration.
+//
+// MDRange kernel (replaces core/src/Cuda/Kokkos_Cuda_Parallel_MDRange.hpp:
+// 248-497): when the box is one contiguous range of memory (LayoutLeft or
+// LayoutRight view, box covering all but the slowest dimension) the host
+// collapses it to the flat kernel.  Otherwise each warp walks one row of
+// the dimension with the smallest stride at a time, lanes across the row.
+#pragma once
+
+#include "gbk_internal.cuh"
+
+namespace gbk {
+
+struct ReduceCfg {
+  int block, unroll, ctas_per_sm;
+};
+
+template <class V>
+__device__ __forceinline__ V ldcg_v(const V* p) {
+  static_assert(sizeof(V) % 4 == 0, "value size");
+  V r;
+  const unsigned* s = reinterpret_cast<const unsigned*>(p);
+  unsigned* d = reinterpret_cast<unsigned*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(V) / 4); ++i) d[i] = __ldcg(s + i);
+  return r;
+}
+
+// Combine this CTA's value into the grid result with the last-CTA pattern.
+template <class R, int BLOCK>
+__device__ __forceinline__ void grid_finish(typename R::V acc, typename R::V* partials, unsigned* counter,
+                                            typename R::V* out, typename R::V* sm) {
+  using V = typename R::V;
+  __shared__ unsigned s_ticket;
+  acc = block_reduce<R, BLOCK>(acc, sm);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = acc;
+    __threadfence();
+    s_ticket = atomicAdd(counter, 1u);
+  }
+  __syncthreads();
+  if (s_ticket != gridDim.x - 1) return;
+  __threadfence();
+  V a = R::init();
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += BLOCK) {
+    V p = ldcg_v(partials + i);
+    R::join(a, p);
+  }
+  __syncthreads();  // sm is reused by the second tree
+  a = block_reduce<R, BLOCK>(a, sm);
+  if (threadIdx.x == 0) {
+    *out = a;
+    *counter = 0u;  // ready for the next launch on this stream
+  }
+}
+
+template <class R, class T, int BLOCK, int UNROLL>
+__global__ void __launch_bounds__(BLOCK)
+    k_reduce_flat(const T* __restrict__ x, int64_t n, int64_t head, int64_t loc0, typename R::V* partials,
+                  unsigned* counter, typename R::V* out) {
+  using V = typename R::V;
+  constexpr int VEC = 16 / sizeof(T);
+  __shared__ V sm[BLOCK / 32];
+  V acc = R::init();
+  const int64_t gtid = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  const int64_t nthr = (int64_t)gridDim.x * BLOCK;
+  // Unaligned head [0, head): one element per thread.
+  if (gtid < head) R::template update<true>(acc, x[gtid], loc0 + gtid);
+  const T* xb = x + head;
+  const int64_t nvec = (n - head) / VEC;
+  constexpr int64_t TILE = (int64_t)BLOCK * UNROLL;
+  const int64_t ntile = nvec / TILE;
+  const int64_t lb = loc0 + head;
+  for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x) {
+    const int64_t vb = t * TILE + threadIdx.x;
+    Vec16<T> v[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) v[u].u = ld_stream16(xb + (vb + (int64_t)u * BLOCK) * VEC);
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const int64_t e0 = lb + (vb + (int64_t)u * BLOCK) * VEC;
+#pragma unroll
+      for (int k = 0; k < VEC; ++k) R::template update<true>(acc, v[u].v[k], e0 + k);
+    }
+  }
+  // Leftover whole vectors, spread over all threads.
+  for (int64_t vi = ntile * TILE + gtid; vi < nvec; vi += nthr) {
+    Vec16<T> v;
+    v.u = ld_stream16(xb + vi * VEC);
+#pragma unroll
+    for (int k = 0; k < VEC; ++k) R::template update<true>(acc, v.v[k], lb + vi * VEC + k);
+  }
+  // Tail elements after the last whole vector.
+  const int64_t t0 = head + nvec * VEC;
+  if (t0 + gtid < n) R::template update<true>(acc, x[t0 + gtid], loc0 + t0 + gtid);
+  grid_finish<R, BLOCK>(acc, partials, counter, out, sm);
+}
+
+template <class R>
+__global__ void k_write_identity(typename R::V* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *out = R::init();
+}
+
+struct MDBox {
+  int64_t lo[6], ext[6], stride[6];
+  int rank;    // number of outer dims in lo/ext/stride (inner dim removed)
+  int64_t inner_lo, inner_ext, inner_stride;
+  int64_t rows;
+};
+
+template <class R, class T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    k_reduce_md(const T* __restrict__ base, MDBox b, typename R::V* partials, unsigned* counter,
+                typename R::V* out) {
+  using V = typename R::V;
+  __shared__ V sm[BLOCK / 32];
+  V acc = R::init();
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * BLOCK) >> 5;
+  for (int64_t r = gw; r < b.rows; r += nw) {
+    int64_t rem = r, off = 0;
+    for (int d = 0; d < b.rank; ++d) {
+      const int64_t i = b.lo[d] + rem % b.ext[d];
+      rem /= b.ext[d];
+      off += i * b.stride[d];
+    }
+    for (int64_t i = lane; i < b.inner_ext; i += 32) {
+      const int64_t o = off + (b.inner_lo + i) * b.inner_stride;
+      R::template update<false>(acc, __ldg(base + o), o);
+    }
+  }
+  grid_finish<R, BLOCK>(acc, partials, counter, out, sm);
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+template <class R, class T, int BLOCK, int UNROLL>
+int launch_flat(const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, int ctas_per_sm) {
+  using V = typename R::V;
+  cudaStream_t s = w->stream;
+  if (n <= 0) {
+    k_write_identity<R><<<1, 32, 0, s>>>((V*)out);
+    note_launch();
+    return cuda_status(cudaGetLastError());
+  }
+  constexpr int VEC = 16 / sizeof(T);
+  const uintptr_t a = (uintptr_t)x;
+  int64_t head = (int64_t)(((16 - (a & 15)) & 15) / sizeof(T));
+  if (head > n) head = n;
+  const int64_t nvec = (n - head) / VEC;
+  const int64_t tiles = (nvec + (int64_t)BLOCK * UNROLL - 1) / ((int64_t)BLOCK * UNROLL);
+  int64_t grid = (int64_t)sm_count() * (ctas_per_sm > 0 ? ctas_per_sm : 4);
+  if (grid > tiles) grid = tiles;
+  if (grid < 1) grid = 1;
+  // head and tail are handled one element per thread: need enough threads.
+  const int64_t tail = (n - head) - nvec * VEC;
+  while (grid * BLOCK < head || grid * BLOCK < tail) ++grid;
+  int st = GBK_OK;
+  char* scr = ws_scratch(w, sizeof(V) * (size_t)grid + 256, &st);
+  if (!scr) return st;
+  k_reduce_flat<R, T, BLOCK, UNROLL><<<(unsigned)grid, BLOCK, 0, s>>>(x, n, head, loc0, (V*)scr,
+                                                                       w->counters + SLOT_REDUCE, (V*)out);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+template <class R, class T>
+int launch_flat_cfg(const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, const gbk_tuning_t* t) {
+  const int blk = t && t->block ? t->block : 256;
+  const int un = t && t->items_per_thread ? t->items_per_thread : 4;
+  const int cps = t && t->ctas_per_sm ? t->ctas_per_sm : (blk >= 512 ? 4 : 8);
+  // The configurations compiled for every reducer; others fall back to 256x4.
+  if (blk == 256 && un == 2) return launch_flat<R, T, 256, 2>(x, n, loc0, out, w, cps);
+  if (blk == 512 && un == 2) return launch_flat<R, T, 512, 2>(x, n, loc0, out, w, cps);
+  if (blk == 512 && un == 4) return launch_flat<R, T, 512, 4>(x, n, loc0, out, w, cps);
+  if (blk == 128 && un == 8) return launch_flat<R, T, 128, 8>(x, n, loc0, out, w, cps);
+  if (blk == 256 && un == 8) return launch_flat<R, T, 256, 8>(x, n, loc0, out, w, cps);
+  if (blk == 1024 && un == 2) return launch_flat<R, T, 1024, 2>(x, n, loc0, out, w, cps);
+  return launch_flat<R, T, 256, 4>(x, n, loc0, out, w, cps);
+}
+
+template <class R, class T>
+int launch_md(const T* base, const MDBox& b, void* out, Workspace* w, const gbk_tuning_t* t) {
+  using V = typename R::V;
+  cudaStream_t s = w->stream;
+  constexpr int BLOCK = 256;
+  int64_t total = b.rows * b.inner_ext;
+  if (total <= 0) {
+    k_write_identity<R><<<1, 32, 0, s>>>((V*)out);
+    note_launch();
+    return cuda_status(cudaGetLastError());
+  }
+  const int cps = t && t->ctas_per_sm ? t->ctas_per_sm : 8;
+  int64_t grid = (int64_t)sm_count() * cps;
+  const int64_t need = (b.rows + (BLOCK / 32) - 1) / (BLOCK / 32);
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  int st = GBK_OK;
+  char* scr = ws_scratch(w, sizeof(V) * (size_t)grid + 256, &st);
+  if (!scr) return st;
+  k_reduce_md<R, T, BLOCK><<<(unsigned)grid, BLOCK, 0, s>>>(base, b, (V*)scr, w->counters + SLOT_REDUCE, (V*)out);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+// Dispatch over reducers for one element type.
+template <class T>
+int reduce_typed(int op, const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, const gbk_tuning_t* t) {
+  constexpr bool INT = !(std::is_same<T, float>::value || std::is_same<T, double>::value);
+  switch (op) {
+    case GBK_SUM: return launch_flat_cfg<RSum<T>, T>(x, n, loc0, out, w, t);
+    case GBK_PROD: return launch_flat_cfg<RProd<T>, T>(x, n, loc0, out, w, t);
+    case GBK_MIN: return launch_flat_cfg<RMin<T>, T>(x, n, loc0, out, w, t);
+    case GBK_MAX: return launch_flat_cfg<RMax<T>, T>(x, n, loc0, out, w, t);
+    case GBK_MINLOC: return launch_flat_cfg<RMinLoc<T>, T>(x, n, loc0, out, w, t);
+    case GBK_MAXLOC: return launch_flat_cfg<RMaxLoc<T>, T>(x, n, loc0, out, w, t);
+    case GBK_MINMAX: return launch_flat_cfg<RMinMax<T>, T>(x, n, loc0, out, w, t);
+    case GBK_MINMAXLOC: return launch_flat_cfg<RMinMaxLoc<T>, T>(x, n, loc0, out, w, t);
+    default: break;
+  }
+  if constexpr (INT) {
+    switch (op) {
+      case GBK_LAND: return launch_flat_cfg<RLAnd<T>, T>(x, n, loc0, out, w, t);
+      case GBK_LOR: return launch_flat_cfg<RLOr<T>, T>(x, n, loc0, out, w, t);
+      case GBK_BAND: return launch_flat_cfg<RBAnd<T>, T>(x, n, loc0, out, w, t);
+      case GBK_BOR: return launch_flat_cfg<RBOr<T>, T>(x, n, loc0, out, w, t);
+      default: break;
+    }
+  }
+  return GBK_ERR_UNSUPPORTED;
+}
+
+template <class T>
+int mdreduce_typed(int op, const T* base, const MDBox& b, void* out, Workspace* w, const gbk_tuning_t* t) {
+  constexpr bool INT = !(std::is_same<T, float>::value || std::is_same<T, double>::value);
+  switch (op) {
+    case GBK_SUM: return launch_md<RSum<T>, T>(base, b, out, w, t);
+    case GBK_PROD: return launch_md<RProd<T>, T>(base, b, out, w, t);
+    case GBK_MIN: return launch_md<RMin<T>, T>(base, b, out, w, t);
+    case GBK_MAX: return launch_md<RMax<T>, T>(base, b, out, w, t);
+    case GBK_MINLOC: return launch_md<RMinLoc<T>, T>(base, b, out, w, t);
+    case GBK_MAXLOC: return launch_md<RMaxLoc<T>, T>(base, b, out, w, t);
+    case GBK_MINMAX: return launch_md<RMinMax<T>, T>(base, b, out, w, t);
+    case GBK_MINMAXLOC: return launch_md<RMinMaxLoc<T>, T>(base, b, out, w, t);
+    default: break;
+  }
+  if constexpr (INT) {
+    switch (op) {
+      case GBK_LAND: return launch_md<RLAnd<T>, T>(base, b, out, w, t);
+      case GBK_LOR: return launch_md<RLOr<T>, T>(base, b, out, w, t);
+      case GBK_BAND: return launch_md<RBAnd<T>, T>(base, b, out, w, t);
+      case GBK_BOR: return launch_md<RBOr<T>, T>(base, b, out, w, t);
+      default: break;
+    }
+  }
+  return GBK_ERR_UNSUPPORTED;
+}
+
+// Explicitly instantiated in gbk_reduce_<dtype>.cu.
+extern template int reduce_typed<int32_t>(int, const int32_t*, int64_t, int64_t, void*, Workspace*, const gbk_tuning_t*);
+extern template int reduce_typed<int64_t>(int, const int64_t*, int64_t, int64_t, void*, Workspace*, const gbk_tuning_t*);
+extern template int reduce_typed<uint32_t>(int, const uint32_t*, int64_t, int64_t, void*, Workspace*, const gbk_tuning_t*);
+extern template int reduce_typed<uint64_t>(int, const uint64_t*, int64_t, int64_t, void*, Workspace*, const gbk_tuning_t*);
+extern template int reduce_typed<float>(int, const float*, int64_t, int64_t, void*, Workspace*, const gbk_tuning_t*);
+extern template int reduce_typed<double>(int, const double*, int64_t, int64_t, void*, Workspace*, const gbk_tuning_t*);
+extern template int mdreduce_typed<int32_t>(int, const int32_t*, const MDBox&, void*, Workspace*, const gbk_tuning_t*);
+extern template int mdreduce_typed<int64_t>(int, const int64_t*, const MDBox&, void*, Workspace*, const gbk_tuning_t*);
+extern template int mdreduce_typed<uint32_t>(int, const uint32_t*, const MDBox&, void*, Workspace*, const gbk_tuning_t*);
+extern template int mdreduce_typed<uint64_t>(int, const uint64_t*, const MDBox&, void*, Workspace*, const gbk_tuning_t*);
+extern template int mdreduce_typed<float>(int, const float*, const MDBox&, void*, Workspace*, const gbk_tuning_t*);
+extern template int mdreduce_typed<double>(int, const double*, const MDBox&, void*, Workspace*, const gbk_tuning_t*);
+
+}  // namespace gbk

@@ -1,0 +1,229 @@
+// Runtime of libgbk: per-stream workspaces, the device error word, device
+// queries, wait limits and the launch counter.
+//
+// One Workspace per (device, stream), created on first use and guarded by
+// its own mutex; launches on one stream are serialised by the stream, as
+// the reference serialises kernels on one OpenMP instance with its instance
+// mutex (core/src/OpenMP/Kokkos_OpenMP_Parallel_Reduce.hpp:87).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "gbk_internal.cuh"
+
+namespace gbk {
+
+namespace {
+std::mutex g_mu;
+std::map<std::pair<int, cudaStream_t>, Workspace*> g_ws;
+std::atomic<int64_t> g_launches{0};
+std::atomic<int64_t> g_wait_limit{int64_t(1) << 22};  // polls with ~256 ns back-off: about a second
+int g_sm[64];
+bool g_sm_init[64];
+
+bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &st) != cudaSuccess) return false;
+  return st != cudaStreamCaptureStatusNone;
+}
+}  // namespace
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return GBK_OK;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GBK_ERR_NO_DEVICE;
+  return GBK_ERR_CUDA;
+}
+
+int sm_count() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (dev < 0 || dev >= 64) return 0;
+  if (!g_sm_init[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    g_sm[dev] = v;
+    g_sm_init[dev] = true;
+  }
+  return g_sm[dev];
+}
+
+int64_t wait_limit() { return g_wait_limit.load(); }
+void note_launch(int64_t k) { g_launches += k; }
+
+Workspace* ws_get(cudaStream_t s, int* status) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) { *status = cuda_status(e); return nullptr; }
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto key = std::make_pair(dev, s);
+  auto it = g_ws.find(key);
+  if (it != g_ws.end()) return it->second;
+  if (capturing(s)) { *status = GBK_ERR_OUT_OF_WORKSPACE; return nullptr; }
+  Workspace* w = new Workspace();
+  w->stream = s;
+  w->device = dev;
+  void* p = nullptr;
+  e = cudaMalloc(&p, 64 * sizeof(unsigned) + 256);
+  if (e != cudaSuccess) { delete w; *status = cuda_status(e); return nullptr; }
+  e = cudaMemset(p, 0, 64 * sizeof(unsigned) + 256);
+  if (e != cudaSuccess) { cudaFree(p); delete w; *status = cuda_status(e); return nullptr; }
+  w->counters = (unsigned*)p;
+  w->err = (int*)((char*)p + 64 * sizeof(unsigned));
+  g_ws[key] = w;
+  return w;
+}
+
+static char* grow(Workspace* w, char** buf, size_t* have, size_t bytes, int* status) {
+  if (bytes <= *have) return *buf;
+  if (capturing(w->stream)) { *status = GBK_ERR_OUT_OF_WORKSPACE; return nullptr; }
+  // The old buffer may still be in use by queued work on this stream.
+  cudaError_t e = cudaStreamSynchronize(w->stream);
+  if (e != cudaSuccess) { *status = cuda_status(e); return nullptr; }
+  if (*buf) cudaFree(*buf);
+  *buf = nullptr;
+  *have = 0;
+  size_t want = bytes + bytes / 4 + (1u << 20);
+  void* p = nullptr;
+  e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) { *status = cuda_status(e); return nullptr; }
+  // Scratch starts zeroed: tile-status words rely on it.
+  e = cudaMemset(p, 0, want);
+  if (e != cudaSuccess) { cudaFree(p); *status = cuda_status(e); return nullptr; }
+  *buf = (char*)p;
+  *have = want;
+  return *buf;
+}
+
+char* ws_scratch(Workspace* w, size_t bytes, int* status) {
+  return grow(w, &w->scratch, &w->scratch_bytes, bytes, status);
+}
+char* ws_stage(Workspace* w, size_t bytes, int* status) { return grow(w, &w->stage, &w->stage_bytes, bytes, status); }
+
+unsigned* ws_flags(Workspace* w, size_t count, unsigned* epoch, int* status) {
+  const size_t had = w->flags_bytes;
+  char* f = grow(w, &w->flags, &w->flags_bytes, count * sizeof(unsigned), status);
+  if (!f) return nullptr;
+  w->epoch = (w->epoch + 1) & 0x3FFFFFFFu;
+  if (w->epoch == 0 || w->flags_bytes != had) {
+    // Fresh (zeroed) buffer or wrapped epoch space: zero is never a valid tag.
+    if (w->epoch == 0) {
+      cudaError_t e = cudaMemsetAsync(f, 0, w->flags_bytes, w->stream);
+      if (e != cudaSuccess) { *status = cuda_status(e); return nullptr; }
+    }
+    if (w->epoch == 0) w->epoch = 1;
+  }
+  *epoch = w->epoch;
+  return (unsigned*)f;
+}
+
+}  // namespace gbk
+
+using namespace gbk;
+
+extern "C" {
+
+int gbk_version(void) { return 100; }
+
+const char* gbk_status_string(int s) {
+  switch (s) {
+    case GBK_OK: return "ok";
+    case GBK_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GBK_ERR_UNSUPPORTED: return "unsupported reducer/dtype combination";
+    case GBK_ERR_CUDA: return "CUDA error";
+    case GBK_ERR_DEVICE_TIMEOUT: return "device-side wait exceeded its bound";
+    case GBK_ERR_OUT_OF_WORKSPACE: return "workspace too small (reserve it before stream capture)";
+    case GBK_ERR_KEY_OUT_OF_RANGE: return "key outside the bin range (skipped)";
+    case GBK_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+int gbk_device_info(int* sm, int* major, int* minor, int64_t* l2) {
+  int dev = 0;
+  GBK_CUDA_TRY(cudaGetDevice(&dev));
+  int v = 0;
+  if (sm) { GBK_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev)); *sm = v; }
+  if (major) { GBK_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMajor, dev)); *major = v; }
+  if (minor) { GBK_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMinor, dev)); *minor = v; }
+  if (l2) { GBK_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev)); *l2 = v; }
+  return GBK_OK;
+}
+
+int gbk_stream_check(gbk_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  GBK_CUDA_TRY(cudaStreamSynchronize(s));
+  int st = GBK_OK;
+  Workspace* w = ws_get(s, &st);
+  if (!w) return st;
+  int bits = 0;
+  GBK_CUDA_TRY(cudaMemcpy(&bits, w->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (bits) {
+    int zero = 0;
+    GBK_CUDA_TRY(cudaMemcpy(w->err, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    // After a timed-out wait the ticket counters may be left non-zero.
+    if (bits & (GBK_EBIT_TIMEOUT | GBK_EBIT_BAD_STATE)) {
+      GBK_CUDA_TRY(cudaMemset(w->counters, 0, 64 * sizeof(unsigned)));
+      if (w->scratch) GBK_CUDA_TRY(cudaMemset(w->scratch, 0, w->scratch_bytes));
+    }
+  }
+  if (bits & GBK_EBIT_TIMEOUT) return GBK_ERR_DEVICE_TIMEOUT;
+  if (bits & GBK_EBIT_BAD_STATE) return GBK_ERR_CUDA;
+  if (bits & GBK_EBIT_KEY_RANGE) return GBK_ERR_KEY_OUT_OF_RANGE;
+  return GBK_OK;
+}
+
+int gbk_workspace_reserve(gbk_stream_t stream, int64_t bytes) {
+  if (bytes < 0) return GBK_ERR_INVALID_ARGUMENT;
+  int st = GBK_OK;
+  Workspace* w = ws_get((cudaStream_t)stream, &st);
+  if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->mu);
+  if (!ws_scratch(w, (size_t)bytes, &st)) return st;
+  return GBK_OK;
+}
+
+int gbk_workspace_release_all(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& kv : g_ws) {
+    Workspace* w = kv.second;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(w->device);
+    cudaStreamSynchronize(w->stream);
+    if (w->counters) cudaFree(w->counters);
+    if (w->scratch) cudaFree(w->scratch);
+    if (w->stage) cudaFree(w->stage);
+    if (w->flags) cudaFree(w->flags);
+    cudaSetDevice(cur);
+    delete w;
+  }
+  g_ws.clear();
+  return GBK_OK;
+}
+
+int gbk_set_wait_limit(int64_t polls) {
+  if (polls < 1) return GBK_ERR_INVALID_ARGUMENT;
+  g_wait_limit = polls;
+  return GBK_OK;
+}
+
+int64_t gbk_launch_count(void) { return g_launches.load(); }
+
+int gbk_deep_copy(void* dst, const void* src, int64_t bytes, gbk_stream_t stream) {
+  if (bytes < 0 || (bytes > 0 && (!dst || !src))) return GBK_ERR_INVALID_ARGUMENT;
+  if (bytes == 0) return GBK_OK;
+  GBK_CUDA_TRY(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDefault, (cudaStream_t)stream));
+  return GBK_OK;
+}
+
+int gbk_memset(void* dst, int value, int64_t bytes, gbk_stream_t stream) {
+  if (bytes < 0 || (bytes > 0 && !dst)) return GBK_ERR_INVALID_ARGUMENT;
+  if (bytes == 0) return GBK_OK;
+  GBK_CUDA_TRY(cudaMemsetAsync(dst, value, (size_t)bytes, (cudaStream_t)stream));
+  return GBK_OK;
+}
+
+}  // extern "C"

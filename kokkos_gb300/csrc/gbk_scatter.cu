@@ -1,0 +1,337 @@
+// ScatterView contributions: histogram and general scatter-op.
+//
+// The reference's CUDA default is NonDuplicated + Atomic: one global
+// atom.add per contribution (containers/src/Kokkos_ScatterView.hpp:152-165,
+// :250-286 -> desul device_atomic_fetch_add).  Here the histogram instead
+// privatises the bins in shared memory:
+//   * CL = 1: each CTA holds all bins (u32 counters) and counts with
+//     shared-memory atomics.
+//   * CL > 1: the bins are split across the CL CTAs of a thread-block
+//     cluster (bin b lives in CTA b % CL at slot b / CL); a key's count goes
+//     to its owner's shared memory through distributed shared memory
+//     (mapa + red.shared::cluster).  2^16 int64 bins need 256 KiB of u32
+//     counters, more than one CTA has, but fit a 2-CTA cluster.
+//   * AGG: warp aggregation first (match.any groups equal keys, the lowest
+//     lane adds the group size), which removes same-address conflicts on the
+//     hot bins of skewed (Zipf) keys.
+// At the end every CTA adds its non-zero counters into the int64 bins with
+// fire-and-forget red.global.add.u64.  Counts are exact integers, so the
+// result is bit-exact whatever the order.  No CTA ever waits on another
+// except at the cluster barriers, which the hardware co-schedules.
+#include <cooperative_groups.h>
+
+#include "gbk_internal.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace gbk {
+namespace {
+
+__device__ __forceinline__ void dsmem_add(uint32_t local_addr, unsigned owner, unsigned v) {
+  uint32_t ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(local_addr), "r"(owner));
+  asm volatile("red.shared::cluster.add.u32 [%0], %1;" ::"r"(ra), "r"(v) : "memory");
+}
+
+template <int CL, bool AGG>
+__device__ __forceinline__ void count_key(int32_t k, int64_t nbins, unsigned* sh, uint32_t sh_base, bool& bad) {
+  const bool ok = (uint32_t)k < (uint64_t)nbins;
+  if (!ok) bad = true;
+  unsigned add = 1;
+  bool leader = ok;
+  if (AGG) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, ok ? k : -1);
+    leader = ok && ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1));
+    add = __popc(peers);
+  }
+  if (!leader) return;
+  if (CL == 1) {
+    atomicAdd(sh + k, add);
+  } else {
+    const unsigned owner = (unsigned)k % CL;
+    const unsigned slot = (unsigned)k / CL;
+    dsmem_add(sh_base + 4u * slot, owner, add);
+  }
+}
+
+template <int CL, int BLOCK, bool AGG>
+__global__ void __launch_bounds__(BLOCK)
+    k_hist_priv(const int32_t* __restrict__ keys, int64_t n, int64_t nbins, unsigned long long* bins, int* err) {
+  extern __shared__ __align__(16) unsigned sh[];
+  const int per = (int)((nbins + CL - 1) / CL);
+  for (int i = threadIdx.x; i < per; i += BLOCK) sh[i] = 0u;
+  unsigned rank = 0;
+  if constexpr (CL > 1) {
+    cg::cluster_group cl = cg::this_cluster();
+    rank = cl.block_rank();
+    cl.sync();
+  } else {
+    __syncthreads();
+  }
+  const uint32_t sh_base = (uint32_t)__cvta_generic_to_shared(sh);
+  bool bad = false;
+  const int64_t g = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * BLOCK;
+  const uintptr_t a = (uintptr_t)keys;
+  int64_t head = (int64_t)(((16 - (a & 15)) & 15) / 4);
+  if (head > n) head = n;
+  if (g < head) count_key<CL, AGG>(keys[g], nbins, sh, sh_base, bad);
+  const int32_t* kb = keys + head;
+  const int64_t nvec = (n - head) / 4;
+  int64_t v = g;
+  for (; v + stride < nvec; v += 2 * stride) {
+    Vec16<int32_t> u0, u1;
+    u0.u = ld_stream16(kb + 4 * v);
+    u1.u = ld_stream16(kb + 4 * (v + stride));
+#pragma unroll
+    for (int j = 0; j < 4; ++j) count_key<CL, AGG>(u0.v[j], nbins, sh, sh_base, bad);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) count_key<CL, AGG>(u1.v[j], nbins, sh, sh_base, bad);
+  }
+  for (; v < nvec; v += stride) {
+    Vec16<int32_t> u0;
+    u0.u = ld_stream16(kb + 4 * v);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) count_key<CL, AGG>(u0.v[j], nbins, sh, sh_base, bad);
+  }
+  const int64_t t0 = head + nvec * 4;
+  if (t0 + g < n) count_key<CL, AGG>(keys[t0 + g], nbins, sh, sh_base, bad);
+  if constexpr (CL > 1) {
+    cg::this_cluster().sync();
+  } else {
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < per; i += BLOCK) {
+    const unsigned c = sh[i];
+    const int64_t b = (int64_t)i * CL + rank;
+    if (c && b < nbins) red_add_u64(bins + b, (unsigned long long)c);
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, GBK_EBIT_KEY_RANGE);
+}
+
+// No privatisation (bins too many for the cluster's shared memory): warp-
+// aggregated global reductions.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    k_hist_global(const int32_t* __restrict__ keys, int64_t n, int64_t nbins, unsigned long long* bins, int* err) {
+  bool bad = false;
+  for (int64_t i = (int64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (int64_t)gridDim.x * BLOCK) {
+    const int32_t k = keys[i];
+    const bool ok = (uint32_t)k < (uint64_t)nbins;
+    if (!ok) bad = true;
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, ok ? k : -1);
+    if (ok && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) red_add_u64(bins + k, (unsigned long long)__popc(peers));
+  }
+  if (bad) atomicOr(err, GBK_EBIT_KEY_RANGE);
+}
+
+template <int CL, int BLOCK, bool AGG>
+int launch_priv(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, Workspace* w, int ctas_per_sm) {
+  const size_t smem = (size_t)((nbins + CL - 1) / CL) * 4;
+  auto kfn = k_hist_priv<CL, BLOCK, AGG>;
+  GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 1) GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cfg.blockDim = dim3(BLOCK);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = w->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  // One wave of co-resident clusters (the count the hardware can place at
+  // once), capped by ctas_per_sm and by the work.
+  int64_t grid = (int64_t)sm_count() * (ctas_per_sm > 0 ? ctas_per_sm : 1);
+  cfg.gridDim = dim3((unsigned)grid);
+  int ncl = 0;
+  if (cudaOccupancyMaxActiveClusters(&ncl, kfn, &cfg) == cudaSuccess && ncl > 0 && (int64_t)ncl * CL < grid)
+    grid = (int64_t)ncl * CL;
+  const int64_t need = (n + (int64_t)BLOCK * 8 - 1) / ((int64_t)BLOCK * 8);
+  if (grid > need) grid = need;
+  if (grid < CL) grid = CL;
+  grid = grid / CL * CL;
+  // Each cluster counts in u32: keep keys per cluster below 2^32.
+  while (n / (grid / CL) >= (int64_t)0xFFFFFFFFLL) grid += CL;
+  cfg.gridDim = dim3((unsigned)grid);
+  GBK_CUDA_TRY(cudaLaunchKernelEx(&cfg, kfn, keys, n, nbins, (unsigned long long*)bins, w->err));
+  note_launch();
+  return GBK_OK;
+}
+
+int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Workspace* w, const gbk_tuning_t* t) {
+  if (n == 0) return GBK_OK;
+  int cl = t && t->variant ? (t->variant & 0xF) : 0;  // cluster size; 0 = auto
+  const bool agg = t ? ((t->variant & 0x10) != 0) : false;
+  const int cps = t && t->ctas_per_sm ? t->ctas_per_sm : 1;
+  const int64_t max_smem = 200 * 1024;
+  if (cl == 0) {
+    cl = 1;
+    while (cl <= 8 && (nbins + cl - 1) / cl * 4 > max_smem) cl *= 2;
+    if (cl == 1 && nbins * 4 > 96 * 1024) cl = 2;
+  }
+  if ((nbins + cl - 1) / cl * 4 > max_smem || cl > 8) {
+    int64_t grid = (int64_t)sm_count() * 8;
+    k_hist_global<256><<<(unsigned)grid, 256, 0, w->stream>>>(keys, n, nbins, (unsigned long long*)bins, w->err);
+    note_launch();
+    return cuda_status(cudaGetLastError());
+  }
+#define GBK_HL(C, A) return launch_priv<C, 1024, A>(keys, n, nbins, bins, w, cps)
+  switch (cl) {
+    case 1: if (agg) GBK_HL(1, true); else GBK_HL(1, false);
+    case 2: if (agg) GBK_HL(2, true); else GBK_HL(2, false);
+    case 4: if (agg) GBK_HL(4, true); else GBK_HL(4, false);
+    case 8: if (agg) GBK_HL(8, true); else GBK_HL(8, false);
+  }
+#undef GBK_HL
+  return GBK_ERR_INVALID_ARGUMENT;
+}
+
+// ---- general scatter -------------------------------------------------------
+template <class T> struct AtomOps;
+template <> struct AtomOps<int32_t> {
+  __device__ static void add(int32_t* p, int32_t v) { atomicAdd(p, v); }
+  __device__ static void mn(int32_t* p, int32_t v) { atomicMin(p, v); }
+  __device__ static void mx(int32_t* p, int32_t v) { atomicMax(p, v); }
+};
+template <> struct AtomOps<uint32_t> {
+  __device__ static void add(uint32_t* p, uint32_t v) { atomicAdd(p, v); }
+  __device__ static void mn(uint32_t* p, uint32_t v) { atomicMin(p, v); }
+  __device__ static void mx(uint32_t* p, uint32_t v) { atomicMax(p, v); }
+};
+template <> struct AtomOps<int64_t> {
+  __device__ static void add(int64_t* p, int64_t v) { atomicAdd((unsigned long long*)p, (unsigned long long)v); }
+  __device__ static void mn(int64_t* p, int64_t v) { atomicMin((long long*)p, (long long)v); }
+  __device__ static void mx(int64_t* p, int64_t v) { atomicMax((long long*)p, (long long)v); }
+};
+template <> struct AtomOps<uint64_t> {
+  __device__ static void add(uint64_t* p, uint64_t v) { atomicAdd((unsigned long long*)p, (unsigned long long)v); }
+  __device__ static void mn(uint64_t* p, uint64_t v) { atomicMin((unsigned long long*)p, (unsigned long long)v); }
+  __device__ static void mx(uint64_t* p, uint64_t v) { atomicMax((unsigned long long*)p, (unsigned long long)v); }
+};
+template <class T, class F>
+__device__ void cas_loop(T* p, F f) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "size");
+  using U = typename std::conditional<sizeof(T) == 4, unsigned, unsigned long long>::type;
+  U* up = reinterpret_cast<U*>(p);
+  U old = *reinterpret_cast<volatile U*>(up), assumed;
+  do {
+    assumed = old;
+    T cur;
+    memcpy(&cur, &assumed, sizeof(T));
+    const T nv = f(cur);
+    U nu;
+    memcpy(&nu, &nv, sizeof(T));
+    if (nu == assumed) return;
+    old = atomicCAS(up, assumed, nu);
+  } while (old != assumed);
+}
+template <> struct AtomOps<float> {
+  __device__ static void add(float* p, float v) { atomicAdd(p, v); }
+  __device__ static void mn(float* p, float v) { cas_loop(p, [v](float c) { return v < c ? v : c; }); }
+  __device__ static void mx(float* p, float v) { cas_loop(p, [v](float c) { return v > c ? v : c; }); }
+};
+template <> struct AtomOps<double> {
+  __device__ static void add(double* p, double v) { atomicAdd(p, v); }
+  __device__ static void mn(double* p, double v) { cas_loop(p, [v](double c) { return v < c ? v : c; }); }
+  __device__ static void mx(double* p, double v) { cas_loop(p, [v](double c) { return v > c ? v : c; }); }
+};
+
+template <class T, int OP>
+__global__ void k_scatter(const int32_t* __restrict__ idx, const T* __restrict__ vals, int64_t n, T* dest,
+                          int64_t ndest, int* err) {
+  bool bad = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t k = idx[i];
+    if ((uint32_t)k >= (uint64_t)ndest) { bad = true; continue; }
+    const T v = vals[i];
+    if (OP == GBK_SUM) AtomOps<T>::add(dest + k, v);
+    else if (OP == GBK_MIN) AtomOps<T>::mn(dest + k, v);
+    else if (OP == GBK_MAX) AtomOps<T>::mx(dest + k, v);
+    else cas_loop(dest + k, [v](T c) { return c * v; });
+  }
+  if (bad) atomicOr(err, GBK_EBIT_KEY_RANGE);
+}
+
+template <class T>
+int scatter_t(int op, const int32_t* idx, const void* vals, int64_t n, void* dest, int64_t nd, Workspace* w) {
+  if (n == 0) return GBK_OK;
+  int64_t grid = (n + 255) / 256;
+  const int64_t cap = (int64_t)sm_count() * 8;
+  if (grid > cap) grid = cap;
+  const T* v = (const T*)vals;
+  T* d = (T*)dest;
+  switch (op) {
+    case GBK_SUM: k_scatter<T, GBK_SUM><<<(unsigned)grid, 256, 0, w->stream>>>(idx, v, n, d, nd, w->err); break;
+    case GBK_PROD: k_scatter<T, GBK_PROD><<<(unsigned)grid, 256, 0, w->stream>>>(idx, v, n, d, nd, w->err); break;
+    case GBK_MIN: k_scatter<T, GBK_MIN><<<(unsigned)grid, 256, 0, w->stream>>>(idx, v, n, d, nd, w->err); break;
+    case GBK_MAX: k_scatter<T, GBK_MAX><<<(unsigned)grid, 256, 0, w->stream>>>(idx, v, n, d, nd, w->err); break;
+    default: return GBK_ERR_UNSUPPORTED;
+  }
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+}  // namespace
+}  // namespace gbk
+
+using namespace gbk;
+
+extern "C" {
+
+int gbk_histogram_i32_i64(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, gbk_stream_t stream,
+                          const gbk_tuning_t* tune) {
+  if (n < 0 || nbins <= 0 || nbins > 0x7FFFFFFF || !bins || (n > 0 && !keys)) return GBK_ERR_INVALID_ARGUMENT;
+  if ((uintptr_t)keys % 4 || (uintptr_t)bins % 8) return GBK_ERR_INVALID_ARGUMENT;
+  int st = GBK_OK;
+  Workspace* w = ws_get((cudaStream_t)stream, &st);
+  if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->mu);
+  return hist_launch(keys, n, bins, nbins, w, tune);
+}
+
+int gbk_histogram_i32_i64_host(const int32_t* hkeys, int64_t n, int64_t* hbins, int64_t nbins, gbk_stream_t stream,
+                               const gbk_tuning_t* tune) {
+  if (n < 0 || nbins <= 0 || nbins > 0x7FFFFFFF || !hbins || (n > 0 && !hkeys)) return GBK_ERR_INVALID_ARGUMENT;
+  int st = GBK_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  Workspace* w = ws_get(s, &st);
+  if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->mu);
+  const size_t kb = ((size_t)n * 4 + 255) / 256 * 256;
+  char* d = ws_stage(w, kb + (size_t)nbins * 8 + 256, &st);
+  if (!d) return st;
+  int64_t* db = (int64_t*)(d + kb);
+  if (n) GBK_CUDA_TRY(cudaMemcpyAsync(d, hkeys, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  GBK_CUDA_TRY(cudaMemcpyAsync(db, hbins, (size_t)nbins * 8, cudaMemcpyHostToDevice, s));
+  st = hist_launch((const int32_t*)d, n, db, nbins, w, tune);
+  if (st) return st;
+  GBK_CUDA_TRY(cudaMemcpyAsync(hbins, db, (size_t)nbins * 8, cudaMemcpyDeviceToHost, s));
+  GBK_CUDA_TRY(cudaStreamSynchronize(s));
+  return GBK_OK;
+}
+
+int gbk_scatter(gbk_reducer_t op, gbk_dtype_t dt, const int32_t* idx, const void* vals, int64_t n, void* dest,
+                int64_t nd, gbk_stream_t stream) {
+  if (n < 0 || nd < 0 || (n > 0 && (!idx || !vals || !dest))) return GBK_ERR_INVALID_ARGUMENT;
+  if (op != GBK_SUM && op != GBK_PROD && op != GBK_MIN && op != GBK_MAX) return GBK_ERR_UNSUPPORTED;
+  int st = GBK_OK;
+  Workspace* w = ws_get((cudaStream_t)stream, &st);
+  if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->mu);
+  switch (dt) {
+    case GBK_I32: return scatter_t<int32_t>(op, idx, vals, n, dest, nd, w);
+    case GBK_I64: return scatter_t<int64_t>(op, idx, vals, n, dest, nd, w);
+    case GBK_U32: return scatter_t<uint32_t>(op, idx, vals, n, dest, nd, w);
+    case GBK_U64: return scatter_t<uint64_t>(op, idx, vals, n, dest, nd, w);
+    case GBK_F32: return scatter_t<float>(op, idx, vals, n, dest, nd, w);
+    case GBK_F64: return scatter_t<double>(op, idx, vals, n, dest, nd, w);
+  }
+  return GBK_ERR_UNSUPPORTED;
+}
+
+}  // extern "C"

@@ -1,0 +1,214 @@
+"""Parity of the GPU reduce / MDRange reduce (through the C ABI) with the
+oracle and with the reference's own golden outputs."""
+import os
+
+import numpy as np
+import pytest
+
+from tests._util import prod_ok, sum_ok, sum_tol
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+INT_OPS = ["sum", "prod", "min", "max", "land", "lor", "band", "bor", "minloc", "maxloc", "minmax", "minmaxloc"]
+FLT_OPS = ["sum", "prod", "min", "max", "minloc", "maxloc", "minmax", "minmaxloc"]
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+
+    from kokkos_gb300 import gbk
+    torch.cuda.set_device(0)
+    return gbk, torch
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def compare(op, got, want, x):
+    """got/want: numpy scalars / structured records of the reducer layout."""
+    names = got.dtype.names
+    fl = x.dtype.kind == "f"
+    if op == "sum" and fl:
+        ok, info = sum_ok(got, x, sum_tol(x.dtype))
+        assert ok, info
+        return
+    if op == "prod" and fl:
+        ok, info = prod_ok(got, x)
+        assert ok, info
+        return
+    if names:
+        for nm in names:
+            assert np.asarray(got[nm]).tobytes() == np.asarray(want[nm]).tobytes(), (op, nm, got, want)
+    else:
+        assert np.asarray(got).tobytes() == np.asarray(want).tobytes(), (op, got, want)
+
+
+def test_golden_reducers_all_dtypes(env):
+    """GPU result vs the reference's own output for every reducer x dtype x
+    size in the golden set (floats within the stated tolerances)."""
+    gbk, torch = env
+    G = np.load(GOLDEN)
+    cases = sorted({k.rsplit("/", 2)[0] for k in G.files if k.startswith("reduce/") and k.endswith("/out")})
+    assert len(cases) > 200
+    for c in cases:
+        _, op, dt, n = c.split("/")
+        x = G[c + "/x"]
+        want = np.frombuffer(G[c + "/4/out"].tobytes(), dtype=gbk.result_dtype(gbk.OPS[op], gbk.DT[{
+            "int32": "i32", "int64": "i64", "uint32": "u32", "uint64": "u64", "float32": "f32", "float64": "f64"}[dt]]))[0]
+        got = gbk.reduce_value(op, _dev(torch, x))
+        compare(op, got, want, x)
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int64, np.uint32, np.uint64, np.float32, np.float64])
+@pytest.mark.parametrize("n", [0, 1, 3, 33, 4097, (1 << 20) + 5])
+def test_reducers_vs_oracle(env, dtype, n):
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    t = np.dtype(dtype)
+    if t.kind == "f":
+        x = datagen.normal_f64(n, seed=n).astype(t)
+    elif t.kind == "i":
+        x = datagen.uniform_i64(n, -1000, 1000, seed=n).astype(t)
+    else:
+        x = datagen.uniform_i64(n, 0, 100000, seed=n).astype(t)
+    ops = FLT_OPS if t.kind == "f" else INT_OPS
+    for op in ops:
+        xx = x
+        if op == "prod":
+            xx = np.ones(n, dtype=t) if t.kind != "f" else (1 + 1e-4 * datagen.normal_f64(n, seed=1)).astype(t)
+            if n > 2 and t.kind != "f":
+                xx[n // 3] = 3
+                xx[n // 2] = 2
+        if op in ("land", "lor"):
+            xx = (x % 5 != 0).astype(t) if op == "land" else (x % 997 == 3).astype(t)
+        d = _dev(torch, xx)
+        got = gbk.reduce_value(op, d)
+        want = oracle.reduce(op, xx, 4)
+        compare(op, got, want, xx)
+
+
+@pytest.mark.parametrize("offset", [1, 2, 3])
+def test_misaligned_views(env, offset):
+    """Views that start off a 16-byte boundary (subviews) take the scalar
+    head path."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    base = datagen.uniform_i32(100003, -50, 50, seed=7)
+    d = _dev(torch, base)
+    sub = d[offset:]
+    for op in ("sum", "minloc", "maxloc", "minmaxloc"):
+        got = gbk.reduce_value(op, sub)
+        want = oracle.reduce(op, base[offset:], 1)
+        compare(op, got, want, base[offset:])
+
+
+def test_c1_sum_f64_full_size(env):
+    """parallel_reduce Sum over View<double*> 2^24 uniform[0,1), seed 0:
+    rel err <= 1e-12 vs the compensated FP64 sum."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    x = datagen.uniform_f64(1 << 24, seed=0)
+    got = gbk.reduce_value("sum", _dev(torch, x))
+    ok, info = sum_ok(got, x, 1e-12)
+    assert ok, info
+    import oracle
+    s, _, _ = oracle.sum_compensated(x)
+    assert abs(float(got) - s) <= 1e-12 * abs(s)
+
+
+def test_c2_mdrange_full_size(env):
+    """MDRangePolicy<Rank<3>> MinLoc / MaxLoc / Sum over LayoutLeft
+    View<float***> 512x512x256 of N(0,1); the extremum is unique, so value
+    and loc are exact."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    n0, n1, n2 = 512, 512, 256
+    x = datagen.normal_f32(n0 * n1 * n2, seed=0)
+    d = _dev(torch, x)
+    lo, up, st = [0, 0, 0], [n0, n1, n2], [1, n0, n0 * n1]
+    imin, imax = int(np.argmin(x)), int(np.argmax(x))
+    assert (x == x[imin]).sum() == 1 and (x == x[imax]).sum() == 1
+    r = gbk.decode_result(gbk.mdrange_reduce("minloc", d, lo, up, st).cpu().numpy(), 8, 4)
+    assert r["val"] == x[imin] and r["loc"] == imin
+    r = gbk.decode_result(gbk.mdrange_reduce("maxloc", d, lo, up, st).cpu().numpy(), 9, 4)
+    assert r["val"] == x[imax] and r["loc"] == imax
+    s = gbk.decode_result(gbk.mdrange_reduce("sum", d, lo, up, st).cpu().numpy(), 0, 4)
+    ok, info = sum_ok(s, x, 1e-5)
+    assert ok, info
+    gbk.stream_check()
+
+
+@pytest.mark.parametrize("layout", ["left", "right"])
+def test_mdrange_subbox_generic(env, layout):
+    """A box that is not one contiguous run (generic row kernel), rank 3."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    n0, n1, n2 = 37, 29, 23
+    x = datagen.normal_f32(n0 * n1 * n2, seed=3)
+    st = [1, n0, n0 * n1] if layout == "left" else [n1 * n2, n2, 1]
+    lo, up = [2, 3, 1], [35, 20, 22]
+    d = _dev(torch, x)
+    for op, code in (("minloc", 8), ("maxloc", 9), ("minmaxloc", 11), ("min", 2), ("max", 3)):
+        got = gbk.decode_result(gbk.mdrange_reduce(op, d, lo, up, st).cpu().numpy(), code, 4)
+        want = oracle.mdrange_reduce(op, x, lo, up, st, 1)
+        for nm in (got.dtype.names or [None]):
+            a = got[nm] if nm else got
+            b = want[nm] if nm else want
+            assert np.asarray(a).tobytes() == np.asarray(b).tobytes(), (op, nm, a, b)
+    got = gbk.decode_result(gbk.mdrange_reduce("sum", d, lo, up, st).cpu().numpy(), 0, 4)
+    idx = np.array([i * st[0] + j * st[1] + k * st[2] for i in range(lo[0], up[0]) for j in range(lo[1], up[1])
+                    for k in range(lo[2], up[2])])
+    ok, info = sum_ok(got, x[idx], 1e-5)
+    assert ok, info
+
+
+def test_mdrange_golden(env):
+    gbk, torch = env
+    G = np.load(GOLDEN)
+    for (n0, n1, n2) in [(37, 19, 11), (64, 32, 16)]:
+        x = G[f"mdrange/f32/{n0}x{n1}x{n2}/x"]
+        d = _dev(torch, x)
+        for op, code in (("minloc", 8), ("maxloc", 9)):
+            want = np.frombuffer(G[f"mdrange/{op}/f32/{n0}x{n1}x{n2}/4/out"].tobytes(), gbk.result_dtype(code, 4))[0]
+            got = gbk.decode_result(gbk.mdrange_reduce(op, d, [0, 0, 0], [n0, n1, n2], [1, n0, n0 * n1]).cpu().numpy(),
+                                    code, 4)
+            assert got["val"] == want["val"] and got["loc"] == want["loc"]
+
+
+def test_host_buffer_entry(env):
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    x = datagen.normal_f32(1 << 18, seed=11)
+    r = gbk.mdrange_reduce_host("minmaxloc", x, [0], [x.size], [1])
+    w = oracle.reduce("minmaxloc", x, 1)
+    for nm in ("min_val", "max_val", "min_loc", "max_loc"):
+        assert r[nm] == w[nm]
+
+
+def test_tuning_configs_agree(env):
+    """Every compiled launch configuration gives a correct (in-tolerance,
+    exact for integers) result."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    x = datagen.uniform_i32((1 << 22) + 17, -3, 3, seed=5)
+    xf = datagen.normal_f32((1 << 22) + 17, seed=5)
+    d, df = _dev(torch, x), _dev(torch, xf)
+    w = oracle.reduce("sum", x, 1)
+    wl = oracle.reduce("minloc", xf, 1)
+    for blk, un, cps in [(256, 2, 8), (256, 4, 8), (512, 2, 4), (512, 4, 2), (128, 8, 16), (256, 8, 4), (1024, 2, 2),
+                         (256, 4, 1)]:
+        got = gbk.decode_result(gbk.reduce("sum", d, tune=(blk, un, cps, 0)).cpu().numpy(), 0, 0)
+        assert got == w, (blk, un, cps)
+        gl = gbk.decode_result(gbk.reduce("minloc", df, tune=(blk, un, cps, 0)).cpu().numpy(), 8, 4)
+        assert gl["val"] == wl["val"] and gl["loc"] == wl["loc"]
+        gs = gbk.decode_result(gbk.reduce("sum", df, tune=(blk, un, cps, 0)).cpu().numpy(), 0, 4)
+        ok, info = sum_ok(gs, xf, 1e-5)
+        assert ok, info

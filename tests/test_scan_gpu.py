@@ -1,0 +1,130 @@
+"""Parity of the single-pass GPU scans (through the C ABI) with the oracle
+and the reference's golden outputs; integer scans bit-exact."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+
+    from kokkos_gb300 import gbk
+    torch.cuda.set_device(0)
+    return gbk, torch
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def test_golden_scans(env):
+    gbk, torch = env
+    G = np.load(GOLDEN)
+    for n in [0, 1, 1000, 20011]:
+        x = G[f"scan/i32/{n}/x"]
+        for init in (0, 7):
+            want = np.frombuffer(G[f"exscan/i32_i64/{n}/{init}/4/out"].tobytes(), np.int64)
+            y = torch.empty(n, dtype=torch.int64, device="cuda")
+            gbk.scan(_dev(torch, x), y, inclusive=False, init=init)
+            np.testing.assert_array_equal(y.cpu().numpy(), want)
+        want = np.frombuffer(G[f"inscan/i32/{n}/4/out"].tobytes(), np.int32)
+        y = torch.empty(n, dtype=torch.int32, device="cuda")
+        gbk.scan(_dev(torch, x), y, inclusive=True)
+        np.testing.assert_array_equal(y.cpu().numpy(), want)
+        xl = G[f"scan/i64/{n}/x"]
+        want = np.frombuffer(G[f"scantotal/i64/{n}/4/out"].tobytes(), np.int64)
+        y = torch.empty(n, dtype=torch.int64, device="cuda")
+        tot = torch.zeros(1, dtype=torch.int64, device="cuda")
+        gbk.scan(_dev(torch, xl), y, inclusive=False, total=tot)
+        np.testing.assert_array_equal(y.cpu().numpy(), want[:n])
+        assert int(tot.item()) == int(want[n])
+        xf = G[f"scan/f64/{n}/x"]
+        want = np.frombuffer(G[f"inscan/f64/{n}/4/out"].tobytes(), np.float64)
+        y = torch.empty(n, dtype=torch.float64, device="cuda")
+        gbk.scan(_dev(torch, xf), y, inclusive=True)
+        if n:
+            ya = y.cpu().numpy()
+            scale = np.cumsum(np.abs(xf))
+            assert np.all(np.abs(ya - want) <= 1e-12 * np.maximum(scale, 1e-300))
+    gbk.stream_check()
+
+
+@pytest.mark.parametrize("n", [1, 5, 4095, 4096, 4097, 123457, (1 << 22) + 3])
+@pytest.mark.parametrize("pair", [("i32", "i64"), ("i32", "i32"), ("i64", "i64"), ("u32", "u64"), ("u64", "u64")])
+def test_int_scans_vs_oracle(env, n, pair):
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    tin, tout = gbk.NP[gbk.DT[pair[0]]], gbk.NP[gbk.DT[pair[1]]]
+    x = datagen.uniform_i64(n, 0, 255, seed=n).astype(tin)
+    d = _dev(torch, x)
+    for incl in (False, True):
+        y = torch.empty(n, dtype=getattr(torch, np.dtype(tout).name), device="cuda")
+        gbk.scan(d, y, inclusive=incl, init=None if incl else 11)
+        want = oracle.scan(x, tout, inclusive=incl, init=11, nthreads=3)
+        np.testing.assert_array_equal(y.cpu().numpy(), want)
+    gbk.stream_check()
+
+
+@pytest.mark.parametrize("pair", [("f32", "f32"), ("f32", "f64"), ("f64", "f64")])
+def test_float_scans(env, pair):
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    n = 300001
+    tin, tout = gbk.NP[gbk.DT[pair[0]]], gbk.NP[gbk.DT[pair[1]]]
+    x = datagen.normal_f64(n, seed=4).astype(tin)
+    d = _dev(torch, x)
+    y = torch.empty(n, dtype=getattr(torch, np.dtype(tout).name), device="cuda")
+    gbk.scan(d, y, inclusive=True)
+    exact = np.cumsum(x.astype(np.float64))
+    scale = np.cumsum(np.abs(x.astype(np.float64)))
+    rel = 1e-12 if tout == np.float64 else 1e-5
+    assert np.all(np.abs(y.cpu().numpy().astype(np.float64) - exact) <= rel * scale + 1e-30)
+
+
+def test_c1_exclusive_scan_full_size(env):
+    """Experimental::exclusive_scan of View<int32*> 2^24 uniform 0..15 into
+    View<int64*>, seed 0: bit-exact."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    n = 1 << 24
+    x = datagen.uniform_i32(n, 0, 15, seed=0)
+    y = torch.empty(n, dtype=torch.int64, device="cuda")
+    gbk.scan(_dev(torch, x), y, inclusive=False, init=0)
+    gbk.stream_check()
+    np.testing.assert_array_equal(y.cpu().numpy(), oracle.scan(x, np.int64, inclusive=False, init=0, nthreads=8))
+
+
+def test_inplace_and_misaligned(env):
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    x = datagen.uniform_i64(50001, -9, 9, seed=2)
+    d = _dev(torch, x)
+    gbk.scan(d, d, inclusive=True)
+    np.testing.assert_array_equal(d.cpu().numpy(), np.cumsum(x))
+    xi = datagen.uniform_i32(70001, 0, 9, seed=3)
+    di = _dev(torch, xi)[1:]
+    yo = torch.empty(70001, dtype=torch.int64, device="cuda")[1:]
+    gbk.scan(di, yo, inclusive=False, init=5)
+    np.testing.assert_array_equal(yo.cpu().numpy(), oracle.scan(xi[1:], np.int64, inclusive=False, init=5))
+
+
+def test_many_launches_reuse_status_words(env):
+    """Back-to-back scans of different sizes on one stream reuse the epoch-
+    tagged status words without clearing them."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    for i, n in enumerate([100000, 7, 400000, 4096 * 3, 99999, 1 << 20]):
+        x = datagen.uniform_i32(n, 0, 99, seed=i)
+        y = torch.empty(n, dtype=torch.int64, device="cuda")
+        gbk.scan(_dev(torch, x), y, inclusive=True)
+        np.testing.assert_array_equal(y.cpu().numpy(), np.cumsum(x.astype(np.int64)))
+    gbk.stream_check()

@@ -1,0 +1,115 @@
+"""Parity of the ScatterView histogram and scatter ops (through the C ABI)
+with the oracle / reference golden outputs; counts bit-exact."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+
+    from kokkos_gb300 import gbk
+    torch.cuda.set_device(0)
+    return gbk, torch
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def test_golden_histograms(env):
+    gbk, torch = env
+    G = np.load(GOLDEN)
+    for (n, nb) in [(100000, 4096), (5000, 65536), (0, 16)]:
+        keys = G[f"hist/{n}/{nb}/x"]
+        want = np.frombuffer(G[f"hist/{n}/{nb}/4/out"].tobytes(), np.int64)
+        bins = torch.zeros(nb, dtype=torch.int64, device="cuda")
+        gbk.histogram(_dev(torch, keys), bins)
+        gbk.stream_check()
+        np.testing.assert_array_equal(bins.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 4, 8, 0x11, 0x12, 0x14, 0x18])
+@pytest.mark.parametrize("nbins", [16, 1000, 4096, 1 << 16])
+def test_histogram_variants(env, variant, nbins):
+    """Every privatisation variant (cluster size 1/2/4/8, with/without warp
+    aggregation) counts exactly; contributions add to existing bins."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    cl = variant & 0xF
+    if cl and (nbins + cl - 1) // cl * 4 > 200 * 1024:
+        pytest.skip("bins do not fit this cluster size")
+    n = 1000003
+    keys = datagen.zipf_i32(n, nbins, 1.1, seed=nbins)
+    init = datagen.uniform_i64(nbins, 0, 5, seed=1)
+    bins = _dev(torch, init.copy())
+    gbk.histogram(_dev(torch, keys), bins, tune=(0, 0, 0, variant))
+    gbk.stream_check()
+    want, _ = oracle.histogram(keys, nbins, 4, bins=init.copy())
+    np.testing.assert_array_equal(bins.cpu().numpy(), want)
+
+
+def test_c2_histogram_full_size(env):
+    """ScatterView histogram of 2^26 int32 Zipf(1.1) keys over 2^16 bins into
+    int64 counts: bit-exact."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    n, nb = 1 << 26, 1 << 16
+    keys = datagen.zipf_i32(n, nb, 1.1, seed=0)
+    bins = torch.zeros(nb, dtype=torch.int64, device="cuda")
+    gbk.histogram(_dev(torch, keys), bins)
+    gbk.stream_check()
+    want, _ = oracle.histogram(keys, nb, 8)
+    np.testing.assert_array_equal(bins.cpu().numpy(), want)
+    assert int(bins.sum().item()) == n
+
+
+def test_out_of_range_keys_flagged(env):
+    gbk, torch = env
+    keys = np.array([0, 1, 5, -1, 7, 100, 3], dtype=np.int32)
+    bins = torch.zeros(8, dtype=torch.int64, device="cuda")
+    gbk.histogram(_dev(torch, keys), bins)
+    with pytest.raises(gbk.GbkError) as e:
+        gbk.stream_check()
+    assert e.value.status == 6
+    assert bins.cpu().numpy().tolist() == [1, 1, 0, 1, 0, 1, 0, 1]
+    gbk.stream_check()  # the flag was cleared
+
+
+@pytest.mark.parametrize("op", ["sum", "min", "max", "prod"])
+@pytest.mark.parametrize("dt", ["i32", "i64", "u64", "f32", "f64"])
+def test_scatter_ops(env, op, dt):
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    t = gbk.NP[gbk.DT[dt]]
+    n, nd = 200000, 1000
+    idx = datagen.uniform_i32(n, 0, nd - 1, seed=9)
+    if op == "prod":
+        vals = np.where(datagen.uniform_i32(n, 0, 999, seed=3) == 0, 2, 1).astype(t)
+    elif np.dtype(t).kind == "f":
+        vals = datagen.uniform_i32(n, -100, 100, seed=3).astype(t)  # exactly representable sums
+    else:
+        vals = datagen.uniform_i64(n, 0, 1000, seed=3).astype(t)
+    init = {"sum": 0, "prod": 1, "min": 10**6, "max": 0}[op]
+    dest = np.full(nd, init, dtype=t)
+    want = dest.copy()
+    if op == "sum":
+        np.add.at(want, idx, vals)
+    elif op == "prod":
+        np.multiply.at(want, idx, vals)
+    elif op == "min":
+        np.minimum.at(want, idx, vals)
+    else:
+        np.maximum.at(want, idx, vals)
+    d = _dev(torch, dest)
+    gbk.scatter(op, _dev(torch, idx), _dev(torch, vals), d)
+    gbk.stream_check()
+    np.testing.assert_array_equal(d.cpu().numpy(), want)
