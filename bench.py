@@ -160,7 +160,7 @@ def cpu_baseline(budget_s=12.0):
         oracle.histogram(keys, NBINS, P)
         steps += 1
         el = time.perf_counter() - t0
-        if el >= budget_s or steps >= 50:
+        if el >= budget_s:
             break
     gbs = steps * STEP_BYTES / el / 1e9
     return {"value": round(gbs, 3), "unit": "GB/s", "cores": P, "kind": "port",
@@ -191,6 +191,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbk", choices=["gbk", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default=None, choices=["minloc", "maxloc", "sum", "hist"],
+                    help="run just this operation warmup+steps times on the bench inputs (for profiler captures)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -243,6 +245,16 @@ def main():
 
     ops = [("mdrange_minloc_f32", op_minloc, RED_BYTES), ("mdrange_maxloc_f32", op_maxloc, RED_BYTES),
            ("mdrange_sum_f32", op_sum, RED_BYTES), ("histogram_zipf_2^16", op_hist, HIST_BYTES)]
+
+    if args.only:
+        f = {"minloc": op_minloc, "maxloc": op_maxloc, "sum": op_sum, "hist": op_hist}[args.only]
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup + args.steps):
+                f()
+        torch.cuda.synchronize()
+        gbk.stream_check(stream)
+        print(json.dumps({"only": args.only, "launches": args.warmup + args.steps}))
+        return
 
     def step(evs=None):
         for i, (_, f, _) in enumerate(ops):

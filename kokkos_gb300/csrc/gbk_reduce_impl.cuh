@@ -76,16 +76,18 @@ __global__ void __launch_bounds__(BLOCK)
   __shared__ V sm[BLOCK / 32];
   V acc = R::init();
   const int64_t gtid = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
-  const int64_t nthr = (int64_t)gridDim.x * BLOCK;
   // Unaligned head [0, head): one element per thread.
   if (gtid < head) R::template update<true>(acc, x[gtid], loc0 + gtid);
   const T* xb = x + head;
   const int64_t nvec = (n - head) / VEC;
   constexpr int64_t TILE = (int64_t)BLOCK * UNROLL;
-  const int64_t ntile = nvec / TILE;
   const int64_t lb = loc0 + head;
-  for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x) {
-    const int64_t vb = t * TILE + threadIdx.x;
+  // Each CTA owns one contiguous, equal share of the whole vectors.
+  const int64_t per = nvec / gridDim.x, rem = nvec % gridDim.x;
+  const int64_t v0 = (int64_t)blockIdx.x * per + ((int64_t)blockIdx.x < rem ? blockIdx.x : rem);
+  const int64_t v1 = v0 + per + ((int64_t)blockIdx.x < rem ? 1 : 0);
+  int64_t vb = v0 + threadIdx.x;
+  for (; vb + (int64_t)(UNROLL - 1) * BLOCK < v1; vb += TILE) {
     Vec16<T> v[UNROLL];
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) v[u].u = ld_stream16(xb + (vb + (int64_t)u * BLOCK) * VEC);
@@ -96,12 +98,11 @@ __global__ void __launch_bounds__(BLOCK)
       for (int k = 0; k < VEC; ++k) R::template update<true>(acc, v[u].v[k], e0 + k);
     }
   }
-  // Leftover whole vectors, spread over all threads.
-  for (int64_t vi = ntile * TILE + gtid; vi < nvec; vi += nthr) {
+  for (; vb < v1; vb += BLOCK) {
     Vec16<T> v;
-    v.u = ld_stream16(xb + vi * VEC);
+    v.u = ld_stream16(xb + vb * VEC);
 #pragma unroll
-    for (int k = 0; k < VEC; ++k) R::template update<true>(acc, v.v[k], lb + vi * VEC + k);
+    for (int k = 0; k < VEC; ++k) R::template update<true>(acc, v.v[k], lb + vb * VEC + k);
   }
   // Tail elements after the last whole vector.
   const int64_t t0 = head + nvec * VEC;

@@ -85,7 +85,6 @@ __global__ void __launch_bounds__(BLOCK)
   constexpr int64_t WSLICE = 32LL * IPT * VEC;
   __shared__ int64_t s_tile;
   __shared__ TO s_warp[WARPS];
-  __shared__ TO s_prefix;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   if (threadIdx.x == 0) {
@@ -100,7 +99,9 @@ __global__ void __launch_bounds__(BLOCK)
   const bool full = tbase + TILE <= n;
 
   // ---- load (warp-striped) and thread-local inclusive scans --------------
-  TO v[IPT][VEC];
+  // Inputs stay in the input type (fewer registers for widening scans); the
+  // in-chunk prefix is recomputed when the outputs are formed.
+  TI v[IPT][VEC];
 #pragma unroll
   for (int k = 0; k < IPT; ++k) {
     const int64_t e0 = wbase + ((int64_t)k * 32 + lane) * VEC;
@@ -108,20 +109,20 @@ __global__ void __launch_bounds__(BLOCK)
       Vec16<TI> u;
       u.u = ld_stream16(x + e0);
 #pragma unroll
-      for (int j = 0; j < VEC; ++j) v[k][j] = (TO)u.v[j];
+      for (int j = 0; j < VEC; ++j) v[k][j] = u.v[j];
     } else {
 #pragma unroll
-      for (int j = 0; j < VEC; ++j) v[k][j] = (e0 + j < n) ? (TO)x[e0 + j] : TO(0);
+      for (int j = 0; j < VEC; ++j) v[k][j] = (e0 + j < n) ? x[e0 + j] : TI(0);
     }
-#pragma unroll
-    for (int j = 1; j < VEC; ++j) v[k][j] = v[k][j - 1] + v[k][j];
   }
   // ---- warp scan over chunks in (k, lane) order ---------------------------
   TO chunk_ex[IPT];
   TO carry = TO(0);
 #pragma unroll
   for (int k = 0; k < IPT; ++k) {
-    const TO c = v[k][VEC - 1];
+    TO c = (TO)v[k][0];
+#pragma unroll
+    for (int j = 1; j < VEC; ++j) c = c + (TO)v[k][j];
     const TO inc = warp_iscan(c);
     TO ex = shup(inc, 1);
     if (lane == 0) ex = TO(0);
@@ -139,65 +140,74 @@ __global__ void __launch_bounds__(BLOCK)
       tile_agg = tile_agg + s_warp[w];
     }
   }
-  // ---- decoupled look-back (warp 0) ---------------------------------------
-  if (warp == 0) {
-    const unsigned ep = S.epoch << 2;
-    TO excl = TO(0);
-    if (tile == 0) {
-      if (lane == 0) {
-        S.incl[0] = tile_agg;
-        __threadfence();
-        st_release_u32(S.flags, ep | FLAG_P);
-      }
-    } else {
-      if (lane == 0) {
-        S.agg[tile] = tile_agg;
-        __threadfence();
-        st_release_u32(S.flags + tile, ep | FLAG_A);
-      }
-      int64_t pt0 = tile - 1;
-      bool timed_out = false;
-      while (true) {
-        const int64_t pt = pt0 - lane;
-        unsigned f = ep | FLAG_P;
-        TO val = TO(0);
-        if (pt >= 0) {
-          int64_t polls = 0;
-          unsigned ns = 32;
-          while (true) {
-            f = ld_acquire_u32(S.flags + pt);
-            if ((f & ~3u) == ep && (f & 3u)) break;
-            if (++polls > S.wait_limit || timed_out) {
-              f = ep | FLAG_P;  // give up: treat as a zero prefix
-              timed_out = true;
-              break;
-            }
-            __nanosleep(ns);
-            if (ns < 256) ns <<= 1;
-          }
-          if (!timed_out) val = ((f & 3u) == FLAG_P) ? ld_relaxed_val(S.incl + pt) : ld_relaxed_val(S.agg + pt);
-        }
-        timed_out = __any_sync(0xffffffffu, timed_out);
-        const unsigned pmask = __ballot_sync(0xffffffffu, (f & 3u) == FLAG_P);
-        const int last = pmask ? (__ffs(pmask) - 1) : 31;
-        // Sum the window up to the nearest inclusive prefix (fixed lane order).
-        TO contrib = (lane <= last) ? val : TO(0);
-        contrib = warp_sum(contrib);
-        excl = excl + contrib;
-        if (pmask) break;
-        pt0 -= 32;
-      }
-      if (lane == 0) {
-        if (timed_out) atomicOr(S.err, GBK_EBIT_TIMEOUT);
-        S.incl[tile] = excl + tile_agg;
-        __threadfence();
-        st_release_u32(S.flags + tile, ep | FLAG_P);
-      }
+  // ---- decoupled look-back, the whole CTA as one BLOCK-tile window ----------
+  // Thread i examines predecessor tile (window start - i).  The window sums
+  // aggregates back to the nearest tile with an inclusive prefix; windows
+  // step back by BLOCK tiles until one holds such a tile.  A whole-CTA
+  // window keeps the walk short when hundreds of tiles are in flight.
+  const unsigned ep = S.epoch << 2;
+  __shared__ int s_near;
+  __shared__ int s_timeout;
+  __shared__ TO s_wsum[WARPS];
+  TO excl = TO(0);
+  if (tile == 0) {
+    if (threadIdx.x == 0) {
+      S.incl[0] = tile_agg;
+      st_release_u32(S.flags, ep | FLAG_P);
     }
-    if (lane == 0) s_prefix = excl;
+  } else {
+    if (threadIdx.x == 0) {
+      S.agg[tile] = tile_agg;
+      st_release_u32(S.flags + tile, ep | FLAG_A);
+      s_timeout = 0;
+    }
+    int64_t pt0 = tile - 1;
+    while (true) {
+      const int64_t pt = pt0 - threadIdx.x;
+      unsigned f = ep | FLAG_P;
+      TO val = TO(0);
+      if (threadIdx.x == 0) s_near = BLOCK;
+      __syncthreads();
+      if (pt >= 0) {
+        int64_t polls = 0;
+        unsigned ns = 0;
+        while (true) {
+          f = ld_relaxed_u32(S.flags + pt);
+          if ((f & ~3u) == ep && (f & 3u)) break;
+          if (++polls > S.wait_limit || *(volatile int*)&s_timeout) {
+            f = ep | FLAG_P;  // give up: treat as a zero prefix
+            atomicExch(&s_timeout, 1);
+            break;
+          }
+          if (polls > 8) {
+            ns = ns ? (ns < 256 ? ns * 2 : 256) : 32;
+            __nanosleep(ns);
+          }
+        }
+        __threadfence();  // acquire: the value below is at least as new as the flag
+        if (!*(volatile int*)&s_timeout) val = ((f & 3u) == FLAG_P) ? ld_relaxed_val(S.incl + pt) : ld_relaxed_val(S.agg + pt);
+      }
+      if ((f & 3u) == FLAG_P) atomicMin(&s_near, (int)threadIdx.x);
+      __syncthreads();
+      const int near = s_near;
+      // Fixed-order sum of the window entries up to the nearest prefix.
+      TO c = ((int)threadIdx.x <= near) ? val : TO(0);
+      c = warp_sum(c);
+      if (lane == 0) s_wsum[warp] = c;
+      __syncthreads();
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) excl = excl + s_wsum[w];
+      if (near < BLOCK) break;
+      pt0 -= BLOCK;
+      __syncthreads();  // s_wsum / s_near are rewritten by the next window
+    }
+    if (threadIdx.x == 0) {
+      if (s_timeout) atomicOr(S.err, GBK_EBIT_TIMEOUT);
+      S.incl[tile] = excl + tile_agg;
+      st_release_u32(S.flags + tile, ep | FLAG_P);
+    }
   }
-  __syncthreads();
-  const TO tile_pre = s_prefix;
+  const TO tile_pre = excl;
   if (total && tile == S.ntiles - 1 && threadIdx.x == 0) *total = INCL ? tile_pre + tile_agg : init + (tile_pre + tile_agg);
 
   // ---- write ---------------------------------------------------------------
@@ -205,12 +215,17 @@ __global__ void __launch_bounds__(BLOCK)
 #pragma unroll
   for (int k = 0; k < IPT; ++k) {
     const int64_t e0 = wbase + ((int64_t)k * 32 + lane) * VEC;
-    const TO pre = base + chunk_ex[k];
+    TO run = base + chunk_ex[k];
     TO o[VEC];
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
-      if (INCL) o[j] = pre + v[k][j];
-      else o[j] = (j == 0) ? pre : pre + v[k][j - 1];
+      if (INCL) {
+        run = run + (TO)v[k][j];
+        o[j] = run;
+      } else {
+        o[j] = run;
+        run = run + (TO)v[k][j];
+      }
     }
     if (ALIGNED && full) {
       constexpr int OV = 16 / sizeof(TO);

@@ -110,8 +110,136 @@ __global__ void __launch_bounds__(BLOCK)
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, GBK_EBIT_KEY_RANGE);
 }
 
-// No privatisation (bins too many for the cluster's shared memory): warp-
-// aggregated global reductions.
+// One CTA per SM holding every bin as a 16-bit counter (two per 32-bit
+// word, 2^16 bins in 128 KiB).  The CTA walks its contiguous share of the
+// keys in rounds of BLOCK*8 keys; after every DRAIN rounds (at most 32768
+// keys, so no half-word can pass 0xFFFF from below 0x8000) all threads sync
+// and every half-word that reached 0x8000 gives 0x8000 to the global bin.
+// Overflow is therefore impossible and no carry ever reaches the
+// neighbouring bin.  Keys for the next round are loaded before the current
+// round is counted, so two rounds of loads are in flight.
+template <int BLOCK, bool AGG>
+__global__ void __launch_bounds__(BLOCK, 1)
+    k_hist16(const int32_t* __restrict__ keys, int64_t nvec, int64_t nbins, unsigned long long* bins, int* err) {
+  extern __shared__ __align__(16) unsigned sh[];
+  constexpr int VPT = 2;                       // vectors (4 keys each) per thread per round
+  constexpr int ROUND = BLOCK * VPT;           // vectors per round
+  constexpr int DRAIN = 32768 / (ROUND * 4);   // rounds between drains
+  static_assert(DRAIN >= 1, "round too large for 16-bit counters");
+  const int nwords = (int)((nbins + 1) >> 1);
+  for (int i = threadIdx.x; i < nwords; i += BLOCK) sh[i] = 0u;
+  __syncthreads();
+  bool bad = false;
+  // Contiguous, balanced share of the vectors for this CTA.
+  const int64_t per = nvec / gridDim.x, rem = nvec % gridDim.x;
+  const int64_t v0 = blockIdx.x * per + (blockIdx.x < rem ? blockIdx.x : rem);
+  const int64_t v1 = v0 + per + (blockIdx.x < rem ? 1 : 0);
+  auto count = [&](int32_t k) {
+    const bool ok = (uint32_t)k < (uint64_t)nbins;
+    if (!ok) bad = true;
+    unsigned add = 1;
+    bool leader = ok;
+    if (AGG) {
+      const unsigned act = __activemask();
+      const unsigned peers = __match_any_sync(act, ok ? k : -1);
+      leader = ok && ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1));
+      add = __popc(peers);
+    }
+    if (leader) atomicAdd(sh + (k >> 1), add << ((k & 1) * 16));
+  };
+  auto drain = [&]() {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nwords; i += BLOCK) {
+      const unsigned w = sh[i];
+      const unsigned hi = w & 0x80008000u;
+      if (hi) {
+        sh[i] = w - hi;
+        if (hi & 0x8000u) red_add_u64(bins + 2 * i, 0x8000ull);
+        if (hi & 0x80000000u) red_add_u64(bins + 2 * i + 1, 0x8000ull);
+      }
+    }
+    __syncthreads();
+  };
+  int64_t v = v0;
+  Vec16<int32_t> cur[VPT], nxt[VPT];
+#pragma unroll
+  for (int j = 0; j < VPT; ++j) {
+    const int64_t q = v + (int64_t)j * BLOCK + threadIdx.x;
+    cur[j].u = q < v1 ? ld_stream16(keys + 4 * q) : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+  }
+  int since = 0;
+  while (v < v1) {
+    const int64_t vn = v + ROUND;
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) {
+      const int64_t q = vn + (int64_t)j * BLOCK + threadIdx.x;
+      nxt[j].u = q < v1 ? ld_stream16(keys + 4 * q) : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    }
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) {
+      const int64_t q = v + (int64_t)j * BLOCK + threadIdx.x;
+      if (q < v1) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) count(cur[j].v[e]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) cur[j] = nxt[j];
+    v = vn;
+    if (++since == DRAIN) {
+      since = 0;
+      drain();
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nwords; i += BLOCK) {
+    const unsigned w = sh[i];
+    if (w & 0xFFFFu) red_add_u64(bins + 2 * i, (unsigned long long)(w & 0xFFFFu));
+    if ((w >> 16) && 2 * i + 1 < nbins) red_add_u64(bins + 2 * i + 1, (unsigned long long)(w >> 16));
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, GBK_EBIT_KEY_RANGE);
+}
+
+// Keys that are not part of a whole 16-byte vector (unaligned head, tail).
+__global__ void k_hist_edges(const int32_t* __restrict__ keys, int64_t head, int64_t tail0, int64_t n, int64_t nbins,
+                             unsigned long long* bins, int* err) {
+  const int64_t i = threadIdx.x;
+  int64_t idx = -1;
+  if (i < head) idx = i;
+  else if (i - head < n - tail0) idx = tail0 + (i - head);
+  if (idx < 0) return;
+  const int32_t k = keys[idx];
+  if ((uint32_t)k < (uint64_t)nbins) red_add_u64(bins + k, 1ull);
+  else atomicOr(err, GBK_EBIT_KEY_RANGE);
+}
+
+template <bool AGG>
+int launch_hist16(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, Workspace* w) {
+  constexpr int BLOCK = 1024;
+  const size_t smem = (size_t)((nbins + 1) >> 1) * 4;
+  auto kfn = k_hist16<BLOCK, AGG>;
+  GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const uintptr_t a = (uintptr_t)keys;
+  int64_t head = (int64_t)(((16 - (a & 15)) & 15) / 4);
+  if (head > n) head = n;
+  const int64_t nvec = (n - head) / 4;
+  const int64_t tail0 = head + nvec * 4;
+  if (head || tail0 < n) {
+    k_hist_edges<<<1, 32, 0, w->stream>>>(keys, head, tail0, n, nbins, (unsigned long long*)bins, w->err);
+    note_launch();
+  }
+  if (nvec > 0) {
+    int64_t grid = sm_count();
+    const int64_t need = (nvec + BLOCK * 2 - 1) / (BLOCK * 2);
+    if (grid > need) grid = need;
+    kfn<<<(unsigned)grid, BLOCK, smem, w->stream>>>(keys + head, nvec, nbins, (unsigned long long*)bins, w->err);
+    note_launch();
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+// No privatisation (bins too many for shared memory): warp-aggregated
+// global reductions.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
     k_hist_global(const int32_t* __restrict__ keys, int64_t n, int64_t nbins, unsigned long long* bins, int* err) {
@@ -165,16 +293,26 @@ int launch_priv(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, Wo
 
 int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Workspace* w, const gbk_tuning_t* t) {
   if (n == 0) return GBK_OK;
-  int cl = t && t->variant ? (t->variant & 0xF) : 0;  // cluster size; 0 = auto
-  const bool agg = t ? ((t->variant & 0x10) != 0) : false;
+  // variant bits: 0x0F cluster size of the 32-bit privatised kernel (1, 2,
+  // 4, 8); 0x10 warp aggregation; 0x20 the 16-bit one-CTA-per-SM kernel;
+  // 0x40 no privatisation.  0 = automatic choice.
+  const int var = t ? t->variant : 0;
+  int cl = var & 0xF;
+  bool agg = (var & 0x10) != 0;
   const int cps = t && t->ctas_per_sm ? t->ctas_per_sm : 1;
   const int64_t max_smem = 200 * 1024;
-  if (cl == 0) {
-    cl = 1;
-    while (cl <= 8 && (nbins + cl - 1) / cl * 4 > max_smem) cl *= 2;
-    if (cl == 1 && nbins * 4 > 96 * 1024) cl = 2;
+  bool use16 = (var & 0x20) != 0;
+  const bool force_global = (var & 0x40) != 0;
+  if (var == 0) {
+    if (nbins * 4 <= 96 * 1024) cl = 1;
+    else if ((nbins + 1) / 2 * 4 <= max_smem) { use16 = true; agg = true; }
+    else { cl = 2; while (cl <= 8 && (nbins + cl - 1) / cl * 4 > max_smem) cl *= 2; }
   }
-  if ((nbins + cl - 1) / cl * 4 > max_smem || cl > 8) {
+  if (use16 && !force_global && (nbins + 1) / 2 * 4 <= max_smem) {
+    return agg ? launch_hist16<true>(keys, n, nbins, bins, w) : launch_hist16<false>(keys, n, nbins, bins, w);
+  }
+  if (cl == 0) cl = 1;
+  if (force_global || (nbins + cl - 1) / cl * 4 > max_smem || cl > 8) {
     int64_t grid = (int64_t)sm_count() * 8;
     k_hist_global<256><<<(unsigned)grid, 256, 0, w->stream>>>(keys, n, nbins, (unsigned long long*)bins, w->err);
     note_launch();

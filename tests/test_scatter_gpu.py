@@ -35,7 +35,7 @@ def test_golden_histograms(env):
         np.testing.assert_array_equal(bins.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 4, 8, 0x11, 0x12, 0x14, 0x18])
+@pytest.mark.parametrize("variant", [0, 1, 2, 4, 8, 0x11, 0x12, 0x14, 0x18, 0x20, 0x30, 0x40])
 @pytest.mark.parametrize("nbins", [16, 1000, 4096, 1 << 16])
 def test_histogram_variants(env, variant, nbins):
     """Every privatisation variant (cluster size 1/2/4/8, with/without warp
@@ -54,6 +54,21 @@ def test_histogram_variants(env, variant, nbins):
     gbk.stream_check()
     want, _ = oracle.histogram(keys, nbins, 4, bins=init.copy())
     np.testing.assert_array_equal(bins.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("variant", [0x20, 0x30, 0])
+def test_hist16_saturating_bins(env, variant):
+    """16-bit privatised counters: one bin taking every key, and two bins
+    sharing one 32-bit word both taking millions of keys, stay exact."""
+    gbk, torch = env
+    nb = 1 << 16
+    for keys in (np.full(3000001, 7, dtype=np.int32),
+                 np.tile(np.array([6, 7, 7, 6, 6, 9], dtype=np.int32), 1000003)):
+        bins = torch.zeros(nb, dtype=torch.int64, device="cuda")
+        gbk.histogram(_dev(torch, keys), bins, tune=(0, 0, 0, variant))
+        gbk.stream_check()
+        want = np.bincount(keys, minlength=nb)
+        np.testing.assert_array_equal(bins.cpu().numpy(), want)
 
 
 def test_c2_histogram_full_size(env):
