@@ -191,8 +191,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbk", choices=["gbk", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default=None, choices=["minloc", "maxloc", "sum", "hist"],
-                    help="run just this operation warmup+steps times on the bench inputs (for profiler captures)")
+    ap.add_argument("--only", default=None, choices=["minloc", "maxloc", "sum", "hist", "sum_f64", "exscan"],
+                    help="run just this operation warmup+steps times (for profiler captures): the bench ops on the "
+                         "bench inputs, or sum_f64 / exscan on 2^24 doubles / int32 (the RangePolicy Sum and "
+                         "exclusive_scan i32->i64 workload)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -209,6 +211,27 @@ def main():
     stream = torch.cuda.Stream(device=dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
     lib = gbk.lib
+
+    if args.only in ("sum_f64", "exscan"):
+        n = 1 << 24
+        res = torch.zeros(64, dtype=torch.uint8, device=dev)
+        if args.only == "sum_f64":
+            x = torch.from_numpy(datagen.uniform_f64(n, seed=0)).to(dev)
+            call = lambda: gbk.check(lib.gbk_reduce(0, 5, ctypes.c_void_p(x.data_ptr()), n,  # noqa: E731
+                                                    ctypes.c_void_p(res.data_ptr()), sp, None), "sum_f64")
+        else:
+            x = torch.from_numpy(datagen.uniform_i32(n, 0, 15, seed=0)).to(dev)
+            y = torch.empty(n, dtype=torch.int64, device=dev)
+            iv = ctypes.c_int64(0)
+            call = lambda: gbk.check(lib.gbk_scan(0, 0, 1, ctypes.c_void_p(x.data_ptr()), n, ctypes.byref(iv),  # noqa: E731
+                                                  ctypes.c_void_p(y.data_ptr()), None, sp, None), "exscan")
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup + args.steps):
+                call()
+        torch.cuda.synchronize()
+        gbk.stream_check(stream)
+        print(json.dumps({"only": args.only, "launches": args.warmup + args.steps}))
+        return
 
     # ---- inputs (pinned host, seeded) and their device copies --------------
     hx = torch.empty(NX, dtype=torch.float32, pin_memory=True)

@@ -86,17 +86,32 @@ __global__ void __launch_bounds__(BLOCK)
   const int64_t per = nvec / gridDim.x, rem = nvec % gridDim.x;
   const int64_t v0 = (int64_t)blockIdx.x * per + ((int64_t)blockIdx.x < rem ? blockIdx.x : rem);
   const int64_t v1 = v0 + per + ((int64_t)blockIdx.x < rem ? 1 : 0);
+  // Software pipeline: the next tile's UNROLL loads are issued before the
+  // current tile is folded, so 2*UNROLL 16-byte loads per thread overlap.
   int64_t vb = v0 + threadIdx.x;
-  for (; vb + (int64_t)(UNROLL - 1) * BLOCK < v1; vb += TILE) {
-    Vec16<T> v[UNROLL];
+  bool have = vb + (int64_t)(UNROLL - 1) * BLOCK < v1;
+  Vec16<T> cur[UNROLL], nxt[UNROLL];
+  if (have) {
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) v[u].u = ld_stream16(xb + (vb + (int64_t)u * BLOCK) * VEC);
+    for (int u = 0; u < UNROLL; ++u) cur[u].u = ld_stream16(xb + (vb + (int64_t)u * BLOCK) * VEC);
+  }
+  while (have) {
+    const int64_t vn = vb + TILE;
+    const bool hn = vn + (int64_t)(UNROLL - 1) * BLOCK < v1;
+    if (hn) {
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) nxt[u].u = ld_stream16(xb + (vn + (int64_t)u * BLOCK) * VEC);
+    }
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       const int64_t e0 = lb + (vb + (int64_t)u * BLOCK) * VEC;
 #pragma unroll
-      for (int k = 0; k < VEC; ++k) R::template update<true>(acc, v[u].v[k], e0 + k);
+      for (int k = 0; k < VEC; ++k) R::template update<true>(acc, cur[u].v[k], e0 + k);
     }
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) cur[u] = nxt[u];
+    vb = vn;
+    have = hn;
   }
   for (; vb < v1; vb += BLOCK) {
     Vec16<T> v;

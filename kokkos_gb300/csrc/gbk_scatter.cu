@@ -305,7 +305,7 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   const bool force_global = (var & 0x40) != 0;
   if (var == 0) {
     if (nbins * 4 <= 96 * 1024) cl = 1;
-    else if ((nbins + 1) / 2 * 4 <= max_smem) { use16 = true; agg = true; }
+    else if ((nbins + 1) / 2 * 4 <= max_smem) { use16 = true; agg = false; }
     else { cl = 2; while (cl <= 8 && (nbins + cl - 1) / cl * 4 > max_smem) cl *= 2; }
   }
   if (use16 && !force_global && (nbins + 1) / 2 * 4 <= max_smem) {
@@ -318,7 +318,9 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
     note_launch();
     return cuda_status(cudaGetLastError());
   }
-#define GBK_HL(C, A) return launch_priv<C, 1024, A>(keys, n, nbins, bins, w, cps)
+  // Two 1024-thread CTAs per SM when the private table is small enough.
+  const int cps2 = (t && t->ctas_per_sm) ? cps : ((nbins + cl - 1) / cl * 4 <= 100 * 1024 ? 2 : 1);
+#define GBK_HL(C, A) return launch_priv<C, 1024, A>(keys, n, nbins, bins, w, cps2)
   switch (cl) {
     case 1: if (agg) GBK_HL(1, true); else GBK_HL(1, false);
     case 2: if (agg) GBK_HL(2, true); else GBK_HL(2, false);
