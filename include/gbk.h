@@ -51,6 +51,7 @@ extern "C" {
 #define GBK_ERR_OUT_OF_WORKSPACE 5
 #define GBK_ERR_KEY_OUT_OF_RANGE 6
 #define GBK_ERR_NO_DEVICE 7
+#define GBK_ERR_SCRATCH_LIMIT 8 /* request exceeds the fixed scratch of gbk_reduce_noalloc */
 
 typedef enum { GBK_I32 = 0, GBK_I64 = 1, GBK_U32 = 2, GBK_U64 = 3, GBK_F32 = 4, GBK_F64 = 5 } gbk_dtype_t;
 
@@ -142,6 +143,26 @@ GBK_FOR_EACH_INT_DTYPE(GBK_DECLARE_TYPED_REDUCE, land)
 GBK_FOR_EACH_INT_DTYPE(GBK_DECLARE_TYPED_REDUCE, lor)
 GBK_FOR_EACH_INT_DTYPE(GBK_DECLARE_TYPED_REDUCE, band)
 GBK_FOR_EACH_INT_DTYPE(GBK_DECLARE_TYPED_REDUCE, bor)
+
+/* Reduce that allocates nothing.  No counterpart in the reference: it is
+ * for callers that may not allocate device memory — code working inside a
+ * device-memory budget owned by someone else (a framework's caching
+ * allocator, an application that forbids allocations after start-up) and
+ * latency-critical loops that must not hit the device-wide synchronisation
+ * cudaMalloc/cudaFree can cause.  Same reducers, dtypes, layouts and result
+ * as gbk_reduce (its default launch shape: grid = SMs * ctas_per_sm CTAs of
+ * 256 threads, ctas_per_sm 0 = 8), but the per-CTA partial values and the
+ * ticket live in one fixed device array inside the library: 128 KiB + 256 B
+ * per GPU that loads the library, held until the process exits, room for at
+ * most 4096 CTAs.  A call that would need more CTAs returns
+ * GBK_ERR_SCRATCH_LIMIT.  The caller still provides x and result (device
+ * memory).  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) and should come before any stream capture.
+ * All calls on a device share the array: calls whose kernels may overlap on
+ * the GPU (different streams not ordered by events) race and must not be
+ * issued. */
+int gbk_reduce_noalloc(gbk_reducer_t op, gbk_dtype_t dtype, const void* x, int64_t n, void* result,
+                       gbk_stream_t stream, int32_t ctas_per_sm);
 
 /* ---- reduce over an MDRangePolicy box of a strided view ------------------ */
 /* parallel_reduce(MDRangePolicy<Rank<rank>>(lower, upper),

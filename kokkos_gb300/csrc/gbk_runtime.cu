@@ -137,6 +137,7 @@ const char* gbk_status_string(int s) {
     case GBK_ERR_OUT_OF_WORKSPACE: return "workspace too small (reserve it before stream capture)";
     case GBK_ERR_KEY_OUT_OF_RANGE: return "key outside the bin range (skipped)";
     case GBK_ERR_NO_DEVICE: return "no CUDA device";
+    case GBK_ERR_SCRATCH_LIMIT: return "request needs more CTAs than the fixed scratch of gbk_reduce_noalloc holds (4096)";
   }
   return "unknown status";
 }
