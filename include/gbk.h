@@ -225,6 +225,39 @@ int gbk_histogram_i32_i64_host(const int32_t* host_keys, int64_t n, int64_t* hos
 int gbk_scatter(gbk_reducer_t op, gbk_dtype_t dtype, const int32_t* idx, const void* vals, int64_t n, void* dest,
                 int64_t ndest, gbk_stream_t stream);
 
+/* ---- sort ----------------------------------------------------------------- */
+/* Kokkos::sort(exec, view) for a contiguous view of i32 i64 u32 u64 f32 f64
+ * keys, ascending, in place (algorithms/src/sorting/Kokkos_SortPublicAPI.hpp:31-116;
+ * the reference's CUDA path is thrust::sort, impl/Kokkos_SortImpl.hpp:204-219).
+ * Floating point: -0.0 sorts before +0.0, NaNs after +inf (sign-bit clear)
+ * or before -inf (sign-bit set).  Stable LSD radix sort; digit passes whose
+ * 8-bit digit is the same for every key are skipped.  n < 2^30.  The call
+ * synchronises the stream once (to read the digit histograms back). */
+int gbk_sort(gbk_dtype_t key_dtype, void* keys, int64_t n, gbk_stream_t stream);
+/* Experimental::sort_by_key(exec, keys, values) (Kokkos_SortByKeyPublicAPI.hpp:30-114,
+ * CUDA path thrust::sort_by_key, impl/Kokkos_SortByKeyImpl.hpp:125-138):
+ * values of 4 or 8 bytes move with their keys.  STABLE: equal keys keep their
+ * input order (the reference's OpenMP sort_by_key is not stable; on distinct
+ * keys the results are identical). */
+int gbk_sort_by_key(gbk_dtype_t key_dtype, void* keys, int value_bytes, void* values, int64_t n,
+                    gbk_stream_t stream);
+int gbk_sort_u64(uint64_t* keys, int64_t n, gbk_stream_t stream);
+int gbk_sort_by_key_u64_i32(uint64_t* keys, int32_t* values, int64_t n, gbk_stream_t stream);
+/* BinSort(keys, BinOp1D(nbins-1, min, max), sort_within_bins)
+ * .create_permute_vector() (algorithms/src/sorting/Kokkos_BinSortPublicAPI.hpp:208-238,
+ * BinOp1D Kokkos_BinOpsPublicAPI.hpp:25-71): bin(k) = (int)(mul * (double(k)
+ * - kmin)) with the caller's mul and kmin (BinOp1D::mul_, min_); nbins =
+ * BinOp1D::max_bins().  Writes bin_count[nbins] (int32), bin_offsets[nbins]
+ * (exclusive starts, int64) and perm[n] (int64): the stable permutation by
+ * bin (by key inside a bin when sort_within_bins).  The reference bins with
+ * atomics, so its order inside a bin is arbitrary; bin contents are equal. */
+int gbk_binsort_u64(const uint64_t* keys, int64_t n, int64_t nbins, double kmin, double mul, int sort_within_bins,
+                    int32_t* bin_count, int64_t* bin_offsets, int64_t* perm, gbk_stream_t stream);
+/* BinSort::sort(values) / applyPermutation: dst[i] = src[perm[i]] for
+ * elements of value_bytes (1, 2, 4, 8) bytes; dst must not alias src
+ * (Kokkos_BinSortPublicAPI.hpp:251-319, impl/Kokkos_SortByKeyImpl.hpp:218-233). */
+int gbk_permute(int value_bytes, const void* src, const int64_t* perm, int64_t n, void* dst, gbk_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

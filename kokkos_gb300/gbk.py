@@ -67,6 +67,13 @@ _SIGS = {
     "gbk_histogram_i32_i64": ([vp, i64, vp, i64, vp, TP], ci),
     "gbk_histogram_i32_i64_host": ([vp, i64, vp, i64, vp, TP], ci),
     "gbk_scatter": ([ci, ci, vp, vp, i64, vp, i64, vp], ci),
+    "gbk_reduce_noalloc": ([ci, ci, vp, i64, vp, vp, ctypes.c_int32], ci),
+    "gbk_sort": ([ci, vp, i64, vp], ci),
+    "gbk_sort_by_key": ([ci, vp, ci, vp, i64, vp], ci),
+    "gbk_sort_u64": ([vp, i64, vp], ci),
+    "gbk_sort_by_key_u64_i32": ([vp, vp, i64, vp], ci),
+    "gbk_binsort_u64": ([vp, i64, i64, ctypes.c_double, ctypes.c_double, ci, vp, vp, vp, vp], ci),
+    "gbk_permute": ([ci, vp, vp, i64, vp, vp], ci),
 }
 
 
@@ -223,6 +230,43 @@ def scatter(op, idx, vals, dest, stream=None):
                           ctypes.c_void_p(vals.data_ptr()), idx.numel(), ctypes.c_void_p(dest.data_ptr()),
                           dest.numel(), _stream(stream)), "scatter")
     return dest
+
+
+def sort(keys, dt=None, stream=None):
+    """Kokkos::sort of a contiguous CUDA tensor in place (dt overrides the
+    element type code, e.g. for unsigned data held in a signed tensor)."""
+    code = dt if dt is not None else dtype_code(keys.dtype)
+    check(lib.gbk_sort(code, ctypes.c_void_p(keys.data_ptr()), keys.numel(), _stream(stream)), "sort")
+    return keys
+
+
+def sort_by_key(keys, vals, dt=None, stream=None):
+    code = dt if dt is not None else dtype_code(keys.dtype)
+    check(lib.gbk_sort_by_key(code, ctypes.c_void_p(keys.data_ptr()), vals.element_size(),
+                              ctypes.c_void_p(vals.data_ptr()), keys.numel(), _stream(stream)), "sort_by_key")
+    return keys, vals
+
+
+def binsort(keys, nbins, kmin, mul, sort_within_bins=False, stream=None):
+    """BinSort(BinOp1D) permutation of u64 keys (held in an int64 tensor).
+    Returns (bin_count int32, bin_offsets int64, perm int64) CUDA tensors."""
+    import torch
+    counts = torch.empty(nbins, dtype=torch.int32, device=keys.device)
+    offs = torch.empty(nbins, dtype=torch.int64, device=keys.device)
+    perm = torch.empty(keys.numel(), dtype=torch.int64, device=keys.device)
+    check(lib.gbk_binsort_u64(ctypes.c_void_p(keys.data_ptr()), keys.numel(), nbins, float(kmin), float(mul),
+                              1 if sort_within_bins else 0, ctypes.c_void_p(counts.data_ptr()),
+                              ctypes.c_void_p(offs.data_ptr()), ctypes.c_void_p(perm.data_ptr()), _stream(stream)),
+          "binsort")
+    return counts, offs, perm
+
+
+def permute(src, perm, stream=None):
+    import torch
+    dst = torch.empty_like(src)
+    check(lib.gbk_permute(src.element_size(), ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(perm.data_ptr()),
+                          src.numel(), ctypes.c_void_p(dst.data_ptr()), _stream(stream)), "permute")
+    return dst
 
 
 def stream_check(stream=None):
