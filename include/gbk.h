@@ -225,6 +225,41 @@ int gbk_histogram_i32_i64_host(const int32_t* host_keys, int64_t n, int64_t* hos
 int gbk_scatter(gbk_reducer_t op, gbk_dtype_t dtype, const int32_t* idx, const void* vals, int64_t n, void* dest,
                 int64_t ndest, gbk_stream_t stream);
 
+/* ---- batched segmented work ------------------------------------------------ */
+/* Segments s = [offsets[s], offsets[s+1]) of x[0..n), offsets non-decreasing
+ * with offsets[0] = 0 and offsets[nseg] = n (device memory, int64).  All
+ * segments are processed in ONE launch, load-balanced over fixed tiles of the
+ * concatenated array whatever the segment lengths.  Stands in for the
+ * TeamPolicy league pattern, one team per segment with a TeamThreadRange
+ * reduce / scan inside (core/src/Kokkos_ExecPolicy.hpp:366-700,
+ * core/src/Cuda/Kokkos_Cuda_Parallel_Team.hpp:589-980,
+ * core/src/OpenMP/Kokkos_OpenMP_Parallel_Reduce.hpp:332-530), and for a loop
+ * of one parallel_reduce / inclusive_scan per segment.
+ * reduce: out[s] = op over segment s (Sum, Min, Max; identity for an empty
+ * segment), all six dtypes. */
+int gbk_segmented_reduce(gbk_reducer_t op, gbk_dtype_t dtype, const void* x, const int64_t* offsets, int64_t nseg,
+                         int64_t n, void* out, gbk_stream_t stream);
+/* scan: per-segment inclusive / exclusive (from 0) prefix sums, (in, out) in
+ * (i32,i32) (i32,i64) (i64,i64) (f32,f32) (f64,f64). */
+int gbk_segmented_scan(int inclusive, gbk_dtype_t in_dtype, gbk_dtype_t out_dtype, const void* x,
+                       const int64_t* offsets, int64_t nseg, int64_t n, void* y, gbk_stream_t stream);
+
+/* ---- graphs ----------------------------------------------------------------- */
+/* Kokkos::Experimental::Graph for this library's calls
+ * (core/src/Kokkos_Graph.hpp:42-183, Kokkos_GraphNode.hpp:227-470; CUDA
+ * GraphImpl core/src/Cuda/Kokkos_Cuda_Graph_Impl.hpp:59-215): every gbk_*
+ * call issued on `stream` between begin and end becomes a node of a CUDA
+ * graph, in issue order (each node depends on the previous one, as a chain
+ * of then_parallel_* nodes).  Calls that synchronise the host (gbk_sort*,
+ * gbk_binsort_u64, *_host, gbk_stream_check) cannot be captured.  Before
+ * capturing, size the stream's workspace with gbk_workspace_reserve and run
+ * each call once uncaptured.  submit() = gbk_graph_launch. */
+typedef struct gbk_graph_s* gbk_graph_t;
+int gbk_graph_begin(gbk_stream_t stream);
+int gbk_graph_end(gbk_stream_t stream, gbk_graph_t* graph);
+int gbk_graph_launch(gbk_graph_t graph, gbk_stream_t stream);
+int gbk_graph_destroy(gbk_graph_t graph);
+
 /* ---- sort ----------------------------------------------------------------- */
 /* Kokkos::sort(exec, view) for a contiguous view of i32 i64 u32 u64 f32 f64
  * keys, ascending, in place (algorithms/src/sorting/Kokkos_SortPublicAPI.hpp:31-116;

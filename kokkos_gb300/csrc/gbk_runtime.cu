@@ -11,6 +11,7 @@
 #include <map>
 #include <mutex>
 #include <utility>
+#include <vector>
 
 #include "gbk_internal.cuh"
 
@@ -102,18 +103,25 @@ char* ws_scratch(Workspace* w, size_t bytes, int* status) {
 }
 char* ws_stage(Workspace* w, size_t bytes, int* status) { return grow(w, &w->stage, &w->stage_bytes, bytes, status); }
 
+// Look-back status words.  Uncaptured launches tag their words with a fresh
+// 30-bit epoch (2, 3, ...; a wrap clears the buffer), so no clearing is
+// needed per launch.  A launch being captured into a CUDA graph replays with
+// the same arguments every time, so it clears its words with a memset node
+// and uses the reserved epoch 1, which uncaptured launches never use.
 unsigned* ws_flags(Workspace* w, size_t count, unsigned* epoch, int* status) {
-  const size_t had = w->flags_bytes;
   char* f = grow(w, &w->flags, &w->flags_bytes, count * sizeof(unsigned), status);
   if (!f) return nullptr;
+  if (capturing(w->stream)) {
+    cudaError_t e = cudaMemsetAsync(f, 0, count * sizeof(unsigned), w->stream);
+    if (e != cudaSuccess) { *status = cuda_status(e); return nullptr; }
+    *epoch = 1;
+    return (unsigned*)f;
+  }
   w->epoch = (w->epoch + 1) & 0x3FFFFFFFu;
-  if (w->epoch == 0 || w->flags_bytes != had) {
-    // Fresh (zeroed) buffer or wrapped epoch space: zero is never a valid tag.
-    if (w->epoch == 0) {
-      cudaError_t e = cudaMemsetAsync(f, 0, w->flags_bytes, w->stream);
-      if (e != cudaSuccess) { *status = cuda_status(e); return nullptr; }
-    }
-    if (w->epoch == 0) w->epoch = 1;
+  if (w->epoch < 2) {
+    cudaError_t e = cudaMemsetAsync(f, 0, w->flags_bytes, w->stream);
+    if (e != cudaSuccess) { *status = cuda_status(e); return nullptr; }
+    w->epoch = 2;
   }
   *epoch = w->epoch;
   return (unsigned*)f;
@@ -183,6 +191,10 @@ int gbk_workspace_reserve(gbk_stream_t stream, int64_t bytes) {
   if (!w) return st;
   std::lock_guard<std::mutex> lk(w->mu);
   if (!ws_scratch(w, (size_t)bytes, &st)) return st;
+  // Status words: a scan keeps two values of up to 8 bytes per tile in
+  // scratch and one 4-byte status word, so a quarter of the scratch size
+  // covers every launch the scratch can serve.
+  if (!grow(w, &w->flags, &w->flags_bytes, (size_t)bytes / 4 + 4096, &st)) return st;
   return GBK_OK;
 }
 
@@ -217,6 +229,66 @@ int gbk_deep_copy(void* dst, const void* src, int64_t bytes, gbk_stream_t stream
   if (bytes < 0 || (bytes > 0 && (!dst || !src))) return GBK_ERR_INVALID_ARGUMENT;
   if (bytes == 0) return GBK_OK;
   GBK_CUDA_TRY(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDefault, (cudaStream_t)stream));
+  return GBK_OK;
+}
+
+struct gbk_graph_s {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t kernels = 0;  // kernel nodes, added to the launch count per replay
+};
+
+int gbk_graph_begin(gbk_stream_t stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!s) return GBK_ERR_INVALID_ARGUMENT;  // the legacy stream cannot be captured
+  GBK_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  return GBK_OK;
+}
+
+int gbk_graph_end(gbk_stream_t stream, gbk_graph_t* out) {
+  if (!out) return GBK_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  cudaGraph_t g = nullptr;
+  GBK_CUDA_TRY(cudaStreamEndCapture((cudaStream_t)stream, &g));
+  cudaGraphExec_t e = nullptr;
+  cudaError_t err = cudaGraphInstantiate(&e, g, 0);
+  if (err != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_status(err);
+  }
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  int64_t kernels = 0;
+  if (nn) {
+    std::vector<cudaGraphNode_t> nodes(nn);
+    cudaGraphGetNodes(g, nodes.data(), &nn);
+    for (size_t i = 0; i < nn; ++i) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+    }
+  }
+  // The captured launches were counted once at capture; count replays only.
+  g_launches -= kernels;
+  gbk_graph_s* h = new gbk_graph_s();
+  h->graph = g;
+  h->exec = e;
+  h->kernels = kernels;
+  *out = h;
+  return GBK_OK;
+}
+
+int gbk_graph_launch(gbk_graph_t h, gbk_stream_t stream) {
+  if (!h || !h->exec) return GBK_ERR_INVALID_ARGUMENT;
+  GBK_CUDA_TRY(cudaGraphLaunch(h->exec, (cudaStream_t)stream));
+  g_launches += h->kernels;
+  return GBK_OK;
+}
+
+int gbk_graph_destroy(gbk_graph_t h) {
+  if (!h) return GBK_OK;
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  delete h;
   return GBK_OK;
 }
 

@@ -74,6 +74,12 @@ _SIGS = {
     "gbk_sort_by_key_u64_i32": ([vp, vp, i64, vp], ci),
     "gbk_binsort_u64": ([vp, i64, i64, ctypes.c_double, ctypes.c_double, ci, vp, vp, vp, vp], ci),
     "gbk_permute": ([ci, vp, vp, i64, vp, vp], ci),
+    "gbk_segmented_reduce": ([ci, ci, vp, vp, i64, i64, vp, vp], ci),
+    "gbk_segmented_scan": ([ci, ci, ci, vp, vp, i64, i64, vp, vp], ci),
+    "gbk_graph_begin": ([vp], ci),
+    "gbk_graph_end": ([vp, ctypes.POINTER(vp)], ci),
+    "gbk_graph_launch": ([vp, vp], ci),
+    "gbk_graph_destroy": ([vp], ci),
 }
 
 
@@ -267,6 +273,52 @@ def permute(src, perm, stream=None):
     check(lib.gbk_permute(src.element_size(), ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(perm.data_ptr()),
                           src.numel(), ctypes.c_void_p(dst.data_ptr()), _stream(stream)), "permute")
     return dst
+
+
+def segmented_reduce(op, x, offsets, out, stream=None):
+    """out[s] = op over x[offsets[s]:offsets[s+1]] for every segment, one launch."""
+    opc = OPS[op] if isinstance(op, str) else op
+    check(lib.gbk_segmented_reduce(opc, dtype_code(x.dtype), ctypes.c_void_p(x.data_ptr()),
+                                   ctypes.c_void_p(offsets.data_ptr()), offsets.numel() - 1, x.numel(),
+                                   ctypes.c_void_p(out.data_ptr()), _stream(stream)), "segmented_reduce")
+    return out
+
+
+def segmented_scan(x, offsets, y, inclusive=True, stream=None):
+    check(lib.gbk_segmented_scan(1 if inclusive else 0, dtype_code(x.dtype), dtype_code(y.dtype),
+                                 ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(offsets.data_ptr()),
+                                 offsets.numel() - 1, x.numel(), ctypes.c_void_p(y.data_ptr()), _stream(stream)),
+          "segmented_scan")
+    return y
+
+
+class Graph:
+    """Kokkos::Experimental::Graph over this library's calls: the calls made
+    inside `with Graph(stream) as g:` on `stream` are captured; g.submit()
+    replays them."""
+
+    def __init__(self, stream):
+        self.stream = stream
+        self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        check(lib.gbk_graph_begin(ctypes.c_void_p(self.stream.cuda_stream)), "graph_begin")
+        return self
+
+    def __exit__(self, et, ev, tb):
+        st = lib.gbk_graph_end(ctypes.c_void_p(self.stream.cuda_stream), ctypes.byref(self.h))
+        if et is None:
+            check(st, "graph_end")
+
+    def submit(self):
+        check(lib.gbk_graph_launch(self.h, ctypes.c_void_p(self.stream.cuda_stream)), "graph_launch")
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib.gbk_graph_destroy(self.h)
+        except Exception:
+            pass
 
 
 def stream_check(stream=None):

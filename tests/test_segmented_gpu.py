@@ -1,0 +1,167 @@
+"""Batched segmented reduce / scan (one launch for all segments) through the
+C ABI vs the oracle's per-segment loops, the reference's TeamPolicy golden
+output, and CUDA-graph capture of dependent reduce/scan chains."""
+import os
+
+import numpy as np
+import pytest
+
+from tests._util import sum_ok
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+
+    from kokkos_gb300 import gbk
+    torch.cuda.set_device(0)
+    return gbk, torch
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def lengths_cases():
+    from kokkos_gb300 import datagen
+    rng = np.random.default_rng(1)
+    yield "lognormal", datagen.lognormal_lengths(2000, median=300.0, max_len=1 << 16, target_total=1 << 20, seed=2)[0]
+    yield "with_empty", rng.integers(0, 6, size=5000)           # many empty and tiny segments
+    yield "one_huge", np.array([1 << 20])                          # a segment over hundreds of tiles
+    yield "tile_edges", np.array([4096, 4096, 1, 4095, 8192, 0, 4097, 3])  # boundaries on tile edges
+    yield "mixed", np.concatenate([rng.integers(1, 50, 300), [300000], rng.integers(0, 3000, 200)])
+
+
+@pytest.mark.parametrize("case", list(lengths_cases()), ids=lambda c: c[0])
+def test_segmented_vs_oracle(env, case):
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    _, lens = case
+    offs = datagen.offsets_from_lengths(np.asarray(lens, dtype=np.int64))
+    n = int(offs[-1])
+    xf = datagen.normal_f32(n, seed=5)
+    xi = datagen.uniform_i32(n, 0, 255, seed=6)
+    do = _dev(torch, offs)
+    nseg = offs.size - 1
+    # float Sum per segment (tolerance), vs compensated sums
+    out = torch.empty(nseg, dtype=torch.float32, device="cuda")
+    gbk.segmented_reduce("sum", _dev(torch, xf), do, out)
+    gbk.stream_check()
+    got = out.cpu().numpy()
+    _, comp, absum = oracle.seg_sum_f32(xf, offs, 4)
+    for s in range(nseg):
+        seg = xf[offs[s]:offs[s + 1]]
+        ok, info = sum_ok(got[s], seg, 1e-5) if seg.size else (got[s] == 0.0, got[s])
+        assert ok, (s, info)
+    # int Sum / Min / Max exact
+    for op in ("sum", "min", "max"):
+        o = torch.empty(nseg, dtype=torch.int32, device="cuda")
+        gbk.segmented_reduce(op, _dev(torch, xi), do, o)
+        gbk.stream_check()
+        w = np.array([getattr(np, {"sum": "sum", "min": "min", "max": "max"}[op])(xi[offs[s]:offs[s + 1]])
+                      if offs[s + 1] > offs[s] else {"sum": 0, "min": 2**31 - 1, "max": -2**31}[op]
+                      for s in range(nseg)], dtype=np.int64).astype(np.int32)
+        np.testing.assert_array_equal(o.cpu().numpy(), w)
+    # int32 inclusive scan per segment, exact
+    y = torch.empty(n, dtype=torch.int32, device="cuda")
+    gbk.segmented_scan(_dev(torch, xi), do, y, inclusive=True)
+    gbk.stream_check()
+    np.testing.assert_array_equal(y.cpu().numpy(), oracle.seg_inclusive_scan_i32(xi, offs, 4))
+    # exclusive, widening to int64
+    y64 = torch.empty(n, dtype=torch.int64, device="cuda")
+    gbk.segmented_scan(_dev(torch, xi), do, y64, inclusive=False)
+    gbk.stream_check()
+    inc = oracle.seg_inclusive_scan_i32(xi, offs, 4).astype(np.int64)
+    np.testing.assert_array_equal(y64.cpu().numpy(), inc - xi.astype(np.int64))
+
+
+def test_golden_team_reduce(env):
+    """TeamPolicy league of per-segment sums (reference TeamThreadRange
+    reduce) — the batched reduce gives the same sums within 1e-12."""
+    gbk, torch = env
+    G = np.load(GOLDEN)
+    offs = G["teamreduce/f64/50/offsets"]
+    x = G["teamreduce/f64/50/x"]
+    want = np.frombuffer(G["teamreduce/f64/50/out"].tobytes(), np.float64)
+    out = torch.empty(50, dtype=torch.float64, device="cuda")
+    gbk.segmented_reduce("sum", _dev(torch, x), _dev(torch, offs), out)
+    gbk.stream_check()
+    got = out.cpu().numpy()
+    for s in range(50):
+        a = np.abs(x[offs[s]:offs[s + 1]]).sum()
+        assert abs(got[s] - want[s]) <= 1e-12 * max(a, 1e-300)
+
+
+def test_c3_batched_full_size(env):
+    """10,000 lognormal segments (median 2,048, max 2^21, total ~2^28):
+    per-segment float Sum and int32 inclusive_scan, one launch each."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    lens, sigma = datagen.lognormal_lengths(10000, median=2048.0, max_len=1 << 21, target_total=1 << 28, seed=0)
+    offs = datagen.offsets_from_lengths(lens)
+    n = int(offs[-1])
+    assert abs(n - (1 << 28)) / (1 << 28) < 0.02
+    xf = datagen.normal_f32(n, seed=0)
+    xi = datagen.uniform_i32(n, 0, 255, seed=0)
+    do = _dev(torch, offs)
+    out = torch.empty(10000, dtype=torch.float32, device="cuda")
+    gbk.segmented_reduce("sum", _dev(torch, xf), do, out)
+    y = torch.empty(n, dtype=torch.int32, device="cuda")
+    gbk.segmented_scan(_dev(torch, xi), do, y, inclusive=True)
+    gbk.stream_check()
+    _, comp, absum = oracle.seg_sum_f32(xf, offs, 16)
+    got = out.cpu().numpy().astype(np.float64)
+    l2 = np.sqrt(np.add.reduceat(xf.astype(np.float64) ** 2, offs[:-1]))
+    err = np.abs(got - comp)
+    assert np.all((err <= 1e-5 * np.abs(comp)) | (err <= 1e-5 * l2))
+    np.testing.assert_array_equal(y.cpu().numpy(), oracle.seg_inclusive_scan_i32(xi, offs, 16))
+
+
+def test_graph_chain_of_dependent_nodes(env):
+    """A CUDA graph of 8 dependent reduce/scan nodes (each node reads the
+    previous node's output) replays to the same results as the stream
+    launches, several times, interleaved with uncaptured scans."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    s = torch.cuda.Stream()
+    n = 1 << 20
+    x = _dev(torch, datagen.uniform_i32(n, 0, 15, seed=1))
+    bufs = [torch.empty(n, dtype=torch.int64, device="cuda") for _ in range(4)]
+    res = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    gbk.lib.gbk_workspace_reserve(__import__("ctypes").c_void_p(s.cuda_stream), 64 << 20)
+
+    def chain():
+        gbk.scan(x, bufs[0], inclusive=False, init=0, stream=s)           # 1 exclusive_scan i32 -> i64
+        gbk.reduce("max", bufs[0], out=res[0:8], stream=s)                # 2 reduce of node 1's output
+        gbk.scan(bufs[0], bufs[1], inclusive=True, stream=s)              # 3 inclusive scan of node 1
+        gbk.reduce("sum", bufs[1], out=res[8:16], stream=s)               # 4
+        gbk.scan(bufs[1], bufs[2], inclusive=False, init=3, stream=s)     # 5
+        gbk.reduce("minloc", bufs[2][1:], out=res[16:32], stream=s)       # 6
+        gbk.scan(bufs[2], bufs[3], inclusive=True, stream=s)              # 7
+        gbk.reduce("maxloc", bufs[3], out=res[32:48], stream=s)           # 8
+
+    with torch.cuda.stream(s):
+        chain()
+    s.synchronize()
+    want = (res.cpu().numpy().copy(), bufs[3].cpu().numpy().copy())
+    g = gbk.Graph(s)
+    with g:
+        chain()
+    for rep in range(3):
+        res.zero_()
+        bufs[3].zero_()
+        torch.cuda.synchronize()
+        g.submit()
+        # an uncaptured scan on the same stream between replays
+        junk = torch.empty(n, dtype=torch.int64, device="cuda")
+        gbk.scan(x, junk, inclusive=True, stream=s)
+        s.synchronize()
+        np.testing.assert_array_equal(res.cpu().numpy(), want[0])
+        np.testing.assert_array_equal(bufs[3].cpu().numpy(), want[1])
+    gbk.stream_check(s)
