@@ -236,13 +236,15 @@ int gbk_scatter(gbk_reducer_t op, gbk_dtype_t dtype, const int32_t* idx, const v
  * core/src/OpenMP/Kokkos_OpenMP_Parallel_Reduce.hpp:332-530), and for a loop
  * of one parallel_reduce / inclusive_scan per segment.
  * reduce: out[s] = op over segment s (Sum, Min, Max; identity for an empty
- * segment), all six dtypes. */
+ * segment), all six dtypes.  tune->items_per_thread (2, 4, 8) sets the tile;
+ * NULL = tuning table or default. */
 int gbk_segmented_reduce(gbk_reducer_t op, gbk_dtype_t dtype, const void* x, const int64_t* offsets, int64_t nseg,
-                         int64_t n, void* out, gbk_stream_t stream);
+                         int64_t n, void* out, gbk_stream_t stream, const gbk_tuning_t* tune);
 /* scan: per-segment inclusive / exclusive (from 0) prefix sums, (in, out) in
  * (i32,i32) (i32,i64) (i64,i64) (f32,f32) (f64,f64). */
 int gbk_segmented_scan(int inclusive, gbk_dtype_t in_dtype, gbk_dtype_t out_dtype, const void* x,
-                       const int64_t* offsets, int64_t nseg, int64_t n, void* y, gbk_stream_t stream);
+                       const int64_t* offsets, int64_t nseg, int64_t n, void* y, gbk_stream_t stream,
+                       const gbk_tuning_t* tune);
 
 /* ---- graphs ----------------------------------------------------------------- */
 /* Kokkos::Experimental::Graph for this library's calls

@@ -52,6 +52,11 @@ unsigned* ws_flags(Workspace* w, size_t count, unsigned* epoch, int* status);
 char* ws_scratch(Workspace* w, size_t bytes, int* status);
 char* ws_stage(Workspace* w, size_t bytes, int* status);
 int sm_count();
+// Tuning-table configuration for a call made with tune == NULL (nullptr if
+// the table is disabled or has no entry).  Kinds: 0 reduce, 1 scan,
+// 2 histogram, 3 segmented.
+enum { TUNE_REDUCE = 0, TUNE_SCAN = 1, TUNE_HIST = 2, TUNE_SEG = 3 };
+const gbk_tuning_t* tuned_config(int kind, int op, int dtype, int64_t n, int extra, gbk_tuning_t* storage);
 int64_t wait_limit();
 void note_launch(int64_t k = 1);
 int cuda_status(cudaError_t e);

@@ -146,6 +146,8 @@ int gbk_reduce(gbk_reducer_t op, gbk_dtype_t dt, const void* x, int64_t n, void*
   int st = GBK_OK;
   Workspace* w = ws_get((cudaStream_t)stream, &st);
   if (!w) return st;
+  gbk_tuning_t tt;
+  if (!tune) tune = tuned_config(TUNE_REDUCE, op, dt, n, 0, &tt);
   std::lock_guard<std::mutex> lk(w->mu);
   return reduce_any(op, dt, x, n, 0, result, w, tune);
 }

@@ -332,6 +332,8 @@ int gbk_scan(int inclusive, gbk_dtype_t din, gbk_dtype_t dout, const void* x, in
   int st = GBK_OK;
   Workspace* w = ws_get((cudaStream_t)stream, &st);
   if (!w) return st;
+  gbk_tuning_t tt;
+  if (!tune) tune = tuned_config(TUNE_SCAN, inclusive ? 1 : 0, din * 8 + dout, n, 0, &tt);
   std::lock_guard<std::mutex> lk(w->mu);
   return scan_any(inclusive ? 1 : 0, din, dout, x, n, init, y, total, w, tune);
 }

@@ -430,6 +430,12 @@ int gbk_histogram_i32_i64(const int32_t* keys, int64_t n, int64_t* bins, int64_t
   int st = GBK_OK;
   Workspace* w = ws_get((cudaStream_t)stream, &st);
   if (!w) return st;
+  gbk_tuning_t tt;
+  if (!tune) {
+    int lb = 0;
+    while (((int64_t)1 << lb) < nbins) ++lb;
+    tune = tuned_config(TUNE_HIST, 0, GBK_I32, n, lb * 8, &tt);
+  }
   std::lock_guard<std::mutex> lk(w->mu);
   return hist_launch(keys, n, bins, nbins, w, tune);
 }

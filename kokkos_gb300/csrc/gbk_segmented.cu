@@ -332,9 +332,9 @@ __global__ void __launch_bounds__(BLOCK)
   }
 }
 
-template <class TI, class TO, int OP, int MODE>
-int launch_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t nseg, Workspace* w) {
-  constexpr int BLOCK = 256, IPT = 4, VEC = 16 / sizeof(TI);
+template <class TI, class TO, int OP, int MODE, int IPT>
+int launch_seg_ipt(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t nseg, Workspace* w) {
+  constexpr int BLOCK = 256, VEC = 16 / sizeof(TI);
   constexpr int64_t TILE = (int64_t)BLOCK * IPT * VEC;
   cudaStream_t s = w->stream;
   const int64_t nt = (n + TILE - 1) / TILE;
@@ -364,14 +364,33 @@ int launch_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t ns
   return cuda_status(cudaGetLastError());
 }
 
+// items_per_thread (16-byte vectors per thread per tile): 2, 4 (default), 8.
+template <class TI, class TO, int OP, int MODE>
+int launch_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t nseg, Workspace* w,
+               const gbk_tuning_t* t) {
+  const int ipt = t && t->items_per_thread ? t->items_per_thread : 4;
+  if (ipt == 2) return launch_seg_ipt<TI, TO, OP, MODE, 2>(x, y, n, offsets, nseg, w);
+  if (ipt == 8) return launch_seg_ipt<TI, TO, OP, MODE, 8>(x, y, n, offsets, nseg, w);
+  return launch_seg_ipt<TI, TO, OP, MODE, 4>(x, y, n, offsets, nseg, w);
+}
+
 template <class T>
-int seg_reduce_t(int op, const void* x, const int64_t* offs, int64_t nseg, int64_t n, void* out, Workspace* w) {
+int seg_reduce_t(int op, const void* x, const int64_t* offs, int64_t nseg, int64_t n, void* out, Workspace* w,
+                 const gbk_tuning_t* t) {
   switch (op) {
-    case GBK_SUM: return launch_seg<T, T, GBK_SUM, M_REDUCE>((const T*)x, (T*)out, n, offs, nseg, w);
-    case GBK_MIN: return launch_seg<T, T, GBK_MIN, M_REDUCE>((const T*)x, (T*)out, n, offs, nseg, w);
-    case GBK_MAX: return launch_seg<T, T, GBK_MAX, M_REDUCE>((const T*)x, (T*)out, n, offs, nseg, w);
+    case GBK_SUM: return launch_seg<T, T, GBK_SUM, M_REDUCE>((const T*)x, (T*)out, n, offs, nseg, w, t);
+    case GBK_MIN: return launch_seg<T, T, GBK_MIN, M_REDUCE>((const T*)x, (T*)out, n, offs, nseg, w, t);
+    case GBK_MAX: return launch_seg<T, T, GBK_MAX, M_REDUCE>((const T*)x, (T*)out, n, offs, nseg, w, t);
   }
   return GBK_ERR_UNSUPPORTED;
+}
+
+// Tuning-table extra for segmented calls: log2 of the mean segment length.
+int seg_extra(int64_t n, int64_t nseg) {
+  int64_t mean = nseg > 0 ? n / nseg : n;
+  int l = 0;
+  while (((int64_t)1 << l) < mean && l < 62) ++l;
+  return l;
 }
 
 }  // namespace
@@ -382,7 +401,7 @@ using namespace gbk;
 extern "C" {
 
 int gbk_segmented_reduce(gbk_reducer_t op, gbk_dtype_t dt, const void* x, const int64_t* offsets, int64_t nseg,
-                         int64_t n, void* out, gbk_stream_t stream) {
+                         int64_t n, void* out, gbk_stream_t stream, const gbk_tuning_t* tune) {
   if (op != GBK_SUM && op != GBK_MIN && op != GBK_MAX) return GBK_ERR_UNSUPPORTED;
   if (nseg < 0 || n < 0 || (nseg > 0 && (!offsets || !out)) || (n > 0 && !x)) return GBK_ERR_INVALID_ARGUMENT;
   if ((uintptr_t)x % dtype_size(dt) || (uintptr_t)out % dtype_size(dt)) return GBK_ERR_INVALID_ARGUMENT;
@@ -390,31 +409,35 @@ int gbk_segmented_reduce(gbk_reducer_t op, gbk_dtype_t dt, const void* x, const 
   int st = GBK_OK;
   Workspace* w = ws_get((cudaStream_t)stream, &st);
   if (!w) return st;
+  gbk_tuning_t tt;
+  if (!tune) tune = tuned_config(TUNE_SEG, op, dt, n, seg_extra(n, nseg), &tt);
   std::lock_guard<std::mutex> lk(w->mu);
   switch (dt) {
-    case GBK_I32: return seg_reduce_t<int32_t>(op, x, offsets, nseg, n, out, w);
-    case GBK_I64: return seg_reduce_t<int64_t>(op, x, offsets, nseg, n, out, w);
-    case GBK_U32: return seg_reduce_t<uint32_t>(op, x, offsets, nseg, n, out, w);
-    case GBK_U64: return seg_reduce_t<uint64_t>(op, x, offsets, nseg, n, out, w);
-    case GBK_F32: return seg_reduce_t<float>(op, x, offsets, nseg, n, out, w);
-    case GBK_F64: return seg_reduce_t<double>(op, x, offsets, nseg, n, out, w);
+    case GBK_I32: return seg_reduce_t<int32_t>(op, x, offsets, nseg, n, out, w, tune);
+    case GBK_I64: return seg_reduce_t<int64_t>(op, x, offsets, nseg, n, out, w, tune);
+    case GBK_U32: return seg_reduce_t<uint32_t>(op, x, offsets, nseg, n, out, w, tune);
+    case GBK_U64: return seg_reduce_t<uint64_t>(op, x, offsets, nseg, n, out, w, tune);
+    case GBK_F32: return seg_reduce_t<float>(op, x, offsets, nseg, n, out, w, tune);
+    case GBK_F64: return seg_reduce_t<double>(op, x, offsets, nseg, n, out, w, tune);
   }
   return GBK_ERR_UNSUPPORTED;
 }
 
 int gbk_segmented_scan(int inclusive, gbk_dtype_t din, gbk_dtype_t dout, const void* x, const int64_t* offsets,
-                       int64_t nseg, int64_t n, void* y, gbk_stream_t stream) {
+                       int64_t nseg, int64_t n, void* y, gbk_stream_t stream, const gbk_tuning_t* tune) {
   if (nseg < 0 || n < 0 || (n > 0 && (!x || !y || !offsets))) return GBK_ERR_INVALID_ARGUMENT;
   if ((uintptr_t)x % dtype_size(din) || (uintptr_t)y % dtype_size(dout)) return GBK_ERR_INVALID_ARGUMENT;
   if (n == 0) return GBK_OK;
   int st = GBK_OK;
   Workspace* w = ws_get((cudaStream_t)stream, &st);
   if (!w) return st;
+  gbk_tuning_t tt;
+  if (!tune) tune = tuned_config(TUNE_SEG, 16 + (inclusive ? 1 : 0), din * 8 + dout, n, seg_extra(n, nseg), &tt);
   std::lock_guard<std::mutex> lk(w->mu);
 #define GBK_SEGSCAN(A, TA, B, TB)                                                                              \
   if (din == A && dout == B)                                                                                   \
-    return inclusive ? launch_seg<TA, TB, GBK_SUM, M_INCL>((const TA*)x, (TB*)y, n, offsets, nseg, w)           \
-                     : launch_seg<TA, TB, GBK_SUM, M_EXCL>((const TA*)x, (TB*)y, n, offsets, nseg, w);
+    return inclusive ? launch_seg<TA, TB, GBK_SUM, M_INCL>((const TA*)x, (TB*)y, n, offsets, nseg, w, tune)     \
+                     : launch_seg<TA, TB, GBK_SUM, M_EXCL>((const TA*)x, (TB*)y, n, offsets, nseg, w, tune);
   GBK_SEGSCAN(GBK_I32, int32_t, GBK_I32, int32_t)
   GBK_SEGSCAN(GBK_I32, int32_t, GBK_I64, int64_t)
   GBK_SEGSCAN(GBK_I64, int64_t, GBK_I64, int64_t)

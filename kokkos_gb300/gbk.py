@@ -74,8 +74,20 @@ _SIGS = {
     "gbk_sort_by_key_u64_i32": ([vp, vp, i64, vp], ci),
     "gbk_binsort_u64": ([vp, i64, i64, ctypes.c_double, ctypes.c_double, ci, vp, vp, vp, vp], ci),
     "gbk_permute": ([ci, vp, vp, i64, vp, vp], ci),
-    "gbk_segmented_reduce": ([ci, ci, vp, vp, i64, i64, vp, vp], ci),
-    "gbk_segmented_scan": ([ci, ci, ci, vp, vp, i64, i64, vp, vp], ci),
+    "gbk_segmented_reduce": ([ci, ci, vp, vp, i64, i64, vp, vp, TP], ci),
+    "gbk_segmented_scan": ([ci, ci, ci, vp, vp, i64, i64, vp, vp, TP], ci),
+    "gbk_tuner_clear": ([], ci),
+    "gbk_tuner_set": ([ci, ci, ci, ci, ci, TP], ci),
+    "gbk_tuner_lookup": ([ci, ci, ci, i64, ci, TP], ci),
+    "gbk_tuner_load": ([ctypes.c_char_p], ci),
+    "gbk_tuner_save": ([ctypes.c_char_p], ci),
+    "gbk_tuner_enable": ([ci], ci),
+    "gbk_tuner_size": ([], i64),
+    "gbk_mlp_param_count": ([ci], i64),
+    "gbk_mlp_forward": ([vp, i64, ci, vp, vp, vp, vp], ci),
+    "gbk_mlp_backward": ([vp, i64, ci, vp, vp, vp, vp, vp], ci),
+    "gbk_mlp_mse": ([vp, vp, i64, vp, vp, vp], ci),
+    "gbk_mlp_adam": ([vp, vp, vp, vp, i64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ci, vp], ci),
     "gbk_graph_begin": ([vp], ci),
     "gbk_graph_end": ([vp, ctypes.POINTER(vp)], ci),
     "gbk_graph_launch": ([vp, vp], ci),
@@ -96,9 +108,12 @@ _bind()
 
 
 def declared_symbols():
-    """Every function name include/gbk.h declares (typed reduce macros expanded)."""
+    """Every function name include/gbk.h and include/gbk_tools.h declare
+    (typed reduce macros expanded, Kokkos Tools callbacks included)."""
     src = open(HEADER).read()
+    tools = open(os.path.join(ROOT, "include", "gbk_tools.h")).read()
     names = set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(gbk_\w+)\s*\(", src, re.M))
+    names |= set(re.findall(r"^\s*(?:int|int64_t|void)\s+((?:gbk|kokkosp)_\w+)\s*\(", tools, re.M))
     ints = ["i32", "i64", "u32", "u64"]
     alls = ints + ["f32", "f64"]
     for m in re.finditer(r"^GBK_FOR_EACH_(INT_)?DTYPE\(GBK_DECLARE_TYPED_REDUCE,\s*(\w+)\)", src, re.M):
@@ -275,19 +290,20 @@ def permute(src, perm, stream=None):
     return dst
 
 
-def segmented_reduce(op, x, offsets, out, stream=None):
+def segmented_reduce(op, x, offsets, out, stream=None, tune=None):
     """out[s] = op over x[offsets[s]:offsets[s+1]] for every segment, one launch."""
     opc = OPS[op] if isinstance(op, str) else op
     check(lib.gbk_segmented_reduce(opc, dtype_code(x.dtype), ctypes.c_void_p(x.data_ptr()),
                                    ctypes.c_void_p(offsets.data_ptr()), offsets.numel() - 1, x.numel(),
-                                   ctypes.c_void_p(out.data_ptr()), _stream(stream)), "segmented_reduce")
+                                   ctypes.c_void_p(out.data_ptr()), _stream(stream), _tune(tune)), "segmented_reduce")
     return out
 
 
-def segmented_scan(x, offsets, y, inclusive=True, stream=None):
+def segmented_scan(x, offsets, y, inclusive=True, stream=None, tune=None):
     check(lib.gbk_segmented_scan(1 if inclusive else 0, dtype_code(x.dtype), dtype_code(y.dtype),
                                  ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(offsets.data_ptr()),
-                                 offsets.numel() - 1, x.numel(), ctypes.c_void_p(y.data_ptr()), _stream(stream)),
+                                 offsets.numel() - 1, x.numel(), ctypes.c_void_p(y.data_ptr()), _stream(stream),
+                                 _tune(tune)),
           "segmented_scan")
     return y
 

@@ -1,0 +1,399 @@
+"""Autotuner and learned tuner for libgbk launch configurations.
+
+* Exhaustive autotuner: for a workload (operation kind, element type, size,
+  segment statistics, histogram bins and key entropy) every candidate launch
+  configuration is timed through the C ABI (CUDA events, median of repeats).
+* Learned tuner: a 3-layer, 64-hidden FP32 MLP (features of the workload and
+  of a candidate configuration -> log time), trained with the library's own
+  CUDA kernels (gbk_mlp_forward / backward / mse / adam); for an unseen
+  workload it picks the candidate with the smallest predicted time.  The
+  exhaustive tuner stays the fallback and the judge of its regret.
+* The tuning table (text, loaded by gbk_tuner_load) maps (kind, op, dtype,
+  log2 n, extra) to the chosen configuration; the entry points consult it
+  when called without an explicit configuration.
+
+    python -m kokkos_gb300.tuner --train-workloads 900 --eval-workloads 2000 --out gpurun_out/tuner
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+KIND_REDUCE, KIND_SCAN, KIND_HIST, KIND_SEG = 0, 1, 2, 3
+REDUCE_CFGS = [(b, u, c) for (b, u) in [(256, 2), (256, 4), (256, 8), (512, 2), (512, 4), (128, 8), (1024, 2)]
+               for c in (1, 2, 4, 8)]
+SCAN_CFGS = [2, 4, 8]
+SEG_CFGS = [2, 4, 8]
+# histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit, no privatisation
+HIST_CFGS_SMALL = [(0x01, 1), (0x01, 2), (0x11, 2), (0x20, 1), (0x30, 1), (0x40, 1)]
+HIST_CFGS_2E16 = [(0x02, 1), (0x12, 1), (0x04, 1), (0x20, 1), (0x30, 1), (0x40, 1)]
+REDUCE_OPS = [("sum", 5), ("sum", 4), ("minloc", 4), ("maxloc", 4), ("sum", 0), ("sum", 1)]  # (op, dtype code)
+OPC = {"sum": 0, "minloc": 8, "maxloc": 9}
+NFEAT = 24
+
+
+def candidates(w):
+    k = w["kind"]
+    if k == KIND_REDUCE:
+        return [{"block": b, "ipt": u, "cps": c, "variant": 0} for (b, u, c) in REDUCE_CFGS]
+    if k == KIND_SCAN:
+        return [{"block": 256, "ipt": u, "cps": 0, "variant": 0} for u in SCAN_CFGS]
+    if k == KIND_SEG:
+        return [{"block": 256, "ipt": u, "cps": 0, "variant": 0} for u in SEG_CFGS]
+    cf = HIST_CFGS_2E16 if w["nbins"] > 24576 else HIST_CFGS_SMALL
+    return [{"block": 0, "ipt": 0, "cps": c, "variant": v} for (v, c) in cf]
+
+
+def features(w, c):
+    """Workload + candidate features (NFEAT floats, roughly unit scale)."""
+    f = np.zeros(NFEAT, dtype=np.float32)
+    f[w["kind"]] = 1.0                                   # 0..3 kind one-hot
+    f[4 + w["dtype"]] = 1.0                              # 4..9 dtype one-hot
+    f[10] = {0: 0.0, 8: 1.0, 9: 1.0}.get(w.get("op", 0), 0.0)  # *Loc reducer
+    f[11] = (math.log2(max(w["n"], 1)) - 22.0) / 6.0     # size
+    f[12] = (w.get("seg_log2mean", 0.0) - 11.0) / 4.0    # segment-length mean (log2)
+    f[13] = w.get("seg_sigma", 0.0) / 2.0                # segment-length spread (lognormal sigma)
+    f[14] = (math.log2(max(w.get("nbins", 1), 1)) - 12.0) / 4.0
+    f[15] = w.get("entropy_bits", 0.0) / 16.0            # key entropy
+    f[16] = (math.log2(max(w.get("inner_extent", 1), 1))) / 10.0  # MDRange inner extent
+    f[17] = (math.log2(max(c["block"], 1)) - 8.0) / 2.0
+    f[18] = (math.log2(max(c["ipt"], 1)) - 2.0) / 1.5
+    f[19] = (math.log2(max(c["cps"], 1)) - 2.0) / 2.0
+    v = c["variant"]
+    f[20] = float((v & 0xF) > 1) if v and not (v & 0x60) else 0.0   # cluster-split bins
+    f[21] = float((v & 0x10) != 0)                       # warp aggregation
+    f[22] = float((v & 0x20) != 0)                       # 16-bit bins
+    f[23] = float((v & 0x40) != 0)                       # no privatisation
+    return f
+
+
+def sample_workloads(count, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        r = rng.random()
+        if r < 0.45:
+            op, dt = REDUCE_OPS[rng.integers(len(REDUCE_OPS))]
+            n = int(2 ** rng.uniform(16, 27 if dt in (1, 5) else 28))
+            out.append({"kind": KIND_REDUCE, "op": OPC[op], "opname": op, "dtype": dt, "n": n, "inner_extent": 1})
+        elif r < 0.65:
+            n = int(2 ** rng.uniform(16, 28))
+            out.append({"kind": KIND_SCAN, "op": int(rng.integers(2)), "dtype": 0, "n": n})
+        elif r < 0.82:
+            nb = int(rng.choice([256, 4096, 65536]))
+            out.append({"kind": KIND_HIST, "op": 0, "dtype": 0, "n": int(2 ** rng.uniform(16, 26)), "nbins": nb,
+                        "pool": int(rng.integers(5))})
+        else:
+            nseg = int(2 ** rng.uniform(6, 13.3))
+            l2m = float(rng.uniform(6, 13))
+            sig = float(rng.uniform(0.3, 2.5))
+            total = min(int(nseg * 2 ** l2m), 1 << 27)
+            out.append({"kind": KIND_SEG, "op": 0, "dtype": 4, "n": total, "nseg": nseg, "seg_log2mean": l2m,
+                        "seg_sigma": sig, "seed": int(rng.integers(1 << 30))})
+    return out
+
+
+class Bench:
+    """Device buffers reused by all workloads (prefixes of large seeded arrays)."""
+
+    def __init__(self, max_n=1 << 28):
+        import torch
+
+        from kokkos_gb300 import datagen, gbk
+        self.torch, self.gbk, self.datagen = torch, gbk, datagen
+        self.s = torch.cuda.Stream()
+        self.sp = ctypes.c_void_p(self.s.cuda_stream)
+        self.max_n = max_n
+        g = torch.Generator(device="cuda")
+        g.manual_seed(0)
+        self.f32 = torch.randn(max_n, device="cuda", generator=g)
+        self.f64 = self.f32[: max_n // 2].double()
+        self.i32 = torch.randint(0, 256, (max_n,), device="cuda", dtype=torch.int32, generator=g)
+        self.i64 = self.i32[: max_n // 2].long()
+        self.y64 = torch.empty(max_n, dtype=torch.int64, device="cuda")
+        self.res = torch.zeros(256, dtype=torch.uint8, device="cuda")
+        self.pools, self.pool_entropy = [], []
+        nk = min(1 << 26, max_n)
+        for i, s_ in enumerate([0.0, 0.6, 0.9, 1.1, 1.4]):
+            keys = datagen.uniform_i32(nk, 0, 65535, seed=i) if s_ == 0.0 else datagen.zipf_i32(nk, 65536, s_, seed=i)
+            self.pools.append(torch.from_numpy(keys).cuda())
+        self.bins = torch.zeros(65536, dtype=torch.int64, device="cuda")
+        self._ent = {}
+        self.seg_cache = {}
+
+    def entropy(self, pool, nbins):
+        key = (pool, nbins)
+        if key not in self._ent:
+            k = self.pools[pool][: 1 << 22] % nbins
+            c = self.torch.bincount(k.long(), minlength=nbins).double()
+            p = c[c > 0] / c.sum()
+            self._ent[key] = float(-(p * p.log2()).sum().item())
+        return self._ent[key]
+
+    def prepare(self, w):
+        if w["kind"] == KIND_REDUCE:
+            w["n"] = min(w["n"], (self.max_n // 2) if w["dtype"] in (1, 5) else self.max_n)
+        if w["kind"] in (KIND_SCAN,):
+            w["n"] = min(w["n"], self.max_n)
+        if w["kind"] == KIND_HIST:
+            w["n"] = min(w["n"], self.pools[0].numel())
+            w["entropy_bits"] = self.entropy(w["pool"], w["nbins"])
+            w["keys"] = (self.pools[w["pool"]][: w["n"]] % w["nbins"]).contiguous() if w["nbins"] < 65536 \
+                else self.pools[w["pool"]][: w["n"]]
+        if w["kind"] == KIND_SEG:
+            lens, _ = self.datagen.lognormal_lengths(w["nseg"], median=2 ** w["seg_log2mean"], max_len=1 << 24,
+                                                     target_total=min(w["n"], self.max_n // 2), seed=w["seed"])
+            lens = np.minimum(lens, max(1, (self.max_n // 2) // max(w["nseg"], 1)))
+            offs = self.datagen.offsets_from_lengths(lens)
+            w["n"] = int(offs[-1])
+            w["offsets"] = self.torch.from_numpy(offs).cuda()
+            w["segout"] = self.torch.empty(w["nseg"], dtype=self.torch.float32, device="cuda")
+
+    def call(self, w, c):
+        gbk, lib, sp = self.gbk, self.gbk.lib, self.sp
+        t = gbk.Tuning(c["block"], c["ipt"], c["cps"], c["variant"])
+        k = w["kind"]
+        if k == KIND_REDUCE:
+            buf = {5: self.f64, 4: self.f32, 0: self.i32, 1: self.i64}[w["dtype"]]
+            return lib.gbk_reduce(w["op"], w["dtype"], ctypes.c_void_p(buf.data_ptr()), w["n"],
+                                  ctypes.c_void_p(self.res.data_ptr()), sp, ctypes.byref(t))
+        if k == KIND_SCAN:
+            iv = ctypes.c_int64(0)
+            return lib.gbk_scan(w["op"], 0, 1, ctypes.c_void_p(self.i32.data_ptr()), w["n"], ctypes.byref(iv),
+                                ctypes.c_void_p(self.y64.data_ptr()), None, sp, ctypes.byref(t))
+        if k == KIND_HIST:
+            return lib.gbk_histogram_i32_i64(ctypes.c_void_p(w["keys"].data_ptr()), w["n"],
+                                             ctypes.c_void_p(self.bins.data_ptr()), w["nbins"], sp, ctypes.byref(t))
+        return lib.gbk_segmented_reduce(0, 4, ctypes.c_void_p(self.f32.data_ptr()),
+                                        ctypes.c_void_p(w["offsets"].data_ptr()), w["nseg"], w["n"],
+                                        ctypes.c_void_p(w["segout"].data_ptr()), sp, ctypes.byref(t))
+
+    def time(self, w, c, reps=3):
+        torch = self.torch
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps)]
+        st = self.call(w, c)  # warm-up
+        if st:
+            return float("inf")
+        for r in range(reps):
+            e[2 * r].record(self.s)
+            self.call(w, c)
+            e[2 * r + 1].record(self.s)
+        e[-1].synchronize()
+        return float(np.median([e[2 * r].elapsed_time(e[2 * r + 1]) for r in range(reps)])) * 1e3  # us
+
+    def sweep(self, w):
+        self.prepare(w)
+        cs = candidates(w)
+        ts = [self.time(w, c) for c in cs]
+        for key in ("keys", "offsets", "segout"):
+            w.pop(key, None)
+        self.gbk.stream_check(self.s)
+        return cs, ts
+
+
+def collect(workloads, bench, log_every=200):
+    rows = []
+    t0 = time.time()
+    for i, w in enumerate(workloads):
+        cs, ts = bench.sweep(w)
+        rows.append((dict(w), cs, ts))
+        if log_every and (i + 1) % log_every == 0:
+            print(f"  swept {i + 1}/{len(workloads)} workloads ({time.time() - t0:.0f} s)", flush=True)
+    return rows
+
+
+class MLP:
+    """FP32 MLP D -> 64 -> 64 -> 1 trained and run by libgbk's CUDA kernels."""
+
+    def __init__(self, D=NFEAT, seed=0):
+        import torch
+
+        from kokkos_gb300 import gbk
+        self.torch, self.gbk, self.D = torch, gbk, D
+        self.P = int(gbk.lib.gbk_mlp_param_count(D))
+        rng = np.random.default_rng(seed)
+        p = np.zeros(self.P, dtype=np.float32)
+        H = 64
+        o = 0
+        p[o:o + D * H] = rng.normal(0, math.sqrt(2.0 / D), D * H)
+        o += D * H + H
+        p[o:o + H * H] = rng.normal(0, math.sqrt(2.0 / H), H * H)
+        o += H * H + H
+        p[o:o + H] = rng.normal(0, math.sqrt(1.0 / H), H)
+        self.params = torch.from_numpy(p).cuda()
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.grads = torch.zeros_like(self.params)
+        self.t = 0
+        self.mu, self.sd = 0.0, 1.0
+
+    def _ptr(self, t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def forward(self, X):
+        torch = self.torch
+        B = X.shape[0]
+        acts = torch.empty(B * 128, dtype=torch.float32, device="cuda")
+        Y = torch.empty(B, dtype=torch.float32, device="cuda")
+        self.gbk.check(self.gbk.lib.gbk_mlp_forward(self._ptr(X), B, self.D, self._ptr(self.params), self._ptr(acts),
+                                                    self._ptr(Y), None), "mlp_forward")
+        return Y, acts
+
+    def train(self, X, T, epochs=300, batch=4096, lr=2e-3, seed=0):
+        """X: [N, D] float32, T: [N] target log-times (standardised here)."""
+        torch, lib = self.torch, self.gbk.lib
+        self.mu, self.sd = float(T.mean()), float(T.std() + 1e-6)
+        Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float32)).cuda()
+        Td = torch.from_numpy(((T - self.mu) / self.sd).astype(np.float32)).cuda()
+        N = Xd.shape[0]
+        rng = np.random.default_rng(seed)
+        loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+        hist = []
+        for ep in range(epochs):
+            perm = torch.from_numpy(rng.permutation(N)).cuda()
+            el = 0.0
+            nb = 0
+            for s in range(0, N, batch):
+                idx = perm[s:s + batch]
+                xb, tb = Xd[idx].contiguous(), Td[idx].contiguous()
+                B = xb.shape[0]
+                Y, acts = self.forward(xb)
+                dY = torch.empty(B, dtype=torch.float32, device="cuda")
+                self.gbk.check(lib.gbk_mlp_mse(self._ptr(Y), self._ptr(tb), B, self._ptr(dY), self._ptr(loss), None))
+                self.gbk.check(lib.gbk_mlp_backward(self._ptr(xb), B, self.D, self._ptr(self.params),
+                                                    self._ptr(acts), self._ptr(dY), self._ptr(self.grads), None))
+                self.t += 1
+                self.gbk.check(lib.gbk_mlp_adam(self._ptr(self.params), self._ptr(self.grads), self._ptr(self.m),
+                                                self._ptr(self.v), self.P, lr, 0.9, 0.999, 1e-8, self.t, None))
+                if ep % 25 == 0 or ep == epochs - 1:
+                    el += float(loss.item())
+                    nb += 1
+            if nb:
+                hist.append((ep, el / nb))
+        return hist
+
+    def predict(self, X):
+        Xd = self.torch.from_numpy(np.ascontiguousarray(X, dtype=np.float32)).cuda()
+        Y, _ = self.forward(Xd)
+        return Y.cpu().numpy() * self.sd + self.mu
+
+
+def default_cfg_index(w, cs):
+    """The configuration the library uses without tuning."""
+    k = w["kind"]
+    for i, c in enumerate(cs):
+        if k == KIND_REDUCE and (c["block"], c["ipt"], c["cps"]) == (256, 4, 8):
+            return i
+        if k in (KIND_SCAN, KIND_SEG) and c["ipt"] == 4:
+            return i
+        if k == KIND_HIST:
+            want = 0x20 if w["nbins"] > 24576 else 0x01
+            if c["variant"] == want:
+                return i
+    return 0
+
+
+def dataset(rows):
+    X, T, grp = [], [], []
+    for gi, (w, cs, ts) in enumerate(rows):
+        for c, t in zip(cs, ts):
+            if math.isfinite(t) and t > 0:
+                X.append(features(w, c))
+                T.append(math.log(t))
+                grp.append(gi)
+    return np.array(X, dtype=np.float32), np.array(T, dtype=np.float64), np.array(grp)
+
+
+def evaluate(model, rows):
+    """Throughput of the predicted-best and of the default configuration
+    relative to the exhaustive best, per held-out workload."""
+    pred_ratio, def_ratio = [], []
+    per_kind = {}
+    for (w, cs, ts) in rows:
+        ts = np.array(ts)
+        ok = np.isfinite(ts)
+        if not ok.any():
+            continue
+        best = ts[ok].min()
+        X = np.stack([features(w, c) for c in cs])
+        p = model.predict(X)
+        p[~ok] = np.inf
+        pr = best / ts[int(np.argmin(p))]
+        dr = best / ts[default_cfg_index(w, cs)]
+        pred_ratio.append(pr)
+        def_ratio.append(dr)
+        per_kind.setdefault(w["kind"], []).append((pr, dr))
+    return {
+        "workloads": len(pred_ratio),
+        "mlp_mean_throughput_vs_best": float(np.mean(pred_ratio)),
+        "mlp_geomean_throughput_vs_best": float(np.exp(np.mean(np.log(pred_ratio)))),
+        "default_mean_throughput_vs_best": float(np.mean(def_ratio)),
+        "mlp_frac_within_5pct": float(np.mean(np.array(pred_ratio) >= 0.95)),
+        "per_kind": {str(k): {"n": len(v), "mlp": float(np.mean([a for a, _ in v])),
+                              "default": float(np.mean([b for _, b in v]))} for k, v in per_kind.items()},
+    }
+
+
+def table_from_model(model, path):
+    """Tuning table over a grid of workload buckets, from the MLP's choices."""
+    lines = ["# kind op dtype log2n extra block items_per_thread ctas_per_sm variant"]
+    for l2 in range(16, 29):
+        for op, dt in REDUCE_OPS:
+            w = {"kind": KIND_REDUCE, "op": OPC[op], "dtype": dt, "n": 1 << l2}
+            cs = candidates(w)
+            c = cs[int(np.argmin(model.predict(np.stack([features(w, c) for c in cs]))))]
+            lines.append(f"0 {OPC[op]} {dt} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0")
+        for inc in (0, 1):
+            w = {"kind": KIND_SCAN, "op": inc, "dtype": 0, "n": 1 << l2}
+            cs = candidates(w)
+            c = cs[int(np.argmin(model.predict(np.stack([features(w, c) for c in cs]))))]
+            lines.append(f"1 {inc} {0 * 8 + 1} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0")
+        for nb in (256, 4096, 65536):
+            w = {"kind": KIND_HIST, "op": 0, "dtype": 0, "n": 1 << l2, "nbins": nb, "entropy_bits": 10.0}
+            cs = candidates(w)
+            c = cs[int(np.argmin(model.predict(np.stack([features(w, c) for c in cs]))))]
+            lines.append(f"2 0 0 {l2} {int(math.log2(nb)) * 8} 0 0 {c['cps']} {c['variant']}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return path
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train-workloads", type=int, default=900)
+    ap.add_argument("--eval-workloads", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=300)
+    ap.add_argument("--out", default="gpurun_out/tuner")
+    ap.add_argument("--max-n", type=int, default=1 << 28)
+    args = ap.parse_args()
+    os.makedirs(args.out, exist_ok=True)
+    bench = Bench(args.max_n)
+    t0 = time.time()
+    train_w = sample_workloads(args.train_workloads, seed=1)
+    eval_w = sample_workloads(args.eval_workloads, seed=2)
+    train_rows = collect(train_w, bench)
+    eval_rows = collect(eval_w, bench)
+    t_collect = time.time() - t0
+    X, T, _ = dataset(train_rows)
+    model = MLP(seed=0)
+    t1 = time.time()
+    hist = model.train(X, T, epochs=args.epochs)
+    t_train = time.time() - t1
+    rep = evaluate(model, eval_rows)
+    rep.update({"train_timings": int(X.shape[0]), "eval_timings": int(sum(len(r[2]) for r in eval_rows)),
+                "collect_s": round(t_collect, 1), "train_s": round(t_train, 1), "loss_history": hist[::4] + hist[-1:]})
+    table_from_model(model, os.path.join(args.out, "tuning_table.txt"))
+    np.save(os.path.join(args.out, "mlp_params.npy"), model.params.cpu().numpy())
+    with open(os.path.join(args.out, "tuner_eval.json"), "w") as f:
+        json.dump(rep, f, indent=1)
+    print(json.dumps({k: v for k, v in rep.items() if k != "loss_history"}, indent=1))
+
+
+if __name__ == "__main__":
+    main()
