@@ -1,0 +1,410 @@
+// Core of the header-template path: execution space, memory spaces, View,
+// deep_copy and the execution policies, with the names and argument meaning
+// of the reference (core/src/Kokkos_Core.hpp, View core/src/View/*,
+// policies core/src/Kokkos_ExecPolicy.hpp:77-1000,
+// core/src/KokkosExp_MDRangePolicy.hpp:159-425).  Compiled by nvcc in the
+// user's translation unit (-std=c++17 --extended-lambda).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <initializer_list>
+#include <ostream>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+
+#include "../gbk.h"
+#include "../gbk_tools.h"
+
+#ifndef KOKKOS_LAMBDA
+#define KOKKOS_LAMBDA [=] __host__ __device__
+#define KOKKOS_CLASS_LAMBDA [ =, *this ] __host__ __device__
+#define KOKKOS_FUNCTION __host__ __device__
+#define KOKKOS_INLINE_FUNCTION __host__ __device__ inline
+#define KOKKOS_FORCEINLINE_FUNCTION __host__ __device__ __forceinline__
+#endif
+
+namespace gb300k {
+
+// Error convention of the reference: a failing device call throws
+// (core/src/Cuda/Kokkos_Cuda_Error.hpp:33-67, impl/Kokkos_Error.hpp).
+inline void check(int status, const char* what) {
+  if (status != GBK_OK) throw std::runtime_error(std::string(what) + ": " + gbk_status_string(status));
+}
+inline void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+struct LayoutLeft {};
+struct LayoutRight {};
+struct HostSpace {};
+struct GB300Space {};
+
+namespace Experimental {
+// The execution space (core/src/Cuda/Kokkos_Cuda.hpp:95-260 is the device
+// model): one CUDA stream; fence() = gbk_stream_check, which also reports
+// device conditions (a bounded wait that gave up, a key outside the bins).
+class GB300 {
+ public:
+  using execution_space = GB300;
+  using memory_space = GB300Space;
+  using array_layout = LayoutLeft;
+  using size_type = int64_t;
+  GB300() = default;
+  explicit GB300(cudaStream_t s) : stream_(s) {}
+  cudaStream_t stream() const { return stream_; }
+  gbk_stream_t handle() const { return (gbk_stream_t)stream_; }
+  void fence(const std::string& = std::string()) const { check(gbk_stream_check(handle()), "GB300::fence"); }
+  static void impl_static_fence(const std::string& = std::string()) {
+    check_cuda(cudaDeviceSynchronize(), "GB300::impl_static_fence");
+  }
+  int concurrency() const {
+    int sm = 0;
+    gbk_device_info(&sm, nullptr, nullptr, nullptr);
+    return sm * 2048;
+  }
+  void print_configuration(std::ostream& os, bool = false) const {
+    int sm = 0, ma = 0, mi = 0;
+    int64_t l2 = 0;
+    gbk_device_info(&sm, &ma, &mi, &l2);
+    os << "GB300 execution space: " << sm << " SMs, compute capability " << ma << "." << mi << ", L2 " << l2
+       << " bytes\n";
+  }
+  static const char* name() { return "GB300"; }
+
+ private:
+  cudaStream_t stream_ = nullptr;
+};
+}  // namespace Experimental
+
+using DefaultExecutionSpace = Experimental::GB300;
+
+// initialize(): GBK_TUNING_TABLE=<file> loads a tuning table (as written by
+// the autotuner) and enables it for every call made without a configuration.
+inline void initialize(int = 0, char** = nullptr) {
+  if (const char* p = std::getenv("GBK_TUNING_TABLE")) {
+    if (gbk_tuner_load(p) == GBK_OK) gbk_tuner_enable(1);
+  }
+}
+inline void finalize() { check_cuda(cudaDeviceSynchronize(), "finalize"); }
+inline void fence(const std::string& = std::string()) { Experimental::GB300::impl_static_fence(); }
+
+// ---------------------------------------------------------------------------
+// View: rank 1..3, LayoutLeft / LayoutRight, device (GB300Space) or host.
+namespace Impl {
+template <class D> struct ViewRank;
+template <class T> struct ViewRank<T*> { using value_type = T; static constexpr int rank = 1; };
+template <class T> struct ViewRank<T**> { using value_type = T; static constexpr int rank = 2; };
+template <class T> struct ViewRank<T***> { using value_type = T; static constexpr int rank = 3; };
+template <class T> struct ViewRank<T****> { using value_type = T; static constexpr int rank = 4; };
+
+template <class... P> struct ViewProps;
+template <> struct ViewProps<> { using layout = LayoutLeft; using space = GB300Space; };
+template <class... P> struct ViewProps<LayoutLeft, P...> { using layout = LayoutLeft; using space = typename ViewProps<P...>::space; };
+template <class... P> struct ViewProps<LayoutRight, P...> { using layout = LayoutRight; using space = typename ViewProps<P...>::space; };
+template <class... P> struct ViewProps<HostSpace, P...> { using layout = LayoutRight; using space = HostSpace; };
+template <class... P> struct ViewProps<GB300Space, P...> { using layout = typename ViewProps<P...>::layout; using space = GB300Space; };
+template <class... P> struct ViewProps<Experimental::GB300, P...> { using layout = typename ViewProps<P...>::layout; using space = GB300Space; };
+
+// Host-side reference count of a View allocation (copies made in device code
+// do not touch it).
+struct Tracker {
+  std::atomic<long> count{1};
+  void* ptr = nullptr;
+  bool device = true;
+  std::string label;
+};
+}  // namespace Impl
+
+template <class DataType, class... Props>
+class View {
+ public:
+  using traits = Impl::ViewRank<DataType>;
+  using value_type = typename traits::value_type;
+  using non_const_value_type = std::remove_const_t<value_type>;
+  using array_layout = typename Impl::ViewProps<Props...>::layout;
+  using memory_space = typename Impl::ViewProps<Props...>::space;
+  using pointer_type = value_type*;
+  static constexpr int rank = traits::rank;
+  static constexpr bool is_device = std::is_same<memory_space, GB300Space>::value;
+
+  KOKKOS_INLINE_FUNCTION View() {}
+  View(const std::string& label, int64_t n0, int64_t n1 = 1, int64_t n2 = 1, int64_t n3 = 1) {
+    set_extents(n0, n1, n2, n3);
+    const size_t bytes = sizeof(value_type) * (size_t)size();
+    trk_ = new Impl::Tracker();
+    trk_->label = label;
+    trk_->device = is_device;
+    if (bytes) {
+      if (is_device) check_cuda(cudaMalloc(&trk_->ptr, bytes), "View allocation");
+      else trk_->ptr = std::malloc(bytes);
+      if (is_device) check_cuda(cudaMemset(trk_->ptr, 0, bytes), "View initialisation");
+      else std::memset(trk_->ptr, 0, bytes);
+    }
+    ptr_ = (value_type*)trk_->ptr;
+  }
+  // Unmanaged view of caller memory.
+  KOKKOS_INLINE_FUNCTION View(value_type* p, int64_t n0, int64_t n1 = 1, int64_t n2 = 1, int64_t n3 = 1) : ptr_(p) {
+    set_extents(n0, n1, n2, n3);
+  }
+  KOKKOS_INLINE_FUNCTION View(const View& o) : ptr_(o.ptr_), trk_(o.trk_) {
+    for (int d = 0; d < 4; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
+    retain();
+  }
+  // Same data type, layout and memory space spelled with other properties
+  // (View<T*> and View<T*, LayoutLeft> on the device are the same view).
+  template <class... P2,
+            std::enable_if_t<std::is_same<typename View<DataType, P2...>::array_layout, array_layout>::value &&
+                                 std::is_same<typename View<DataType, P2...>::memory_space, memory_space>::value &&
+                                 !std::is_same<View<DataType, P2...>, View>::value,
+                             bool> = true>
+  KOKKOS_INLINE_FUNCTION View(const View<DataType, P2...>& o) : ptr_(o.ptr_), trk_(o.trk_) {
+    for (int d = 0; d < 4; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
+    retain();
+  }
+  template <class D2, class... P2>
+  friend class View;
+
+  KOKKOS_INLINE_FUNCTION View& operator=(const View& o) {
+    if (this != &o) {
+      release();
+      ptr_ = o.ptr_;
+      trk_ = o.trk_;
+      for (int d = 0; d < 4; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
+      retain();
+    }
+    return *this;
+  }
+  KOKKOS_INLINE_FUNCTION ~View() { release(); }
+
+  KOKKOS_FORCEINLINE_FUNCTION value_type& operator()(int64_t i) const { return ptr_[i * str_[0]]; }
+  KOKKOS_FORCEINLINE_FUNCTION value_type& operator()(int64_t i, int64_t j) const { return ptr_[i * str_[0] + j * str_[1]]; }
+  KOKKOS_FORCEINLINE_FUNCTION value_type& operator()(int64_t i, int64_t j, int64_t k) const {
+    return ptr_[i * str_[0] + j * str_[1] + k * str_[2]];
+  }
+  KOKKOS_FORCEINLINE_FUNCTION value_type& operator()(int64_t i, int64_t j, int64_t k, int64_t l) const {
+    return ptr_[i * str_[0] + j * str_[1] + k * str_[2] + l * str_[3]];
+  }
+  KOKKOS_FORCEINLINE_FUNCTION value_type& operator[](int64_t i) const { return ptr_[i]; }
+  KOKKOS_INLINE_FUNCTION value_type* data() const { return ptr_; }
+  KOKKOS_INLINE_FUNCTION int64_t extent(int d) const { return d < rank ? ext_[d] : 1; }
+  KOKKOS_INLINE_FUNCTION int64_t extent_int(int d) const { return extent(d); }
+  KOKKOS_INLINE_FUNCTION int64_t stride(int d) const { return str_[d]; }
+  KOKKOS_INLINE_FUNCTION int64_t size() const {
+    int64_t s = 1;
+    for (int d = 0; d < rank; ++d) s *= ext_[d];
+    return s;
+  }
+  KOKKOS_INLINE_FUNCTION int64_t span() const { return size(); }
+  std::string label() const { return trk_ ? trk_->label : std::string(); }
+  long use_count() const { return trk_ ? trk_->count.load() : 0; }
+
+ private:
+  KOKKOS_INLINE_FUNCTION void set_extents(int64_t n0, int64_t n1, int64_t n2, int64_t n3) {
+    const int64_t e[4] = {n0, n1, n2, n3};
+    for (int d = 0; d < 4; ++d) ext_[d] = d < rank ? e[d] : 1;
+    if (std::is_same<array_layout, LayoutLeft>::value) {
+      int64_t s = 1;
+      for (int d = 0; d < 4; ++d) { str_[d] = s; s *= ext_[d]; }
+    } else {
+      int64_t s = 1;
+      for (int d = rank - 1; d >= 0; --d) { str_[d] = s; s *= ext_[d]; }
+      for (int d = rank; d < 4; ++d) str_[d] = s;
+    }
+  }
+  KOKKOS_INLINE_FUNCTION void retain() {
+#ifndef __CUDA_ARCH__
+    if (trk_) trk_->count.fetch_add(1);
+#endif
+  }
+  KOKKOS_INLINE_FUNCTION void release() {
+#ifndef __CUDA_ARCH__
+    if (trk_ && trk_->count.fetch_sub(1) == 1) {
+      if (trk_->ptr) {
+        if (trk_->device) cudaFree(trk_->ptr);
+        else std::free(trk_->ptr);
+      }
+      delete trk_;
+    }
+    trk_ = nullptr;
+#endif
+  }
+
+  value_type* ptr_ = nullptr;
+  Impl::Tracker* trk_ = nullptr;
+  int64_t ext_[4] = {0, 1, 1, 1};
+  int64_t str_[4] = {1, 1, 1, 1};
+};
+
+template <class D, class... P>
+auto create_mirror_view(const View<D, P...>& v) {
+  using L = typename View<D, P...>::array_layout;
+  return View<D, L, HostSpace>(v.label() + "_mirror", v.extent(0), v.extent(1), v.extent(2), v.extent(3));
+}
+
+// deep_copy between views of equal extents and layout (one contiguous copy)
+template <class D1, class... P1, class D2, class... P2>
+void deep_copy(const View<D1, P1...>& dst, const View<D2, P2...>& src) {
+  static_assert(sizeof(typename View<D1, P1...>::value_type) == sizeof(typename View<D2, P2...>::value_type),
+                "deep_copy: element types differ");
+  if (dst.size() != src.size()) throw std::runtime_error("deep_copy: extents differ");
+  check(gbk_deep_copy(dst.data(), src.data(), (int64_t)(sizeof(typename View<D1, P1...>::value_type) * dst.size()),
+                      nullptr),
+        "deep_copy");
+  check_cuda(cudaStreamSynchronize(nullptr), "deep_copy");
+}
+
+// ---------------------------------------------------------------------------
+// Policies
+struct ChunkSize {
+  int value;
+  explicit ChunkSize(int v) : value(v) {}
+};
+
+template <class ExecSpace = Experimental::GB300, class... Rest>
+class RangePolicy {
+ public:
+  using execution_space = ExecSpace;
+  using index_type = int64_t;
+  RangePolicy(int64_t b, int64_t e) : begin_(b), end_(e) { validate(); }
+  RangePolicy(const ExecSpace& s, int64_t b, int64_t e) : space_(s), begin_(b), end_(e) { validate(); }
+  RangePolicy(int64_t b, int64_t e, ChunkSize c) : begin_(b), end_(e), chunk_(c.value) { validate(); }
+  int64_t begin() const { return begin_; }
+  int64_t end() const { return end_; }
+  const ExecSpace& space() const { return space_; }
+  int64_t chunk_size() const { return chunk_; }
+  RangePolicy& set_chunk_size(int c) { chunk_ = c; return *this; }
+
+ private:
+  void validate() {
+    if (end_ < begin_) throw std::runtime_error("Kokkos::RangePolicy bounds error: begin > end");
+  }
+  ExecSpace space_{};
+  int64_t begin_ = 0, end_ = 0, chunk_ = 0;
+};
+
+enum class Iterate { Default, Left, Right };
+template <unsigned N, Iterate OuterDir = Iterate::Default, Iterate InnerDir = Iterate::Default>
+struct Rank {
+  static constexpr int rank = N;
+};
+
+template <class RankT, class ExecSpace = Experimental::GB300>
+class MDRangePolicy {
+ public:
+  static constexpr int rank = RankT::rank;
+  static_assert(rank >= 2 && rank <= 4, "MDRangePolicy rank 2..4");
+  using execution_space = ExecSpace;
+  MDRangePolicy(std::initializer_list<int64_t> lo, std::initializer_list<int64_t> up) { set(lo, up); }
+  MDRangePolicy(const ExecSpace& s, std::initializer_list<int64_t> lo, std::initializer_list<int64_t> up) : space_(s) {
+    set(lo, up);
+  }
+  int64_t lower(int d) const { return lo_[d]; }
+  int64_t upper(int d) const { return up_[d]; }
+  const ExecSpace& space() const { return space_; }
+
+ private:
+  void set(std::initializer_list<int64_t> lo, std::initializer_list<int64_t> up) {
+    if ((int)lo.size() != rank || (int)up.size() != rank) throw std::runtime_error("MDRangePolicy: wrong rank");
+    int d = 0;
+    for (auto v : lo) lo_[d++] = v;
+    d = 0;
+    for (auto v : up) up_[d++] = v;
+    for (d = 0; d < rank; ++d)
+      if (up_[d] < lo_[d]) throw std::runtime_error("MDRangePolicy bounds error");
+  }
+  ExecSpace space_{};
+  int64_t lo_[4] = {0, 0, 0, 0}, up_[4] = {0, 0, 0, 0};
+};
+
+struct AUTO_t {};
+constexpr AUTO_t AUTO{};
+
+// Team member: one team = one CTA (team_size threads), league ranks
+// distributed over the grid (core/src/Cuda/Kokkos_Cuda_Team.hpp:72-360 is the
+// reference's device member).
+// Member functions are host-device (they are called from KOKKOS_LAMBDA
+// bodies); they only do work in device code.
+class TeamMember {
+ public:
+  KOKKOS_INLINE_FUNCTION TeamMember(int64_t league_rank, int64_t league_size) : lr_(league_rank), ls_(league_size) {}
+  KOKKOS_INLINE_FUNCTION int64_t league_rank() const { return lr_; }
+  KOKKOS_INLINE_FUNCTION int64_t league_size() const { return ls_; }
+  KOKKOS_INLINE_FUNCTION int team_rank() const {
+#ifdef __CUDA_ARCH__
+    return threadIdx.x;
+#else
+    return 0;
+#endif
+  }
+  KOKKOS_INLINE_FUNCTION int team_size() const {
+#ifdef __CUDA_ARCH__
+    return blockDim.x;
+#else
+    return 1;
+#endif
+  }
+  KOKKOS_INLINE_FUNCTION void team_barrier() const {
+#ifdef __CUDA_ARCH__
+    __syncthreads();
+#endif
+  }
+
+ private:
+  int64_t lr_, ls_;
+};
+
+template <class ExecSpace = Experimental::GB300, class... Rest>
+class TeamPolicy {
+ public:
+  using execution_space = ExecSpace;
+  using member_type = TeamMember;
+  TeamPolicy(int64_t league, int team) : league_(league), team_(team) { validate(); }
+  TeamPolicy(int64_t league, AUTO_t) : league_(league), team_(256) { validate(); }
+  TeamPolicy(int64_t league, int team, int) : league_(league), team_(team) { validate(); }
+  TeamPolicy(const ExecSpace& s, int64_t league, int team) : space_(s), league_(league), team_(team) { validate(); }
+  TeamPolicy(const ExecSpace& s, int64_t league, AUTO_t) : space_(s), league_(league), team_(256) { validate(); }
+  int64_t league_size() const { return league_; }
+  int team_size() const { return team_; }
+  const ExecSpace& space() const { return space_; }
+
+ private:
+  void validate() {
+    if (team_ < 32 || team_ > 1024 || team_ % 32) throw std::runtime_error("TeamPolicy: team size must be 32..1024, multiple of 32");
+    if (league_ < 0) throw std::runtime_error("TeamPolicy: negative league size");
+  }
+  ExecSpace space_{};
+  int64_t league_ = 0;
+  int team_ = 256;
+};
+
+template <class IndexT = int64_t>
+struct TeamThreadRangeBoundaries {
+  const TeamMember& member;
+  int64_t begin, end;
+};
+KOKKOS_INLINE_FUNCTION TeamThreadRangeBoundaries<> TeamThreadRange(const TeamMember& m, int64_t n) {
+  return {m, 0, n};
+}
+KOKKOS_INLINE_FUNCTION TeamThreadRangeBoundaries<> TeamThreadRange(const TeamMember& m, int64_t b, int64_t e) {
+  return {m, b, e};
+}
+
+struct PerTeamTag {
+  const TeamMember& member;
+};
+KOKKOS_INLINE_FUNCTION PerTeamTag PerTeam(const TeamMember& m) { return {m}; }
+template <class F>
+KOKKOS_INLINE_FUNCTION void single(const PerTeamTag& t, const F& f) {
+#ifdef __CUDA_ARCH__
+  if (t.member.team_rank() == 0) f();
+  __syncthreads();
+#endif
+}
+
+}  // namespace gb300k

@@ -1,0 +1,385 @@
+// parallel_for / parallel_reduce over RangePolicy, MDRangePolicy and
+// TeamPolicy for user functors, plus the nested TeamThreadRange /
+// ThreadVectorRange patterns (core/src/Kokkos_Parallel.hpp,
+// core/src/Kokkos_Parallel_Reduce.hpp:1684-1790; the reference's CUDA
+// versions are core/src/Cuda/Kokkos_Cuda_Parallel_Range.hpp,
+// Kokkos_Cuda_Parallel_MDRange.hpp, Kokkos_Cuda_Parallel_Team.hpp,
+// Kokkos_Cuda_Team.hpp:517-810).
+//
+// Kernel shape (the library's flat-reduce skeleton, instantiated for the
+// user's functor): a grid of at most SMs x 8 CTAs of 256 threads, each CTA
+// owning one contiguous, equal share of the index space with its threads
+// striding by 256 (coalesced for functors that read x(i)); a warp butterfly
+// and a CTA tree of the reducer's join; the last CTA to take a ticket
+// combines the per-CTA partials in CTA order — one launch, deterministic for
+// a given device.  A host-scalar result is copied back and the space fenced
+// (the reference's fence rule, Kokkos_Parallel_Reduce.hpp:1581-1640); a View
+// result is written on the device without a fence.
+#pragma once
+
+#include <string>
+
+#include "reducers.hpp"
+
+namespace gb300k {
+namespace Impl {
+
+constexpr int kBlock = 256;
+constexpr int kSlotReduce = 32;  // library ticket slot used by header reduces
+
+struct Scratch {
+  char* base;
+  unsigned* counters;
+  int* err;
+};
+inline Scratch acquire(cudaStream_t s, size_t bytes) {
+  void* p = nullptr;
+  unsigned* c = nullptr;
+  int* e = nullptr;
+  check(gbk_workspace_acquire((gbk_stream_t)s, (int64_t)bytes, &p, &c, &e), "workspace");
+  return {(char*)p, c, e};
+}
+inline int num_sms() {
+  static int sm = 0;
+  if (!sm) gbk_device_info(&sm, nullptr, nullptr, nullptr);
+  return sm > 0 ? sm : 1;
+}
+inline void launched(cudaError_t e, const char* what) {
+  check_cuda(e, what);
+  gbk_note_launches(1);
+}
+
+template <class V>
+__device__ V ld_cg(const V* p) {
+  V r;
+  const unsigned* s = reinterpret_cast<const unsigned*>(p);
+  unsigned* d = reinterpret_cast<unsigned*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(V) / 4); ++i) d[i] = __ldcg(s + i);
+  return r;
+}
+
+template <class Red, class V>
+__device__ void grid_finish_obj(const Red& red, V acc, V* partials, unsigned* counter, V* out) {
+  __shared__ __align__(16) unsigned char smraw[32 * sizeof(V)];
+  __shared__ unsigned s_ticket;
+  V* sm = reinterpret_cast<V*>(smraw);
+  acc = block_reduce_obj(red, acc, sm);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = acc;
+    __threadfence();
+    s_ticket = atomicAdd(counter, 1u);
+  }
+  __syncthreads();
+  if (s_ticket != gridDim.x - 1) return;
+  __threadfence();
+  V a;
+  red.init(a);
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    V p = ld_cg(partials + i);
+    red.join(a, p);
+  }
+  a = block_reduce_obj(red, a, sm);
+  if (threadIdx.x == 0) {
+    *out = a;
+    *counter = 0u;
+  }
+}
+
+__device__ inline void cta_share(int64_t n, int64_t* c0, int64_t* c1) {
+  const int64_t per = n / gridDim.x, rem = n % gridDim.x, b = blockIdx.x;
+  *c0 = b * per + (b < rem ? b : rem);
+  *c1 = *c0 + per + (b < rem ? 1 : 0);
+}
+
+// ---- RangePolicy ------------------------------------------------------------
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_range_for(F f, int64_t b, int64_t n) {
+  int64_t c0, c1;
+  cta_share(n, &c0, &c1);
+  for (int64_t i = c0 + threadIdx.x; i < c1; i += kBlock) f(b + i);
+}
+
+template <class F, class Red, class V>
+__global__ void __launch_bounds__(kBlock)
+    k_range_reduce(F f, Red red, int64_t b, int64_t n, V* partials, unsigned* counter, V* out) {
+  V v;
+  red.init(v);
+  int64_t c0, c1;
+  cta_share(n, &c0, &c1);
+  for (int64_t i = c0 + threadIdx.x; i < c1; i += kBlock) f(b + i, v);
+  grid_finish_obj(red, v, partials, counter, out);
+}
+
+// ---- MDRangePolicy (index 0 fastest: the GPU default Iterate::Left) -----------
+struct MDArgs {
+  int64_t lo[4], ext[4];
+  int rank;
+};
+template <int R, class F, class... A>
+__device__ __forceinline__ void md_call(const F& f, const MDArgs& m, int64_t flat, A&... a) {
+  int64_t i[4];
+  int64_t r = flat;
+#pragma unroll
+  for (int d = 0; d < R; ++d) {
+    const int64_t e = m.ext[d];
+    i[d] = m.lo[d] + (d == R - 1 ? r : r % e);
+    r = (d == R - 1) ? 0 : r / e;
+  }
+  if constexpr (R == 2) f(i[0], i[1], a...);
+  else if constexpr (R == 3) f(i[0], i[1], i[2], a...);
+  else f(i[0], i[1], i[2], i[3], a...);
+}
+template <int R, class F>
+__global__ void __launch_bounds__(kBlock) k_md_for(F f, MDArgs m, int64_t n) {
+  int64_t c0, c1;
+  cta_share(n, &c0, &c1);
+  for (int64_t i = c0 + threadIdx.x; i < c1; i += kBlock) md_call<R>(f, m, i);
+}
+template <int R, class F, class Red, class V>
+__global__ void __launch_bounds__(kBlock)
+    k_md_reduce(F f, Red red, MDArgs m, int64_t n, V* partials, unsigned* counter, V* out) {
+  V v;
+  red.init(v);
+  int64_t c0, c1;
+  cta_share(n, &c0, &c1);
+  for (int64_t i = c0 + threadIdx.x; i < c1; i += kBlock) md_call<R>(f, m, i, v);
+  grid_finish_obj(red, v, partials, counter, out);
+}
+
+// ---- TeamPolicy: one CTA per team, league ranks strided over the grid ----------
+template <class F>
+__global__ void k_team_for(F f, int64_t league) {
+  for (int64_t lr = blockIdx.x; lr < league; lr += gridDim.x) {
+    TeamMember m(lr, league);
+    f(m);
+    __syncthreads();
+  }
+}
+template <class F, class Red, class V>
+__global__ void k_team_reduce(F f, Red red, int64_t league, V* partials, unsigned* counter, V* out) {
+  V v;
+  red.init(v);
+  for (int64_t lr = blockIdx.x; lr < league; lr += gridDim.x) {
+    TeamMember m(lr, league);
+    f(m, v);
+    __syncthreads();
+  }
+  grid_finish_obj(red, v, partials, counter, out);
+}
+
+// Run a reduce kernel and deliver the result.
+template <class Red, class Launch>
+void run_reduce(cudaStream_t s, int64_t grid, const Red& red, Launch launch) {
+  using V = typename Red::value_type;
+  Scratch sc = acquire(s, 256 + (size_t)grid * sizeof(V) + 256);
+  V* dev_out = red.res.device ? red.res.ptr : reinterpret_cast<V*>(sc.base);
+  V* partials = reinterpret_cast<V*>(sc.base + 256);
+  launched(launch(partials, sc.counters + kSlotReduce, dev_out), "parallel_reduce");
+  if (!red.res.device) {
+    check_cuda(cudaMemcpyAsync(red.res.ptr, dev_out, sizeof(V), cudaMemcpyDeviceToHost, s), "parallel_reduce");
+    check(gbk_stream_check((gbk_stream_t)s), "parallel_reduce");
+  }
+}
+
+inline int64_t grid_for(int64_t n) {
+  int64_t g = (n + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  if (g > cap) g = cap;
+  return g < 1 ? 1 : g;
+}
+
+template <class T>
+struct AsReducer {
+  using type = Sum<T>;
+  static Sum<T> make(T& r) { return Sum<T>(r); }
+};
+
+}  // namespace Impl
+
+// ---- parallel_for ------------------------------------------------------------
+template <class E, class... R, class F>
+void parallel_for(const RangePolicy<E, R...>& p, const F& f) {
+  const int64_t n = p.end() - p.begin();
+  if (n <= 0) return;
+  const int64_t g = Impl::grid_for(n);
+  Impl::k_range_for<<<(unsigned)g, Impl::kBlock, 0, p.space().stream()>>>(f, p.begin(), n);
+  Impl::launched(cudaGetLastError(), "parallel_for");
+}
+template <class F>
+void parallel_for(int64_t n, const F& f) {
+  parallel_for(RangePolicy<>(0, n), f);
+}
+template <class RankT, class E, class F>
+void parallel_for(const MDRangePolicy<RankT, E>& p, const F& f) {
+  constexpr int R = RankT::rank;
+  Impl::MDArgs m{};
+  int64_t n = 1;
+  for (int d = 0; d < R; ++d) {
+    m.lo[d] = p.lower(d);
+    m.ext[d] = p.upper(d) - p.lower(d);
+    n *= m.ext[d];
+  }
+  m.rank = R;
+  if (n <= 0) return;
+  Impl::k_md_for<R><<<(unsigned)Impl::grid_for(n), Impl::kBlock, 0, p.space().stream()>>>(f, m, n);
+  Impl::launched(cudaGetLastError(), "parallel_for(MDRange)");
+}
+template <class E, class... R, class F>
+void parallel_for(const TeamPolicy<E, R...>& p, const F& f) {
+  if (p.league_size() <= 0) return;
+  int64_t g = p.league_size();
+  const int64_t cap = (int64_t)Impl::num_sms() * (2048 / p.team_size());
+  if (g > cap) g = cap;
+  Impl::k_team_for<<<(unsigned)g, p.team_size(), 0, p.space().stream()>>>(f, p.league_size());
+  Impl::launched(cudaGetLastError(), "parallel_for(TeamPolicy)");
+}
+template <class P, class F>
+void parallel_for(const std::string&, const P& p, const F& f) {
+  parallel_for(p, f);
+}
+
+// ---- parallel_reduce -----------------------------------------------------------
+template <class E, class... R, class F, class Red,
+          std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
+void parallel_reduce(const RangePolicy<E, R...>& p, const F& f, const Red& red) {
+  using V = typename Red::value_type;
+  const int64_t n = p.end() - p.begin();
+  const int64_t g = Impl::grid_for(n);
+  cudaStream_t s = p.space().stream();
+  const int64_t b = p.begin();
+  Impl::run_reduce(s, g, red, [&](V* part, unsigned* ctr, V* out) {
+    Impl::k_range_reduce<<<(unsigned)g, Impl::kBlock, 0, s>>>(f, red, b, n, part, ctr, out);
+    return cudaGetLastError();
+  });
+}
+template <class RankT, class E, class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
+void parallel_reduce(const MDRangePolicy<RankT, E>& p, const F& f, const Red& red) {
+  using V = typename Red::value_type;
+  constexpr int R = RankT::rank;
+  Impl::MDArgs m{};
+  int64_t n = 1;
+  for (int d = 0; d < R; ++d) {
+    m.lo[d] = p.lower(d);
+    m.ext[d] = p.upper(d) - p.lower(d);
+    n *= m.ext[d];
+  }
+  m.rank = R;
+  const int64_t g = Impl::grid_for(n);
+  cudaStream_t s = p.space().stream();
+  Impl::run_reduce(s, g, red, [&](V* part, unsigned* ctr, V* out) {
+    Impl::k_md_reduce<R><<<(unsigned)g, Impl::kBlock, 0, s>>>(f, red, m, n, part, ctr, out);
+    return cudaGetLastError();
+  });
+}
+template <class E, class... R, class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
+void parallel_reduce(const TeamPolicy<E, R...>& p, const F& f, const Red& red) {
+  using V = typename Red::value_type;
+  int64_t g = p.league_size();
+  const int64_t cap = (int64_t)Impl::num_sms() * (2048 / p.team_size());
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  cudaStream_t s = p.space().stream();
+  const int64_t league = p.league_size();
+  const int ts = p.team_size();
+  Impl::run_reduce(s, g, red, [&](V* part, unsigned* ctr, V* out) {
+    Impl::k_team_reduce<<<(unsigned)g, ts, 0, s>>>(f, red, league, part, ctr, out);
+    return cudaGetLastError();
+  });
+}
+namespace Impl {
+template <class P> struct is_policy : std::false_type {};
+template <class E, class... R> struct is_policy<RangePolicy<E, R...>> : std::true_type {};
+template <class K, class E> struct is_policy<MDRangePolicy<K, E>> : std::true_type {};
+template <class E, class... R> struct is_policy<TeamPolicy<E, R...>> : std::true_type {};
+}  // namespace Impl
+
+// Scalar result: a Sum into a host variable.
+template <class P, class F, class T,
+          std::enable_if_t<std::is_arithmetic<T>::value && Impl::is_policy<P>::value, bool> = true>
+void parallel_reduce(const P& p, const F& f, T& result) {
+  parallel_reduce(p, f, Sum<T>(result));
+}
+template <class F, class T, std::enable_if_t<std::is_arithmetic<T>::value, bool> = true>
+void parallel_reduce(int64_t n, const F& f, T& result) {
+  parallel_reduce(RangePolicy<>(0, n), f, Sum<T>(result));
+}
+template <class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
+void parallel_reduce(int64_t n, const F& f, const Red& red) {
+  parallel_reduce(RangePolicy<>(0, n), f, red);
+}
+template <class P, class F, class T>
+void parallel_reduce(const std::string&, const P& p, const F& f, T&& result) {
+  parallel_reduce(p, f, std::forward<T>(result));
+}
+
+// ---- nested patterns inside a TeamPolicy functor ---------------------------------
+// (host-device because they are called from KOKKOS_LAMBDA bodies; they only
+// do work in device code)
+template <class F>
+KOKKOS_INLINE_FUNCTION void parallel_for(const TeamThreadRangeBoundaries<>& r, const F& f) {
+#ifdef __CUDA_ARCH__
+  for (int64_t i = r.begin + r.member.team_rank(); i < r.end; i += r.member.team_size()) f(i);
+#endif
+}
+
+namespace Impl {
+// Team-wide join of every thread's value; the result reaches all threads.
+template <class Red, class V>
+__device__ V team_allreduce(const Red& red, V v) {
+  __shared__ __align__(16) unsigned char raw[33 * sizeof(V)];
+  V* sm = reinterpret_cast<V*>(raw);
+  v = block_reduce_obj(red, v, sm);
+  if (threadIdx.x == 0) sm[32] = v;
+  __syncthreads();
+  v = sm[32];
+  __syncthreads();
+  return v;
+}
+template <class T>
+struct DevSum {
+  using value_type = T;
+  __device__ void init(T& v) const { v = T(0); }
+  __device__ void join(T& a, const T& b) const { a += b; }
+};
+}  // namespace Impl
+
+template <class F, class T, std::enable_if_t<std::is_arithmetic<T>::value, bool> = true>
+KOKKOS_INLINE_FUNCTION void parallel_reduce(const TeamThreadRangeBoundaries<>& r, const F& f, T& result) {
+#ifdef __CUDA_ARCH__
+  T v = T(0);
+  for (int64_t i = r.begin + r.member.team_rank(); i < r.end; i += r.member.team_size()) f(i, v);
+  result = Impl::team_allreduce(Impl::DevSum<T>{}, v);
+#endif
+}
+template <class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
+KOKKOS_INLINE_FUNCTION void parallel_reduce(const TeamThreadRangeBoundaries<>& r, const F& f, const Red& red) {
+#ifdef __CUDA_ARCH__
+  typename Red::value_type v;
+  red.init(v);
+  for (int64_t i = r.begin + r.member.team_rank(); i < r.end; i += r.member.team_size()) f(i, v);
+  red.reference() = Impl::team_allreduce(red, v);
+#endif
+}
+
+// ThreadVectorRange: vector length 1 in this mapping (a team thread runs the
+// range itself).
+struct ThreadVectorRangeBoundaries {
+  int64_t begin, end;
+};
+KOKKOS_INLINE_FUNCTION ThreadVectorRangeBoundaries ThreadVectorRange(const TeamMember&, int64_t n) { return {0, n}; }
+KOKKOS_INLINE_FUNCTION ThreadVectorRangeBoundaries ThreadVectorRange(const TeamMember&, int64_t b, int64_t e) {
+  return {b, e};
+}
+template <class F>
+KOKKOS_INLINE_FUNCTION void parallel_for(const ThreadVectorRangeBoundaries& r, const F& f) {
+  for (int64_t i = r.begin; i < r.end; ++i) f(i);
+}
+template <class F, class T>
+KOKKOS_INLINE_FUNCTION void parallel_reduce(const ThreadVectorRangeBoundaries& r, const F& f, T& result) {
+  T v = T(0);
+  for (int64_t i = r.begin; i < r.end; ++i) f(i, v);
+  result = v;
+}
+
+}  // namespace gb300k

@@ -90,6 +90,18 @@ int gbk_stream_check(gbk_stream_t stream);
 int gbk_workspace_reserve(gbk_stream_t stream, int64_t bytes);
 /* Free every workspace (after all work on them has finished). */
 int gbk_workspace_release_all(void);
+/* For kernels instantiated in the caller's translation unit (the header
+ * template path, include/Kokkos_GB300.hpp): the stream's workspace with at
+ * least scratch_bytes of scratch, its 64 ticket counters (slots 32..63 are
+ * free for the caller; each kernel resets the slot it takes) and its error
+ * word.  Stands in for the per-instance scratch of
+ * core/src/Cuda/Kokkos_Cuda_Instance.cpp:508-535 (scratch_space,
+ * scratch_flags). */
+int gbk_workspace_acquire(gbk_stream_t stream, int64_t scratch_bytes, void** scratch, unsigned** counters,
+                          int** error_word);
+/* Record `count` kernel launches made by caller-instantiated kernels in the
+ * library's launch counter. */
+int gbk_note_launches(int64_t count);
 /* Bound, in polls, of every device-side wait (lookback, barriers).  The
  * default bounds a wait at roughly a second. */
 int gbk_set_wait_limit(int64_t polls);

@@ -217,6 +217,27 @@ int gbk_workspace_release_all(void) {
   return GBK_OK;
 }
 
+int gbk_workspace_acquire(gbk_stream_t stream, int64_t scratch_bytes, void** scratch, unsigned** counters,
+                          int** error_word) {
+  if (scratch_bytes < 0) return GBK_ERR_INVALID_ARGUMENT;
+  int st = GBK_OK;
+  Workspace* w = ws_get((cudaStream_t)stream, &st);
+  if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->mu);
+  char* s = ws_scratch(w, (size_t)(scratch_bytes > 0 ? scratch_bytes : 1), &st);
+  if (!s) return st;
+  if (scratch) *scratch = s;
+  if (counters) *counters = w->counters;
+  if (error_word) *error_word = w->err;
+  return GBK_OK;
+}
+
+int gbk_note_launches(int64_t count) {
+  if (count < 0) return GBK_ERR_INVALID_ARGUMENT;
+  note_launch(count);
+  return GBK_OK;
+}
+
 int gbk_set_wait_limit(int64_t polls) {
   if (polls < 1) return GBK_ERR_INVALID_ARGUMENT;
   g_wait_limit = polls;

@@ -12,7 +12,7 @@
   log2 n, extra) to the chosen configuration; the entry points consult it
   when called without an explicit configuration.
 
-    python -m kokkos_gb300.tuner --train-workloads 900 --eval-workloads 2000 --out gpurun_out/tuner
+    python -m kokkos_gb300.tuner --train-workloads 1350 --eval-workloads 2000 --out <dir>
 """
 from __future__ import annotations
 
@@ -366,7 +366,7 @@ def table_from_model(model, path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--train-workloads", type=int, default=900)
+    ap.add_argument("--train-workloads", type=int, default=1350)  # about 20,000 timings
     ap.add_argument("--eval-workloads", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--out", default="gpurun_out/tuner")
