@@ -191,6 +191,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbk", choices=["gbk", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tuning-table", action="store_true",
+                    help="use the library defaults instead of the autotuner's table (kokkos_gb300/tuning_table.txt)")
     ap.add_argument("--only", default=None, choices=["minloc", "maxloc", "sum", "hist", "sum_f64", "exscan"],
                     help="run just this operation warmup+steps times (for profiler captures): the bench ops on the "
                          "bench inputs, or sum_f64 / exscan on 2^24 doubles / int32 (the RangePolicy Sum and "
@@ -211,6 +213,10 @@ def main():
     stream = torch.cuda.Stream(device=dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
     lib = gbk.lib
+    table = os.path.join(ROOT, "kokkos_gb300", "tuning_table.txt")
+    tuned = False
+    if not args.no_tuning_table and os.path.exists(table):
+        tuned = lib.gbk_tuner_load(table.encode()) == 0 and lib.gbk_tuner_enable(1) == 0
 
     if args.only in ("sum_f64", "exscan"):
         n = 1 << 24
@@ -363,7 +369,8 @@ def main():
         "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded xoshiro256**, seed 0; N(0,1) floats, Zipf(1.1) keys)",
         "config": {"workload": WORKLOAD, "step_bytes": STEP_BYTES, "l2": "inputs 268 MB each > 129 MB L2; no flush",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "launch_config": "autotuner table" if tuned else "library defaults"},
         "roofline": {"bound": "hbm", "kernel": "k_reduce_flat (MinLoc/MaxLoc/Sum f32)",
                      "achieved": round(red_gbs, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(red_gbs / hbm, 4), "peak_kind": peak_kind + " hbm_gbs (burst copy)",

@@ -126,6 +126,8 @@ int md_launch(int op, int dt, const void* base, int rank, const int64_t* lo, con
   if (kind < 0) return GBK_ERR_INVALID_ARGUMENT;
   if (kind == 1) {
     const char* p = (const char*)base + off * (int64_t)dtype_size(dt);
+    gbk_tuning_t tt;
+    if (!t) t = tuned_config(TUNE_REDUCE, op, dt, cnt, 0, &tt);
     return reduce_any(op, dt, p, cnt, off, out, w, t);
   }
   return md_any(op, dt, base, b, out, w, t);
