@@ -4,17 +4,34 @@
 // core/src/Cuda/Kokkos_Cuda_Parallel_Range.hpp:390-700 (and the
 // ParallelScanWithTotal variant :704-1053): one read of x, one write of y.
 //
-// Tiles of BLOCK * IPT 16-byte input vectors.  A CTA takes its tile index
-// from an atomic ticket, so every tile it waits on belongs to a CTA that is
-// already running: the look-back cannot deadlock whatever the occupancy.
-// Each warp owns a contiguous slice of the tile in warp-striped order
-// (vector k of lane l at slice + (32k + l) * VEC), so loads and stores are
-// coalesced without a shared-memory transpose; the scan inside the warp is a
-// shuffle scan per row k with a running carry.  Tile status words carry the
-// launch epoch in their upper 30 bits, so stale words from earlier launches
-// read as "not ready" and no memset is needed per launch.  Every wait polls
-// with a back-off and gives up after the library's wait limit, setting the
-// timeout bit of the stream's error word instead of hanging.
+// Persistent, warp-specialised CTAs on a cooperative (co-resident) grid of G
+// CTAs: CTA b owns tiles b, b + G, b + 2G, ... of 256 * IPT 16-byte input
+// vectors.  Every tile a look-back waits on belongs to a running CTA that
+// handles its tiles in order, so the waits cannot deadlock; and the static
+// order keeps aggregates appearing in tile order (tickets taken ahead of use
+// let a CTA hold tiles whose aggregates come microseconds late, and every
+// look-back behind them waits).  Per CTA:
+//   * eight compute warps run a software pipeline over the CTA's tiles: the
+//     tile-sum pass of tile i+AHEAD (its aggregate is published at once),
+//     then the output pass of tile i, whose exclusive prefix is ready by then;
+//   * NLB look-back warps resolve the prefixes, tile slots round-robin.
+// Input tiles arrive in a shared-memory ring by 1-D bulk copies
+// (TMA engine, mbarrier completion); output tiles are staged in shared
+// memory and leave as coalesced 16-byte streaming stores.  (A bulk store
+// would need a generic-to-async proxy fence per tile, and that fence waited
+// for the ring's copies in flight: microseconds per tile.)
+//
+// Tile status is one 16-byte descriptor of two 64-bit words that both carry
+// the tag (epoch << 2) | status beside half of the value: a reader that finds
+// one tag in both words holds the whole value, so neither side needs a
+// fence.  (128-bit single-copy-atomic loads would do the same in one access,
+// but those were served one at a time, about 850 cycles each under load.)
+// The epoch (30 bits, fresh per launch) makes stale descriptors from earlier
+// launches read as "not ready", so no clearing is needed per launch.  A
+// look-back window is 128 or 256 descriptors per L2 round trip.  Every wait is bounded
+// by the library's wait limit and sets the timeout bit of the stream's error
+// word instead of hanging.
+#include <algorithm>
 #include <type_traits>
 
 #include "gbk_internal.cuh"
@@ -24,21 +41,74 @@ namespace {
 
 constexpr unsigned FLAG_A = 1;  // tile aggregate available
 constexpr unsigned FLAG_P = 2;  // inclusive prefix available
+constexpr int SCAN_COMPUTE = 256;  // compute threads per CTA
+// Look-back warps: the CTA's tile slots go round-robin to them, so up to NLB
+// look-backs of one CTA are in flight at once (a look-back needs only its
+// predecessors' aggregates, not their prefixes).
+constexpr int NLB = 4;
+constexpr int SCAN_BLOCK = SCAN_COMPUTE + 32 * NLB;
+// Named barriers: tile info handed to look-back warp k (id BAR_INFO + k),
+// prefix handed back (BAR_PREFIX + k), compute warps only.
+constexpr int BAR_INFO = 1, BAR_PREFIX = 1 + NLB, BAR_COMPUTE = 1 + 2 * NLB;
+constexpr int BAR_HANDOFF = SCAN_COMPUTE + 32;  // threads in one hand-off
+static_assert(BAR_COMPUTE <= 15, "named barrier ids");
 
-template <class TO>
+// Descriptors per lane in a look-back window: 256 predecessors per round trip
+// for 4-byte sums, 128 for 8-byte sums (register budget; their tiles carry
+// more bytes, so fewer of them are in flight at the same bandwidth).
+template <class TO> constexpr int lookback_k() { return sizeof(TO) == 8 ? 4 : 8; }
+
+// Two 64-bit words, each {tag (32 bits) : half of the value (32 bits)}, with
+// tag = (epoch << 2) | status.  Each word is a single-copy-atomic access, and
+// every (epoch, status) of a tile is published once, so a reader that finds
+// the same tag in both words holds both halves of that publication; a torn
+// read (one word from the aggregate, one from the prefix) shows two tags and
+// counts as not ready.
+struct alignas(16) TileDesc {
+  unsigned long long w0, w1;
+};
+
 struct ScanState {
-  unsigned* flags;
-  TO* agg;
-  TO* incl;
-  unsigned* ticket;
+  TileDesc* desc;
   int* err;
   unsigned epoch;  // 30 bits
   int64_t ntiles;
   int64_t wait_limit;
 };
 
+// Descriptor of tile t, one per 128-byte line: hundreds of look-backs poll
+// the few KB of descriptors behind the frontier, and packed 16 bytes apart
+// they sat on a handful of L2 slices (round trips of several microseconds).
+constexpr int DESC_STRIDE = 8;
+__device__ __forceinline__ TileDesc* desc_at(const ScanState& S, int64_t t) { return S.desc + t * DESC_STRIDE; }
+
+__device__ __forceinline__ void desc_store(TileDesc* p, unsigned tag, unsigned long long bits) {
+  const unsigned long long w0 = ((unsigned long long)tag << 32) | (bits & 0xFFFFFFFFull);
+  const unsigned long long w1 = ((unsigned long long)tag << 32) | (bits >> 32);
+  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(w0), "l"(w1) : "memory");
+}
+// tag = 0 (never a valid tag: epochs start at 1) when the two words disagree.
+__device__ __forceinline__ void desc_load(const TileDesc* p, unsigned* tag, unsigned long long* bits) {
+  unsigned long long w0, w1;
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(p) : "memory");
+  const unsigned t0 = (unsigned)(w0 >> 32), t1 = (unsigned)(w1 >> 32);
+  *tag = t0 == t1 ? t0 : 0u;
+  *bits = (w0 & 0xFFFFFFFFull) | (w1 << 32);
+}
+template <class TO>
+__device__ __forceinline__ unsigned long long to_bits(TO v) {
+  unsigned long long b = 0;
+  memcpy(&b, &v, sizeof(TO));
+  return b;
+}
+template <class TO>
+__device__ __forceinline__ TO from_bits(unsigned long long b) {
+  TO v;
+  memcpy(&v, &b, sizeof(TO));
+  return v;
+}
+
 template <class T> __device__ __forceinline__ T shup(T v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
-template <class T> __device__ __forceinline__ T shidx(T v, int l) { return __shfl_sync(0xffffffffu, v, l); }
 
 // Inclusive warp scan (Kogge-Stone).
 template <class T>
@@ -59,189 +129,378 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-template <class TO>
-__device__ __forceinline__ TO ld_relaxed_val(const TO* p) {
-  if constexpr (sizeof(TO) == 8) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    TO r;
-    memcpy(&r, &v, 8);
-    return r;
-  } else {
-    unsigned v;
-    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    TO r;
-    memcpy(&r, &v, 4);
-    return r;
+// Look-back for `tile` (> 0, aggregate already published) by one full warp:
+// sums predecessors' aggregates back to the nearest inclusive prefix and
+// publishes the tile's inclusive prefix; returns the exclusive prefix (in
+// every lane).  A window is 32 * K descriptors, lane l holding distances
+// l*K .. l*K+K-1 from the window start, all loaded at once.  `bad` is set
+// when a wait gave up; the missing prefix then counts as zero.
+template <class TO, int K>
+__device__ __forceinline__ TO look_back(const ScanState& S, int64_t tile, TO tile_agg, bool* bad) {
+  static_assert(K >= 1 && K <= 16, "descriptors per lane");
+  const int lane = threadIdx.x & 31;
+  const unsigned ep = S.epoch << 2;
+  constexpr unsigned ALL = (1u << K) - 1u;
+  TO excl = TO(0);
+  int64_t base = tile - 1;
+  while (true) {
+    unsigned long long val[K];
+    unsigned okm = 0, pm = 0;  // per entry: status valid / inclusive prefix
+    const int64_t p0 = base - (int64_t)lane * K;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      val[j] = 0;
+      if (p0 - j < 0) {  // before tile 0: a zero prefix
+        okm |= 1u << j;
+        pm |= 1u << j;
+      } else {
+        unsigned tg;
+        desc_load(desc_at(S, p0 - j), &tg, &val[j]);
+        if ((tg & ~3u) == ep && (tg & 3u)) okm |= 1u << j;
+        if (tg == (ep | FLAG_P)) pm |= 1u << j;
+      }
+    }
+    int64_t polls = 0;
+    unsigned ns = 0, need, lanes_p;
+    while (true) {
+      // Entries that count: everything before the nearest prefix and that
+      // prefix itself (lowest lane holding one, then its lowest entry).
+      lanes_p = __ballot_sync(0xffffffffu, pm != 0);
+      const int lp = lanes_p ? __ffs(lanes_p) - 1 : 32;
+      need = lane < lp ? ALL : (lane == lp ? (pm ^ (pm - 1u)) & ALL : 0u);
+      const unsigned miss = need & ~okm;
+      if (!__ballot_sync(0xffffffffu, miss != 0)) break;
+      if (++polls > S.wait_limit) {
+        // Give up; still publish, so that successors do not wait as well.
+        *bad = true;
+        if (lane == 0) desc_store(desc_at(S, tile), ep | FLAG_P, to_bits(tile_agg));
+        return TO(0);
+      }
+      if (polls > 2) {
+        ns = ns ? (ns < 256 ? ns * 2 : 256) : 32;
+        __nanosleep(ns);
+      }
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        if ((miss >> j) & 1u) {
+          unsigned tg;
+          desc_load(desc_at(S, p0 - j), &tg, &val[j]);
+          if ((tg & ~3u) == ep && (tg & 3u)) okm |= 1u << j;
+          if (tg == (ep | FLAG_P)) pm |= 1u << j;
+        }
+      }
+    }
+    TO v = TO(0);
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if ((need >> j) & 1u) v = v + from_bits<TO>(val[j]);
+    excl = excl + warp_sum(v);
+    if (lanes_p) break;
+    base -= 32 * K;
   }
+  if (lane == 0) desc_store(desc_at(S, tile), ep | FLAG_P, to_bits(TO(excl + tile_agg)));
+  return excl;
 }
 
-template <class TI, class TO, bool INCL, bool ALIGNED, int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK)
-    k_scan(const TI* __restrict__ x, TO* __restrict__ y, int64_t n, TO init, ScanState<TO> S, TO* total) {
+// FAST: x and y are 16-byte aligned; tiles move by bulk copies through
+// shared memory.  Otherwise every element is loaded and stored directly with
+// the same thread-to-element mapping (the path for unaligned views).
+//
+// Thread-sequential chunks: compute thread i owns input vectors
+// i*IPT .. i*IPT+IPT-1 of a tile.  IPT is odd, so the 8 lanes of a
+// quarter-warp touch 8 different bank groups at every step and shared-memory
+// accesses need no swizzle.  A thread scans its IPT * VEC elements serially:
+// one warp scan per thread and about two additions per element (the FP64
+// pipe, not HBM, bounds the f64 scans).
+//
+// Pipeline: the tile-sum pass runs AHEAD tiles ahead of the output pass, so
+// a look-back has AHEAD iterations to finish; STAGES >= AHEAD + 1 input
+// stages (one more lets the next copy land a full iteration early).  The
+// out tile goes out in ROUNDS rounds (1, or 2 for widening scans: half the
+// threads each, and an out tile of one input tile's bytes).
+template <class TI, class TO, bool INCL, bool FAST, int IPT, int STAGES, int AHEAD, int ROUNDS>
+__global__ void __launch_bounds__(SCAN_BLOCK, 2)
+    k_scan(const TI* __restrict__ x, TO* __restrict__ y, int64_t n, TO init, ScanState S, TO* total) {
   constexpr int VEC = 16 / sizeof(TI);
-  constexpr int WARPS = BLOCK / 32;
-  constexpr int64_t TILE = (int64_t)BLOCK * IPT * VEC;
-  constexpr int64_t WSLICE = 32LL * IPT * VEC;
-  __shared__ int64_t s_tile;
-  __shared__ TO s_warp[WARPS];
+  constexpr int WARPS = SCAN_COMPUTE / 32;
+  constexpr int OVN = (int)(VEC * sizeof(TO) / 16);  // output vectors per input vector: 1 or 2
+  constexpr int OV = 16 / sizeof(TO);                 // elements per output vector
+  constexpr int64_t TILE = (int64_t)SCAN_COMPUTE * IPT * VEC;
+  constexpr unsigned IN_BYTES = (unsigned)SCAN_COMPUTE * IPT * 16;
+  constexpr int RT = SCAN_COMPUTE / ROUNDS;  // threads per output round
+  constexpr int64_t RTILE = TILE / ROUNDS;    // elements per output round
+  static_assert(IPT % 2 == 1, "an odd vector count per thread keeps shared-memory accesses conflict-free");
+  static_assert(OVN == 1 || OVN == 2, "output at most twice the input width");
+  static_assert(AHEAD >= 1 && STAGES >= AHEAD + 1 && AHEAD < NLB, "pipeline depth");
+  static_assert(ROUNDS == 1 || ROUNDS == OVN, "output rounds");
+  // FAST: STAGES input stages, then the out tile (IN_BYTES * OVN / ROUNDS)
+  extern __shared__ __align__(128) unsigned char dsm[];
+  __shared__ __align__(8) unsigned long long s_bar[STAGES];
+  __shared__ int64_t s_info_tile[NLB];  // tile handed to look-back warp k
+  __shared__ TO s_info_agg[NLB];
+  __shared__ TO s_excl[NLB];            // its exclusive prefix, handed back
+  __shared__ TO s_warp[2][WARPS];
+  __shared__ int s_bad;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t nin = FAST ? n / VEC * VEC : 0;  // elements the bulk loads cover
+  const int64_t nout = FAST ? n / OV * OV : 0;   // elements the bulk stores cover
+  unsigned char* outt = dsm + (size_t)STAGES * IN_BYTES;
+  // The CTA's j-th tile.
+  auto tile_of = [&](int j) { return (int64_t)blockIdx.x + (int64_t)j * gridDim.x; };
+
+  // Thread 0 only: start the copy of the CTA's j-th tile into its stage.
+  auto fill = [&](int j) {
+    const int64_t t = tile_of(j);
+    if (FAST && t < S.ntiles) {
+      const int s = j % STAGES;
+      const int64_t e0 = t * TILE;
+      const int64_t cnt = nin - e0 < TILE ? nin - e0 : TILE;
+      const unsigned bytes = (unsigned)(cnt * (int64_t)sizeof(TI));
+      mbar_arrive_expect_tx(&s_bar[s], bytes);
+      if (bytes) bulk_g2s(dsm + (size_t)s * IN_BYTES, x + e0, bytes, &s_bar[s]);
+    }
+  };
 
   if (threadIdx.x == 0) {
-    const unsigned t = atomicAdd(S.ticket, 1u);
-    if ((int64_t)t == S.ntiles - 1) *S.ticket = 0u;  // every tile has been claimed
-    s_tile = (int64_t)t;
+    s_bad = 0;
+#pragma unroll
+    for (int s = 0; s < STAGES; ++s) mbar_init(&s_bar[s], 1);
+    fence_mbar_init();
+#pragma unroll
+    for (int j = 0; j < STAGES; ++j) fill(j);
   }
   __syncthreads();
-  const int64_t tile = s_tile;
-  const int64_t tbase = tile * TILE;
-  const int64_t wbase = tbase + warp * WSLICE;
-  const bool full = tbase + TILE <= n;
+  bool bad = false;
 
-  // ---- load (warp-striped) and thread-local inclusive scans --------------
-  // Inputs stay in the input type (fewer registers for widening scans); the
-  // in-chunk prefix is recomputed when the outputs are formed.
-  TI v[IPT][VEC];
-#pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    const int64_t e0 = wbase + ((int64_t)k * 32 + lane) * VEC;
-    if (ALIGNED && full) {
-      Vec16<TI> u;
-      u.u = ld_stream16(x + e0);
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) v[k][j] = u.v[j];
-    } else {
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) v[k][j] = (e0 + j < n) ? x[e0 + j] : TI(0);
-    }
-  }
-  // ---- warp scan over chunks in (k, lane) order ---------------------------
-  TO chunk_ex[IPT];
-  TO carry = TO(0);
-#pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    TO c = (TO)v[k][0];
-#pragma unroll
-    for (int j = 1; j < VEC; ++j) c = c + (TO)v[k][j];
-    const TO inc = warp_iscan(c);
-    TO ex = shup(inc, 1);
-    if (lane == 0) ex = TO(0);
-    chunk_ex[k] = carry + ex;
-    carry = carry + shidx(inc, 31);
-  }
-  if (lane == 0) s_warp[warp] = carry;
-  __syncthreads();
-  TO warp_pre = TO(0), tile_agg = TO(0);
-  {
-    // Every thread walks the (few) warp totals: deterministic, no extra sync.
-#pragma unroll
-    for (int w = 0; w < WARPS; ++w) {
-      if (w == warp) warp_pre = tile_agg;
-      tile_agg = tile_agg + s_warp[w];
-    }
-  }
-  // ---- decoupled look-back, the whole CTA as one BLOCK-tile window ----------
-  // Thread i examines predecessor tile (window start - i).  The window sums
-  // aggregates back to the nearest tile with an inclusive prefix; windows
-  // step back by BLOCK tiles until one holds such a tile.  A whole-CTA
-  // window keeps the walk short when hundreds of tiles are in flight.
-  const unsigned ep = S.epoch << 2;
-  __shared__ int s_near;
-  __shared__ int s_timeout;
-  __shared__ TO s_wsum[WARPS];
-  TO excl = TO(0);
-  if (tile == 0) {
-    if (threadIdx.x == 0) {
-      S.incl[0] = tile_agg;
-      st_release_u32(S.flags, ep | FLAG_P);
+  if (warp >= WARPS) {
+    // ---- look-back warp k: the CTA's tile slots k, k + NLB, k + 2 NLB, ... --
+    const int k = warp - WARPS;
+    while (true) {
+      bar_sync(BAR_INFO + k, BAR_HANDOFF);
+      const int64_t tile = s_info_tile[k];
+      if (tile >= S.ntiles) break;
+      const TO agg = s_info_agg[k];
+      const TO excl = tile == 0 ? TO(0) : look_back<TO, lookback_k<TO>()>(S, tile, agg, &bad);
+      if (lane == 0) {
+        s_excl[k] = excl;
+        if (total && tile == S.ntiles - 1) *total = INCL ? excl + agg : init + (excl + agg);
+      }
+      bar_arrive(BAR_PREFIX + k, BAR_HANDOFF);
     }
   } else {
-    if (threadIdx.x == 0) {
-      S.agg[tile] = tile_agg;
-      st_release_u32(S.flags + tile, ep | FLAG_A);
-      s_timeout = 0;
+    // ---- compute warps ------------------------------------------------------
+    // Vector jj of this thread in the tile held by stage s.
+    auto load_vec = [&](int s, int64_t tbase, int jj, TI (&v)[VEC]) {
+      const int64_t e0 = tbase + ((int64_t)threadIdx.x * IPT + jj) * VEC;
+      const unsigned char* stg = dsm + (size_t)s * IN_BYTES;
+      if (FAST && tbase + TILE <= nin) {
+        Vec16<TI> u;
+        u.u = reinterpret_cast<const uint4*>(stg)[threadIdx.x * IPT + jj];
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) v[q] = u.v[q];
+      } else if (FAST) {
+        const TI* sv = reinterpret_cast<const TI*>(stg) + ((size_t)threadIdx.x * IPT + jj) * VEC;
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) v[q] = e0 + q < nin ? sv[q] : (e0 + q < n ? x[e0 + q] : TI(0));
+      } else {
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) v[q] = e0 + q < n ? x[e0 + q] : TI(0);
+      }
+    };
+    // Tile-sum pass of the CTA's j-th tile (stage j % STAGES): this thread's
+    // exclusive prefix within its warp (tex) and its warp's within the tile
+    // (wpre); thread 0 publishes the aggregate and fills the hand-off slot.
+    auto tile_sums = [&](int j, int64_t tile, TO& tex, TO& wpre) {
+      const int s = j % STAGES;
+      if (FAST && !mbar_wait(&s_bar[s], (unsigned)(j / STAGES) & 1u, S.wait_limit)) bad = true;
+      TO tsum = TO(0);
+#pragma unroll
+      for (int jj = 0; jj < IPT; ++jj) {
+        TI v[VEC];
+        load_vec(s, tile * TILE, jj, v);
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) tsum = tsum + (TO)v[q];
+      }
+      const TO tinc = warp_iscan(tsum);
+      tex = shup(tinc, 1);
+      if (lane == 0) tex = TO(0);
+      if (lane == 31) s_warp[j & 1][warp] = tinc;
+      bar_sync(BAR_COMPUTE, SCAN_COMPUTE);
+      TO agg = TO(0);
+      wpre = TO(0);
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) {
+        if (w == warp) wpre = agg;
+        agg = agg + s_warp[j & 1][w];
+      }
+      if (threadIdx.x == 0) {
+        desc_store(desc_at(S, tile), (S.epoch << 2) | (tile == 0 ? FLAG_P : FLAG_A), to_bits(agg));
+        s_info_tile[j % NLB] = tile;
+        s_info_agg[j % NLB] = agg;
+      }
+    };
+
+    // Per-thread prefixes of the tiles summed but not yet written: entry a
+    // belongs to the CTA's tile i + a.
+    TO q_tex[AHEAD + 1], q_wpre[AHEAD + 1];
+#pragma unroll
+    for (int a = 0; a <= AHEAD; ++a) q_tex[a] = q_wpre[a] = TO(0);
+    // Hand-offs go to the look-back warps for valid tiles only, in slot
+    // order; after the last one every look-back warp gets one end mark.
+    auto hand_off = [&](int j) { bar_arrive(BAR_INFO + j % NLB, BAR_HANDOFF); };
+#pragma unroll
+    for (int a = 0; a < AHEAD; ++a) {
+      if (tile_of(a) < S.ntiles) {
+        tile_sums(a, tile_of(a), q_tex[a], q_wpre[a]);
+        hand_off(a);
+      }
     }
-    int64_t pt0 = tile - 1;
-    while (true) {
-      const int64_t pt = pt0 - threadIdx.x;
-      unsigned f = ep | FLAG_P;
-      TO val = TO(0);
-      if (threadIdx.x == 0) s_near = BLOCK;
-      __syncthreads();
-      if (pt >= 0) {
-        int64_t polls = 0;
-        unsigned ns = 0;
-        while (true) {
-          f = ld_relaxed_u32(S.flags + pt);
-          if ((f & ~3u) == ep && (f & 3u)) break;
-          if (++polls > S.wait_limit || *(volatile int*)&s_timeout) {
-            f = ep | FLAG_P;  // give up: treat as a zero prefix
-            atomicExch(&s_timeout, 1);
-            break;
-          }
-          if (polls > 8) {
-            ns = ns ? (ns < 256 ? ns * 2 : 256) : 32;
-            __nanosleep(ns);
+    int i = 0;
+    for (; tile_of(i) < S.ntiles; ++i) {
+      // Tile sums AHEAD tiles ahead first: that aggregate goes out while this
+      // tile's prefix is being resolved.
+      if (tile_of(i + AHEAD) < S.ntiles) {
+        tile_sums(i + AHEAD, tile_of(i + AHEAD), q_tex[AHEAD], q_wpre[AHEAD]);
+        hand_off(i + AHEAD);
+      }
+      bar_sync(BAR_PREFIX + i % NLB, BAR_HANDOFF);
+      const TO tile_pre = s_excl[i % NLB];
+
+      // ---- output pass of the CTA's i-th tile (stage i % STAGES) -----------
+      const int s = i % STAGES;
+      const int64_t tbase = tile_of(i) * TILE;
+      const bool out_full = FAST && tbase + TILE <= nout;
+#pragma unroll
+      for (int r = 0; r < ROUNDS; ++r) {
+        if (FAST ? threadIdx.x / RT == r : r == 0) {
+          const int lt = FAST ? threadIdx.x - r * RT : 0;  // index within the round
+          const int64_t e_thr = tbase + (int64_t)threadIdx.x * IPT * VEC;
+          TO run = (INCL ? tile_pre + q_wpre[0] : init + (tile_pre + q_wpre[0])) + q_tex[0];
+#pragma unroll
+          for (int jj = 0; jj < IPT; ++jj) {
+            TI v[VEC];
+            load_vec(s, tbase, jj, v);
+            TO o[VEC];
+#pragma unroll
+            for (int q = 0; q < VEC; ++q) {
+              if (INCL) {
+                run = run + (TO)v[q];
+                o[q] = run;
+              } else {
+                o[q] = run;
+                run = run + (TO)v[q];
+              }
+            }
+            if (FAST) {
+              uint4* ov = reinterpret_cast<uint4*>(outt) + ((size_t)lt * IPT + jj) * OVN;
+              if constexpr (OVN == 1) {
+                Vec16<TO> u;
+#pragma unroll
+                for (int q = 0; q < VEC; ++q) u.v[q] = o[q];
+                ov[0] = u.u;
+              } else {
+                // Lanes 4..7 of each quarter-warp write their second vector
+                // first: with the odd stride each step hits 8 bank groups.
+                Vec16<TO> a, b;
+#pragma unroll
+                for (int q = 0; q < OV; ++q) {
+                  a.v[q] = o[q];
+                  b.v[q] = o[OV + q];
+                }
+                const int flip = (lane >> 2) & 1;
+                ov[flip] = flip ? b.u : a.u;
+                ov[flip ^ 1] = flip ? a.u : b.u;
+              }
+              if (!out_full) {
+                // Past the last 16-byte boundary of y: direct stores.
+#pragma unroll
+                for (int q = 0; q < VEC; ++q) {
+                  const int64_t e = e_thr + jj * VEC + q;
+                  if (e >= nout && e < n) y[e] = o[q];
+                }
+              }
+            } else {
+#pragma unroll
+              for (int q = 0; q < VEC; ++q) {
+                const int64_t e = e_thr + jj * VEC + q;
+                if (e < n) y[e] = o[q];
+              }
+            }
           }
         }
-        __threadfence();  // acquire: the value below is at least as new as the flag
-        if (!*(volatile int*)&s_timeout) val = ((f & 3u) == FLAG_P) ? ld_relaxed_val(S.incl + pt) : ld_relaxed_val(S.agg + pt);
-      }
-      if ((f & 3u) == FLAG_P) atomicMin(&s_near, (int)threadIdx.x);
-      __syncthreads();
-      const int near = s_near;
-      // Fixed-order sum of the window entries up to the nearest prefix.
-      TO c = ((int)threadIdx.x <= near) ? val : TO(0);
-      c = warp_sum(c);
-      if (lane == 0) s_wsum[warp] = c;
-      __syncthreads();
+        // This round's part of the out tile is written (and, after the last
+        // round, stage s has been read by every compute thread): stream it to
+        // y in warp-striped order, 512 contiguous bytes per warp instruction,
+        // and refill the stage (the barrier orders those reads before the
+        // copy's writes).
+        bar_sync(BAR_COMPUTE, SCAN_COMPUTE);
+        if (r == ROUNDS - 1 && threadIdx.x == 0) fill(i + STAGES);
+        if (FAST) {
+          const int64_t rbase = tbase + (int64_t)r * RTILE;
+          const uint4* ov = reinterpret_cast<const uint4*>(outt);
+          uint4* yv = reinterpret_cast<uint4*>(y + rbase);
+          const int64_t left = nout - rbase < RTILE ? nout - rbase : RTILE;
+          const int64_t nvec = left > 0 ? left * (int64_t)sizeof(TO) / 16 : 0;
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) excl = excl + s_wsum[w];
-      if (near < BLOCK) break;
-      pt0 -= BLOCK;
-      __syncthreads();  // s_wsum / s_near are rewritten by the next window
+          for (int k = 0; k < IPT * OVN / ROUNDS; ++k) {
+            const int q = k * SCAN_COMPUTE + threadIdx.x;
+            if (out_full || q < nvec) __stcs(yv + q, ov[q]);
+          }
+          // The next round rewrites the out tile.  (The next tile's first
+          // writes come after its prefix barrier.)
+          if (r + 1 < ROUNDS) bar_sync(BAR_COMPUTE, SCAN_COMPUTE);
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < AHEAD; ++a) {
+        q_tex[a] = q_tex[a + 1];
+        q_wpre[a] = q_wpre[a + 1];
+      }
     }
-    if (threadIdx.x == 0) {
-      if (s_timeout) atomicOr(S.err, GBK_EBIT_TIMEOUT);
-      S.incl[tile] = excl + tile_agg;
-      st_release_u32(S.flags + tile, ep | FLAG_P);
+    // i = the number of tiles this CTA handed off: one end mark per look-back
+    // warp, in slot order.
+    for (int j = i; j < i + NLB; ++j) {
+      if (threadIdx.x == 0) s_info_tile[j % NLB] = S.ntiles;
+      hand_off(j);
     }
   }
-  const TO tile_pre = excl;
-  if (total && tile == S.ntiles - 1 && threadIdx.x == 0) *total = INCL ? tile_pre + tile_agg : init + (tile_pre + tile_agg);
 
-  // ---- write ---------------------------------------------------------------
-  const TO base = INCL ? tile_pre + warp_pre : init + (tile_pre + warp_pre);
-#pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    const int64_t e0 = wbase + ((int64_t)k * 32 + lane) * VEC;
-    TO run = base + chunk_ex[k];
-    TO o[VEC];
-#pragma unroll
-    for (int j = 0; j < VEC; ++j) {
-      if (INCL) {
-        run = run + (TO)v[k][j];
-        o[j] = run;
-      } else {
-        o[j] = run;
-        run = run + (TO)v[k][j];
-      }
-    }
-    if (ALIGNED && full) {
-      constexpr int OV = 16 / sizeof(TO);
-#pragma unroll
-      for (int j = 0; j < VEC; j += OV) {
-        Vec16<TO> u;
-#pragma unroll
-        for (int q = 0; q < OV; ++q) u.v[q] = o[j + q];
-        __stcs(reinterpret_cast<uint4*>(y + e0 + j), u.u);
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < VEC; ++j)
-        if (e0 + j < n) y[e0 + j] = o[j];
-    }
+  if (bad) s_bad = 1;
+  __syncthreads();
+  if (threadIdx.x == 0 && s_bad) atomicOr(S.err, GBK_EBIT_TIMEOUT);
+}
+
+// Launch one instantiation as a cooperative grid (all CTAs co-resident, which
+// the static tile order needs): min(tiles, resident CTAs), or ctas_per_sm x
+// SMs when the tuning asks for fewer.
+template <class TI, class TO, bool INCL, bool FAST, int IPT, int STAGES, int AHEAD, int ROUNDS>
+int launch_k_scan(const TI* x, TO* y, int64_t n, TO init, const ScanState& S, TO* total, int cps, cudaStream_t s) {
+  auto kfn = k_scan<TI, TO, INCL, FAST, IPT, STAGES, AHEAD, ROUNDS>;
+  constexpr size_t in_bytes = (size_t)SCAN_COMPUTE * IPT * 16;
+  // stages + out tile
+  const size_t dyn = FAST ? STAGES * in_bytes + in_bytes * (sizeof(TO) / sizeof(TI)) / ROUNDS : 0;
+  static int resident = 0;  // CTAs per SM, per instantiation
+  if (!resident) {
+    // Static + dynamic shared memory above 48 KiB needs the opt-in.
+    if (dyn) GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    int r = 0;
+    GBK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kfn, SCAN_BLOCK, dyn));
+    if (r < 1) return GBK_ERR_UNSUPPORTED;
+    resident = r;
   }
+  const int per_sm = cps > 0 && cps < resident ? cps : resident;
+  const int64_t grid = std::min<int64_t>(S.ntiles, (int64_t)per_sm * sm_count());
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(SCAN_BLOCK);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(cudaLaunchKernelEx(&cfg, kfn, x, y, n, init, S, total));
 }
 
 template <class TI, class TO, bool INCL>
@@ -256,36 +515,42 @@ int launch_scan_t(const TI* x, TO* y, int64_t n, TO init, TO* total, Workspace* 
     return GBK_OK;
   }
   constexpr int VEC = 16 / sizeof(TI);
-  const int ipt = t && t->items_per_thread ? t->items_per_thread : 4;
-  const int64_t tile = (int64_t)256 * ipt * VEC;
+  constexpr bool WIDE = sizeof(TO) > sizeof(TI);
+  // Shapes (vectors per thread, stages, tiles ahead, output rounds), all two
+  // CTAs per SM; bigger tiles mean fewer look-backs.  Measured on 2^24 and
+  // 2^28 elements, the default is the fastest of the shapes tried:
+  //   default  9, 2, 1, 1 (widening: 7, 2, 1, 1, its out tile is two input tiles)
+  //   <= 8     7, 3, 1, 1 (widening: 5, 3, 2, 1)
+  //   <= 4     3, 4, 2, 1 or 2 (small tiles)
+  const bool fast = (uintptr_t)x % 16 == 0 && (uintptr_t)y % 16 == 0;
+  constexpr int BIG = WIDE ? 7 : 9;
+  const int want = t && t->items_per_thread > 0 ? t->items_per_thread : 9;
+  const int ipt = !fast ? BIG : want <= 4 ? 3 : want <= 8 ? (WIDE ? 5 : 7) : BIG;
+  const int shape = !fast ? 0 : want <= 4 ? 2 : want <= 8 ? 1 : 0;
+  const int cps = t ? t->ctas_per_sm : 0;
+  const int64_t tile = (int64_t)SCAN_COMPUTE * ipt * VEC;
   const int64_t ntiles = (n + tile - 1) / tile;
-  if (ntiles >= (int64_t)0xFFFFFFFFu) return GBK_ERR_INVALID_ARGUMENT;
+  if (ntiles >= (int64_t)0xFFFFFFFFu - (1 << 24)) return GBK_ERR_INVALID_ARGUMENT;
   int st = GBK_OK;
-  const size_t vbytes = ((size_t)ntiles * sizeof(TO) + 255) / 256 * 256;
-  char* scr = ws_scratch(w, 2 * vbytes, &st);
-  if (!scr) return st;
-  ScanState<TO> S;
-  S.flags = ws_flags(w, (size_t)ntiles, &S.epoch, &st);
-  if (!S.flags) return st;
-  S.agg = (TO*)scr;
-  S.incl = (TO*)(scr + vbytes);
-  S.ticket = w->counters + SLOT_SCAN_TILE;
+  ScanState S;
+  S.desc = (TileDesc*)ws_flags(w, (size_t)ntiles * DESC_STRIDE * (sizeof(TileDesc) / sizeof(unsigned)), &S.epoch, &st);
+  if (!S.desc) return st;
   S.err = w->err;
   S.ntiles = ntiles;
   S.wait_limit = wait_limit();
-  const bool aligned = ((uintptr_t)x % 16 == 0) && ((uintptr_t)y % 16 == 0);
-  const unsigned grid = (unsigned)ntiles;
-#define GBK_SCAN_LAUNCH(AL, IPT) k_scan<TI, TO, INCL, AL, 256, IPT><<<grid, 256, 0, s>>>(x, y, n, init, S, total)
-  if (ipt == 2) {
-    if (aligned) GBK_SCAN_LAUNCH(true, 2); else GBK_SCAN_LAUNCH(false, 2);
-  } else if (ipt == 8) {
-    if (aligned) GBK_SCAN_LAUNCH(true, 8); else GBK_SCAN_LAUNCH(false, 8);
-  } else {
-    if (aligned) GBK_SCAN_LAUNCH(true, 4); else GBK_SCAN_LAUNCH(false, 4);
-  }
-#undef GBK_SCAN_LAUNCH
+  constexpr int OVN = sizeof(TO) / sizeof(TI);
+  if (!fast)
+    st = launch_k_scan<TI, TO, INCL, false, BIG, 2, 1, 1>(x, y, n, init, S, total, cps, s);
+  else if (shape == 2)
+    st = launch_k_scan<TI, TO, INCL, true, 3, 4, 2, OVN>(x, y, n, init, S, total, cps, s);
+  else if (shape == 1)
+    st = WIDE ? launch_k_scan<TI, TO, INCL, true, 5, 3, 2, 1>(x, y, n, init, S, total, cps, s)
+              : launch_k_scan<TI, TO, INCL, true, 7, 3, 1, 1>(x, y, n, init, S, total, cps, s);
+  else
+    st = launch_k_scan<TI, TO, INCL, true, BIG, 2, 1, 1>(x, y, n, init, S, total, cps, s);
+  if (st) return st;
   note_launch();
-  return cuda_status(cudaGetLastError());
+  return GBK_OK;
 }
 
 template <class TI, class TO>

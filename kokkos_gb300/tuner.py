@@ -28,7 +28,7 @@ import numpy as np
 KIND_REDUCE, KIND_SCAN, KIND_HIST, KIND_SEG = 0, 1, 2, 3
 REDUCE_CFGS = [(b, u, c) for (b, u) in [(256, 2), (256, 4), (256, 8), (512, 2), (512, 4), (128, 8), (1024, 2)]
                for c in (1, 2, 4, 8)]
-SCAN_CFGS = [2, 4, 8]
+SCAN_CFGS = [(9, 0), (7, 0), (3, 0), (9, 1)]  # (vectors per thread, CTAs per SM; 0 = all resident)
 SEG_CFGS = [2, 4, 8]
 # histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit, no privatisation
 HIST_CFGS_SMALL = [(0x01, 1), (0x01, 2), (0x11, 2), (0x20, 1), (0x30, 1), (0x40, 1)]
@@ -43,7 +43,7 @@ def candidates(w):
     if k == KIND_REDUCE:
         return [{"block": b, "ipt": u, "cps": c, "variant": 0} for (b, u, c) in REDUCE_CFGS]
     if k == KIND_SCAN:
-        return [{"block": 256, "ipt": u, "cps": 0, "variant": 0} for u in SCAN_CFGS]
+        return [{"block": 256, "ipt": u, "cps": c, "variant": 0} for (u, c) in SCAN_CFGS]
     if k == KIND_SEG:
         return [{"block": 256, "ipt": u, "cps": 0, "variant": 0} for u in SEG_CFGS]
     cf = HIST_CFGS_2E16 if w["nbins"] > 24576 else HIST_CFGS_SMALL
@@ -290,7 +290,9 @@ def default_cfg_index(w, cs):
     for i, c in enumerate(cs):
         if k == KIND_REDUCE and (c["block"], c["ipt"], c["cps"]) == (256, 4, 8):
             return i
-        if k in (KIND_SCAN, KIND_SEG) and c["ipt"] == 4:
+        if k == KIND_SCAN and (c["ipt"], c["cps"]) == (9, 0):
+            return i
+        if k == KIND_SEG and c["ipt"] == 4:
             return i
         if k == KIND_HIST:
             want = 0x20 if w["nbins"] > 24576 else 0x01

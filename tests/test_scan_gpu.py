@@ -117,6 +117,50 @@ def test_inplace_and_misaligned(env):
     np.testing.assert_array_equal(yo.cpu().numpy(), oracle.scan(xi[1:], np.int64, inclusive=False, init=5))
 
 
+@pytest.mark.parametrize("ipt,cps", [(3, 1), (3, 0), (7, 1), (7, 0), (9, 1), (9, 0)])
+def test_tuned_ring_shapes(env, ipt, cps):
+    """Every (vectors per thread, CTAs per SM) shape of the persistent grid,
+    with few CTAs (many laps of the staging ring) and a ragged last tile;
+    totals through ParallelScanWithTotal."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    for pair, n in [(("i32", "i64"), (1 << 23) + 13), (("i64", "i64"), 3 * 8192 + 1), (("u32", "u32"), 999_999)]:
+        tin, tout = gbk.NP[gbk.DT[pair[0]]], gbk.NP[gbk.DT[pair[1]]]
+        x = datagen.uniform_i64(n, 0, 1000, seed=ipt * 10 + cps).astype(tin)
+        d = _dev(torch, x)
+        y = torch.empty(n, dtype=getattr(torch, np.dtype(tout).name), device="cuda")
+        tot = torch.zeros(1, dtype=y.dtype, device="cuda")
+        gbk.scan(d, y, inclusive=False, init=3, total=tot, tune=(256, ipt, cps, 0))
+        want = oracle.scan(x, tout, inclusive=False, init=3, nthreads=8)
+        np.testing.assert_array_equal(y.cpu().numpy(), want)
+        assert int(tot.item()) == int(want[-1]) + int(x[-1])
+    gbk.stream_check()
+
+
+def test_scan_2e28_properties(env):
+    """2^28 int32 -> int64 (1 GiB in, 2 GiB out), checked on the device by
+    size-independent properties: y[0] = init, y[i+1] - y[i] = x[i], total."""
+    gbk, torch = env
+    n = 1 << 28
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    x = torch.randint(0, 256, (n,), dtype=torch.int32, device="cuda", generator=g)
+    y = torch.empty(n, dtype=torch.int64, device="cuda")
+    tot = torch.zeros(1, dtype=torch.int64, device="cuda")
+    gbk.scan(x, y, inclusive=False, init=-7, total=tot)
+    gbk.stream_check()
+    assert int(y[0].item()) == -7
+    assert bool(torch.equal(y[1:] - y[:-1], x[:-1].to(torch.int64)))
+    assert int(tot.item()) == -7 + int(x.sum(dtype=torch.int64).item())
+    del y
+    yi = torch.empty(n, dtype=torch.int32, device="cuda")
+    xs = (x & 7).contiguous()
+    gbk.scan(xs, yi, inclusive=True)
+    gbk.stream_check()
+    assert bool(torch.equal(yi[1:] - yi[:-1], xs[1:])) and int(yi[0].item()) == int(xs[0].item())
+
+
 def test_many_launches_reuse_status_words(env):
     """Back-to-back scans of different sizes on one stream reuse the epoch-
     tagged status words without clearing them."""
