@@ -21,26 +21,18 @@
 // would need a generic-to-async proxy fence per tile, and that fence waited
 // for the ring's copies in flight: microseconds per tile.)
 //
-// Tile status is one 16-byte descriptor of two 64-bit words that both carry
-// the tag (epoch << 2) | status beside half of the value: a reader that finds
-// one tag in both words holds the whole value, so neither side needs a
-// fence.  (128-bit single-copy-atomic loads would do the same in one access,
-// but those were served one at a time, about 850 cycles each under load.)
-// The epoch (30 bits, fresh per launch) makes stale descriptors from earlier
-// launches read as "not ready", so no clearing is needed per launch.  A
-// look-back window is 128 or 256 descriptors per L2 round trip.  Every wait is bounded
-// by the library's wait limit and sets the timeout bit of the stream's error
-// word instead of hanging.
+// Tile status lives in the look-back descriptors of gbk_lookback.cuh (tagged
+// 64-bit word pairs, no fences, epoch-tagged so nothing is cleared per
+// launch).  Every wait is bounded by the library's wait limit and sets the
+// timeout bit of the stream's error word instead of hanging.
 #include <algorithm>
 #include <type_traits>
 
-#include "gbk_internal.cuh"
+#include "gbk_lookback.cuh"
 
 namespace gbk {
 namespace {
 
-constexpr unsigned FLAG_A = 1;  // tile aggregate available
-constexpr unsigned FLAG_P = 2;  // inclusive prefix available
 constexpr int SCAN_COMPUTE = 256;  // compute threads per CTA
 // Look-back warps: the CTA's tile slots go round-robin to them, so up to NLB
 // look-backs of one CTA are in flight at once (a look-back needs only its
@@ -52,61 +44,6 @@ constexpr int SCAN_BLOCK = SCAN_COMPUTE + 32 * NLB;
 constexpr int BAR_INFO = 1, BAR_PREFIX = 1 + NLB, BAR_COMPUTE = 1 + 2 * NLB;
 constexpr int BAR_HANDOFF = SCAN_COMPUTE + 32;  // threads in one hand-off
 static_assert(BAR_COMPUTE <= 15, "named barrier ids");
-
-// Descriptors per lane in a look-back window: 256 predecessors per round trip
-// for 4-byte sums, 128 for 8-byte sums (register budget; their tiles carry
-// more bytes, so fewer of them are in flight at the same bandwidth).
-template <class TO> constexpr int lookback_k() { return sizeof(TO) == 8 ? 4 : 8; }
-
-// Two 64-bit words, each {tag (32 bits) : half of the value (32 bits)}, with
-// tag = (epoch << 2) | status.  Each word is a single-copy-atomic access, and
-// every (epoch, status) of a tile is published once, so a reader that finds
-// the same tag in both words holds both halves of that publication; a torn
-// read (one word from the aggregate, one from the prefix) shows two tags and
-// counts as not ready.
-struct alignas(16) TileDesc {
-  unsigned long long w0, w1;
-};
-
-struct ScanState {
-  TileDesc* desc;
-  int* err;
-  unsigned epoch;  // 30 bits
-  int64_t ntiles;
-  int64_t wait_limit;
-};
-
-// Descriptor of tile t, one per 128-byte line: hundreds of look-backs poll
-// the few KB of descriptors behind the frontier, and packed 16 bytes apart
-// they sat on a handful of L2 slices (round trips of several microseconds).
-constexpr int DESC_STRIDE = 8;
-__device__ __forceinline__ TileDesc* desc_at(const ScanState& S, int64_t t) { return S.desc + t * DESC_STRIDE; }
-
-__device__ __forceinline__ void desc_store(TileDesc* p, unsigned tag, unsigned long long bits) {
-  const unsigned long long w0 = ((unsigned long long)tag << 32) | (bits & 0xFFFFFFFFull);
-  const unsigned long long w1 = ((unsigned long long)tag << 32) | (bits >> 32);
-  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(w0), "l"(w1) : "memory");
-}
-// tag = 0 (never a valid tag: epochs start at 1) when the two words disagree.
-__device__ __forceinline__ void desc_load(const TileDesc* p, unsigned* tag, unsigned long long* bits) {
-  unsigned long long w0, w1;
-  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(p) : "memory");
-  const unsigned t0 = (unsigned)(w0 >> 32), t1 = (unsigned)(w1 >> 32);
-  *tag = t0 == t1 ? t0 : 0u;
-  *bits = (w0 & 0xFFFFFFFFull) | (w1 << 32);
-}
-template <class TO>
-__device__ __forceinline__ unsigned long long to_bits(TO v) {
-  unsigned long long b = 0;
-  memcpy(&b, &v, sizeof(TO));
-  return b;
-}
-template <class TO>
-__device__ __forceinline__ TO from_bits(unsigned long long b) {
-  TO v;
-  memcpy(&v, &b, sizeof(TO));
-  return v;
-}
 
 template <class T> __device__ __forceinline__ T shup(T v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
 
@@ -120,86 +57,6 @@ __device__ __forceinline__ T warp_iscan(T v) {
     if (lane >= d) v = o + v;
   }
   return v;
-}
-
-template <class T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
-  return v;
-}
-
-// Look-back for `tile` (> 0, aggregate already published) by one full warp:
-// sums predecessors' aggregates back to the nearest inclusive prefix and
-// publishes the tile's inclusive prefix; returns the exclusive prefix (in
-// every lane).  A window is 32 * K descriptors, lane l holding distances
-// l*K .. l*K+K-1 from the window start, all loaded at once.  `bad` is set
-// when a wait gave up; the missing prefix then counts as zero.
-template <class TO, int K>
-__device__ __forceinline__ TO look_back(const ScanState& S, int64_t tile, TO tile_agg, bool* bad) {
-  static_assert(K >= 1 && K <= 16, "descriptors per lane");
-  const int lane = threadIdx.x & 31;
-  const unsigned ep = S.epoch << 2;
-  constexpr unsigned ALL = (1u << K) - 1u;
-  TO excl = TO(0);
-  int64_t base = tile - 1;
-  while (true) {
-    unsigned long long val[K];
-    unsigned okm = 0, pm = 0;  // per entry: status valid / inclusive prefix
-    const int64_t p0 = base - (int64_t)lane * K;
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      val[j] = 0;
-      if (p0 - j < 0) {  // before tile 0: a zero prefix
-        okm |= 1u << j;
-        pm |= 1u << j;
-      } else {
-        unsigned tg;
-        desc_load(desc_at(S, p0 - j), &tg, &val[j]);
-        if ((tg & ~3u) == ep && (tg & 3u)) okm |= 1u << j;
-        if (tg == (ep | FLAG_P)) pm |= 1u << j;
-      }
-    }
-    int64_t polls = 0;
-    unsigned ns = 0, need, lanes_p;
-    while (true) {
-      // Entries that count: everything before the nearest prefix and that
-      // prefix itself (lowest lane holding one, then its lowest entry).
-      lanes_p = __ballot_sync(0xffffffffu, pm != 0);
-      const int lp = lanes_p ? __ffs(lanes_p) - 1 : 32;
-      need = lane < lp ? ALL : (lane == lp ? (pm ^ (pm - 1u)) & ALL : 0u);
-      const unsigned miss = need & ~okm;
-      if (!__ballot_sync(0xffffffffu, miss != 0)) break;
-      if (++polls > S.wait_limit) {
-        // Give up; still publish, so that successors do not wait as well.
-        *bad = true;
-        if (lane == 0) desc_store(desc_at(S, tile), ep | FLAG_P, to_bits(tile_agg));
-        return TO(0);
-      }
-      if (polls > 2) {
-        ns = ns ? (ns < 256 ? ns * 2 : 256) : 32;
-        __nanosleep(ns);
-      }
-#pragma unroll
-      for (int j = 0; j < K; ++j) {
-        if ((miss >> j) & 1u) {
-          unsigned tg;
-          desc_load(desc_at(S, p0 - j), &tg, &val[j]);
-          if ((tg & ~3u) == ep && (tg & 3u)) okm |= 1u << j;
-          if (tg == (ep | FLAG_P)) pm |= 1u << j;
-        }
-      }
-    }
-    TO v = TO(0);
-#pragma unroll
-    for (int j = 0; j < K; ++j)
-      if ((need >> j) & 1u) v = v + from_bits<TO>(val[j]);
-    excl = excl + warp_sum(v);
-    if (lanes_p) break;
-    base -= 32 * K;
-  }
-  if (lane == 0) desc_store(desc_at(S, tile), ep | FLAG_P, to_bits(TO(excl + tile_agg)));
-  return excl;
 }
 
 // FAST: x and y are 16-byte aligned; tiles move by bulk copies through
@@ -220,7 +77,7 @@ __device__ __forceinline__ TO look_back(const ScanState& S, int64_t tile, TO til
 // threads each, and an out tile of one input tile's bytes).
 template <class TI, class TO, bool INCL, bool FAST, int IPT, int STAGES, int AHEAD, int ROUNDS>
 __global__ void __launch_bounds__(SCAN_BLOCK, 2)
-    k_scan(const TI* __restrict__ x, TO* __restrict__ y, int64_t n, TO init, ScanState S, TO* total) {
+    k_scan(const TI* __restrict__ x, TO* __restrict__ y, int64_t n, TO init, LbState S, TO* total) {
   constexpr int VEC = 16 / sizeof(TI);
   constexpr int WARPS = SCAN_COMPUTE / 32;
   constexpr int OVN = (int)(VEC * sizeof(TO) / 16);  // output vectors per input vector: 1 or 2
@@ -280,7 +137,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK, 2)
       const int64_t tile = s_info_tile[k];
       if (tile >= S.ntiles) break;
       const TO agg = s_info_agg[k];
-      const TO excl = tile == 0 ? TO(0) : look_back<TO, lookback_k<TO>()>(S, tile, agg, &bad);
+      const TO excl = tile == 0 ? TO(0) : look_back<TO, lb_k<TO>(), LbSum<TO>>(S, tile, agg, true, &bad);
       if (lane == 0) {
         s_excl[k] = excl;
         if (total && tile == S.ntiles - 1) *total = INCL ? excl + agg : init + (excl + agg);
@@ -334,7 +191,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK, 2)
         agg = agg + s_warp[j & 1][w];
       }
       if (threadIdx.x == 0) {
-        desc_store(desc_at(S, tile), (S.epoch << 2) | (tile == 0 ? FLAG_P : FLAG_A), to_bits(agg));
+        lb_publish(S, tile, tile == 0 ? LB_FLAG_P : LB_FLAG_A, agg);
         s_info_tile[j % NLB] = tile;
         s_info_agg[j % NLB] = agg;
       }
@@ -474,7 +331,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK, 2)
 // the static tile order needs): min(tiles, resident CTAs), or ctas_per_sm x
 // SMs when the tuning asks for fewer.
 template <class TI, class TO, bool INCL, bool FAST, int IPT, int STAGES, int AHEAD, int ROUNDS>
-int launch_k_scan(const TI* x, TO* y, int64_t n, TO init, const ScanState& S, TO* total, int cps, cudaStream_t s) {
+int launch_k_scan(const TI* x, TO* y, int64_t n, TO init, const LbState& S, TO* total, int cps, cudaStream_t s) {
   auto kfn = k_scan<TI, TO, INCL, FAST, IPT, STAGES, AHEAD, ROUNDS>;
   constexpr size_t in_bytes = (size_t)SCAN_COMPUTE * IPT * 16;
   // stages + out tile
@@ -532,8 +389,8 @@ int launch_scan_t(const TI* x, TO* y, int64_t n, TO init, TO* total, Workspace* 
   const int64_t ntiles = (n + tile - 1) / tile;
   if (ntiles >= (int64_t)0xFFFFFFFFu - (1 << 24)) return GBK_ERR_INVALID_ARGUMENT;
   int st = GBK_OK;
-  ScanState S;
-  S.desc = (TileDesc*)ws_flags(w, (size_t)ntiles * DESC_STRIDE * (sizeof(TileDesc) / sizeof(unsigned)), &S.epoch, &st);
+  LbState S;
+  S.desc = (TileDesc*)ws_flags(w, lb_flag_words(ntiles), &S.epoch, &st);
   if (!S.desc) return st;
   S.err = w->err;
   S.ntiles = ntiles;

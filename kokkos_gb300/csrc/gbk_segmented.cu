@@ -5,26 +5,29 @@
 // parallel_reduce / inclusive_scan launch per segment.
 //
 // Segments are given by offsets[0..nseg] (segment s = [offsets[s],
-// offsets[s+1]), non-decreasing, offsets[nseg] = n).  The concatenated array
-// is cut into fixed tiles of BLOCK*IPT*VEC elements, independent of the
-// segment lengths, so the work is balanced whatever the length
-// distribution.  Per tile:
-//   * warp 0 finds the segment starts that fall in the tile with a 32-ary
-//     search of offsets and the CTA marks them in a shared-memory bitmap;
-//   * a segmented scan (pairs (head-seen, value), operator
-//     (h1,v1).(h2,v2) = (h1|h2, h2 ? v2 : v1 op v2)) runs in registers, then
-//     across warps;
-//   * the carry into the tile comes from a decoupled look-back over the
-//     predecessor tiles that stops at the first tile holding a segment head
-//     (normally the previous tile), so long segments chain and short ones
-//     never wait long;
-//   * REDUCE mode writes each segment's total at its last element; scan
-//     modes write every element.
-// Tile status words are epoch-tagged (no memset per launch) and every wait is
-// bounded.
+// offsets[s+1]), non-decreasing, offsets[0] = 0, offsets[nseg] = n).  The
+// concatenated array is cut into fixed tiles of 256 * IPT 16-byte vectors,
+// independent of the segment lengths, so the work is balanced whatever the
+// length distribution.  One persistent, warp-specialised kernel on a
+// cooperative (co-resident) grid, CTA b owning tiles b, b + G, ...:
+//   * phase 0 (all threads): zero a head bitmap (one bit per element), grid
+//     barrier, then one bit per segment start and, per tile, the first
+//     segment starting in it; identities for empty segments (reduce); grid
+//     barrier.  Bounded waits;
+//   * the tile pipeline of the plain scan (gbk_scan.cu): each tile's input
+//     and its bitmap row arrive by one bulk copy into a two-stage ring; the
+//     compute warps do the tile sums of tile i+1 and then the outputs of tile
+//     i; look-back warps resolve the carry into each tile.  The operator is
+//     the segmented one on pairs (head seen, value):
+//     (h1, v1) . (h2, v2) = (h1 | h2, h2 ? v2 : v1 op v2).  A tile holding a
+//     head publishes its inclusive prefix (the value after its last head) at
+//     once, so long chains only form inside long segments;
+//   * reduce mode writes each segment's total at its last element; scan
+//     modes write every element through a shared-memory out tile.
+#include <algorithm>
 #include <type_traits>
 
-#include "gbk_internal.cuh"
+#include "gbk_lookback.cuh"
 
 namespace gbk {
 namespace {
@@ -45,333 +48,470 @@ template <class T> struct SOp<T, GBK_MAX> {
   __device__ static T f(T a, T b) { return b > a ? b : a; }
 };
 
-template <class TO>
-struct SegState {
-  unsigned* flags;  // epoch << 2 | status: 1 = aggregate, 3 = aggregate of a tile holding a head, 2 = prefix
-  TO* agg;
-  TO* incl;
-  unsigned* ticket;
-  int* err;
-  unsigned epoch;  // 30 bits, shared with the plain scan's status words
-  int64_t ntiles;
-  int64_t wait_limit;
+constexpr int SEG_COMPUTE = 256;  // compute threads
+constexpr int SEG_NLB = 4;        // look-back warps, tile slots round-robin
+constexpr int SEG_BLOCK = SEG_COMPUTE + 32 * SEG_NLB;
+constexpr int SBAR_INFO = 1, SBAR_PREFIX = 1 + SEG_NLB, SBAR_COMPUTE = 1 + 2 * SEG_NLB;
+constexpr int SBAR_HANDOFF = SEG_COMPUTE + 32;
+static_assert(SBAR_COMPUTE <= 15, "named barrier ids");
+
+struct SegArgs {
+  const int64_t* offsets;
+  int64_t nseg;
+  unsigned* bitmap;   // (ntiles + 1) rows of TILE / 32 words, then 4 spare words
+  int64_t* tile_lo;   // [ntiles + 1]: first segment s with offsets[s] >= t * TILE
+  unsigned* arrive;   // grid barrier counters (zero between launches)
+  unsigned* depart;
 };
+
+// Bounded grid barrier of a co-resident grid; `target` counts CTAs arrived so
+// far over all barriers of the launch.  False when it gave up.
+__device__ bool grid_barrier(unsigned* arrive, unsigned target, int64_t limit, int* s_ok) {
+  __threadfence();  // every thread's writes, before the CTA's arrival
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(arrive, 1u);
+    int64_t polls = 0;
+    int ok = 1;
+    while (ld_acquire_u32(arrive) < target) {
+      if (++polls > limit) {
+        ok = 0;
+        break;
+      }
+      __nanosleep(polls < 8 ? 32 : 256);
+    }
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+// Phase 0: head bitmap, per-tile first segment, empty-segment identities.
+template <class TO, int OP, int MODE>
+__device__ void seg_phase0(const SegArgs& A, TO* y, int64_t n, int64_t tile_elems, int64_t ntiles,
+                           int64_t wait_limit, bool* bad, int* s_ok) {
+  using O = SOp<TO, OP>;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
+  const int64_t words = (ntiles + 1) * (tile_elems / 32) + 4;
+  for (int64_t i = tid; i < words; i += nthr) A.bitmap[i] = 0u;
+  if (!grid_barrier(A.arrive, gridDim.x, wait_limit, s_ok)) *bad = true;
+  for (int64_t s = tid; s <= A.nseg; s += nthr) {
+    const int64_t p = A.offsets[s];
+    if (s < A.nseg && p < n) atomicOr(A.bitmap + p / 32, 1u << (p & 31));
+    // Tiles whose first element falls in (offsets[s-1], offsets[s]] start at s.
+    const int64_t prev = s > 0 ? A.offsets[s - 1] : -1;
+    int64_t t0 = prev < 0 ? 0 : prev / tile_elems + 1;
+    const int64_t t1 = p / tile_elems;  // last tile t with t * tile_elems <= p
+    for (int64_t t = t0; t <= t1 && t <= ntiles; ++t) A.tile_lo[t] = s;
+    if (MODE == M_REDUCE && s < A.nseg && A.offsets[s + 1] == p) y[s] = O::id();
+  }
+  // Tiles past the last segment start (only when offsets end below n).
+  for (int64_t t = A.offsets[A.nseg] / tile_elems + 1 + tid; t <= ntiles; t += nthr) A.tile_lo[t] = A.nseg + 1;
+  if (!grid_barrier(A.arrive, 2 * gridDim.x, wait_limit, s_ok)) *bad = true;
+}
 
 template <class T> __device__ __forceinline__ T sh_up(T v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
 
-template <class TO>
-__device__ __forceinline__ TO ld_relaxed_any(const TO* p) {
-  if constexpr (sizeof(TO) == 8) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    TO r;
-    memcpy(&r, &v, 8);
-    return r;
-  } else {
-    unsigned v;
-    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    TO r;
-    memcpy(&r, &v, 4);
-    return r;
-  }
-}
-
-// First index s in [lo, hi) with offsets[s] >= key (hi if none), by one
-// warp: each round 32 lanes probe evenly spaced indices.
-__device__ int64_t warp_lower_bound(const int64_t* __restrict__ offsets, int64_t lo, int64_t hi, int64_t key) {
-  const int lane = threadIdx.x & 31;
-  while (hi - lo > 32) {
-    const int64_t step = (hi - lo + 31) / 32;
-    const int64_t idx = lo + lane * step;
-    const bool ge = idx < hi ? (__ldg(offsets + idx) >= key) : true;
-    const unsigned m = __ballot_sync(0xffffffffu, ge);
-    const int first = m ? __ffs(m) - 1 : 32;  // first probe with offsets >= key
-    const int64_t nlo = first == 0 ? lo : lo + (int64_t)(first - 1) * step;
-    const int64_t nhi = first == 32 ? hi : (lo + (int64_t)first * step < hi ? lo + (int64_t)first * step : hi);
-    lo = nlo;
-    hi = (nhi > lo) ? nhi : lo;
-    if (first == 0) { hi = lo; break; }
-  }
-  const int64_t idx = lo + lane;
-  const bool ge = idx < hi ? (__ldg(offsets + idx) >= key) : true;
-  const unsigned m = __ballot_sync(0xffffffffu, ge);
-  const int first = m ? __ffs(m) - 1 : 32;
-  const int64_t r = lo + first;
-  return r < hi ? r : hi;
-}
-
-template <class TI, class TO, int OP, int MODE, bool ALIGNED, int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK)
-    k_segmented(const TI* __restrict__ x, TO* __restrict__ y, int64_t n, const int64_t* __restrict__ offsets,
-                int64_t nseg, SegState<TO> S) {
+// FAST: x (and, for scans, y) 16-byte aligned: input tiles by bulk copy,
+// scan outputs through the out tile.  Otherwise direct element loads and
+// stores with the same mapping.  Compute thread i owns the C = IPT * VEC
+// consecutive elements starting at i * C (IPT odd: conflict-free shared
+// reads); C <= 32, so its head bits (and the next element's) sit in one
+// 64-bit window of the bitmap row.
+template <class TI, class TO, int OP, int MODE, bool FAST, int IPT, int STG>
+__global__ void __launch_bounds__(SEG_BLOCK, 2)
+    k_seg(const TI* __restrict__ x, TO* __restrict__ y, int64_t n, SegArgs A, LbState S) {
   using O = SOp<TO, OP>;
   constexpr int VEC = 16 / sizeof(TI);
-  constexpr int WARPS = BLOCK / 32;
-  constexpr int TILE = BLOCK * IPT * VEC;
-  constexpr int WSLICE = 32 * IPT * VEC;
-  constexpr int BMW = TILE / 32 + 2;  // bitmap words covering [tbase, tbase + TILE]
-  __shared__ unsigned s_bm[BMW];
-  __shared__ int64_t s_tile, s_lo, s_hi;
-  __shared__ TO s_wv[WARPS];
-  __shared__ unsigned s_wh[WARPS];
-  __shared__ int s_near, s_timeout;
-  __shared__ TO s_wsum[WARPS];
+  constexpr int C = IPT * VEC;
+  constexpr int WARPS = SEG_COMPUTE / 32;
+  constexpr int OVN = (int)(VEC * sizeof(TO) / 16);
+  constexpr int OV = 16 / sizeof(TO);
+  constexpr int64_t TILE = (int64_t)SEG_COMPUTE * C;
+  constexpr unsigned IN_BYTES = (unsigned)SEG_COMPUTE * IPT * 16;
+  constexpr unsigned BM_BYTES = (unsigned)(TILE / 8) + 16;  // the tile's row and the next row's first word
+  constexpr unsigned STAGE_BYTES = (IN_BYTES + BM_BYTES + 127) / 128 * 128;
+  constexpr bool OUT_TILE = FAST && MODE != M_REDUCE;
+  static_assert(IPT % 2 == 1 && C <= 32, "odd vector count, at most 32 elements per thread");
+  static_assert(OVN == 1 || OVN == 2, "output at most twice the input width");
+  static_assert(STG >= 2, "the stage of tile i+1 is summed while tile i is written");
+  extern __shared__ __align__(128) unsigned char dsm[];  // STG stages {input, bitmap row}, then the out tile
+  __shared__ __align__(8) unsigned long long s_bar[STG];
+  __shared__ int64_t s_info_tile[SEG_NLB];
+  __shared__ TO s_info_agg[SEG_NLB];
+  __shared__ unsigned s_info_h[SEG_NLB];  // head / first-element head / segment end flags
+  __shared__ TO s_excl[SEG_NLB];
+  __shared__ TO s_wv[2][WARPS];
+  __shared__ unsigned s_wh[2][WARPS];
+  __shared__ int s_bad, s_ok;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t nin = FAST ? n / VEC * VEC : 0;
+  const int64_t nout = OUT_TILE ? n / OV * OV : 0;
+  unsigned char* outt = dsm + (size_t)STG * STAGE_BYTES;
+  auto tile_of = [&](int j) { return (int64_t)blockIdx.x + (int64_t)j * gridDim.x; };
 
   if (threadIdx.x == 0) {
-    const unsigned t = atomicAdd(S.ticket, 1u);
-    if ((int64_t)t == S.ntiles - 1) *S.ticket = 0u;
-    s_tile = (int64_t)t;
-    s_timeout = 0;
+    s_bad = 0;
+#pragma unroll
+    for (int q = 0; q < STG; ++q) mbar_init(&s_bar[q], 1);
+    fence_mbar_init();
   }
-  for (int i = threadIdx.x; i < BMW; i += BLOCK) s_bm[i] = 0u;
-  __syncthreads();
-  const int64_t tile = s_tile;
-  const int64_t tbase = tile * (int64_t)TILE;
-  if (MODE == M_REDUCE) {
-    // Empty segments get the identity (their start is shared with the next).
-    for (int64_t s = tile * BLOCK + threadIdx.x; s < nseg; s += S.ntiles * BLOCK)
-      if (offsets[s + 1] == offsets[s]) y[s] = O::id();
-  }
-  if (warp == 0) {
-    const int64_t lo = warp_lower_bound(offsets, 0, nseg + 1, tbase);
-    const int64_t hi = warp_lower_bound(offsets, lo, nseg + 1, tbase + TILE + 1);
-    if (lane == 0) { s_lo = lo; s_hi = hi; }
-  }
-  __syncthreads();
-  for (int64_t s = s_lo + threadIdx.x; s < s_hi; s += BLOCK) {
-    const int64_t p = offsets[s] - tbase;  // in [0, TILE]
-    atomicOr(&s_bm[p >> 5], 1u << (p & 31));
-  }
-  __syncthreads();
-  auto head = [&](int64_t e) -> unsigned {  // e relative to tbase, 0..TILE
-    return (s_bm[e >> 5] >> (e & 31)) & 1u;
-  };
+  bool bad = false;
+  seg_phase0<TO, OP, MODE>(A, y, n, TILE, S.ntiles, S.wait_limit, &bad, &s_ok);
 
-  const int wb = warp * WSLICE;
-  const bool full = tbase + TILE <= n;
-  TI v[IPT][VEC];
+  // Thread 0 only: start the copies of the CTA's j-th tile (input and bitmap row).
+  auto fill = [&](int j) {
+    const int64_t t = tile_of(j);
+    if (t >= S.ntiles) return;
+    const int s = j % STG;
+    unsigned char* stg = dsm + (size_t)s * STAGE_BYTES;
+    const int64_t e0 = t * TILE;
+    const int64_t cnt = FAST ? (nin - e0 < TILE ? nin - e0 : TILE) : 0;
+    const unsigned in_bytes = cnt > 0 ? (unsigned)(cnt * (int64_t)sizeof(TI)) : 0u;
+    mbar_arrive_expect_tx(&s_bar[s], in_bytes + BM_BYTES);
+    if (in_bytes) bulk_g2s(stg, x + e0, in_bytes, &s_bar[s]);
+    bulk_g2s(stg + IN_BYTES, A.bitmap + t * (TILE / 32), BM_BYTES, &s_bar[s]);
+  };
+  if (threadIdx.x == 0) {
+    // The bitmap was written through the generic proxy; the bulk copies read
+    // it through the async proxy.
+    asm volatile("fence.proxy.async;" ::: "memory");
 #pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    const int64_t e0 = tbase + wb + (k * 32 + lane) * VEC;
-    if (ALIGNED && full) {
-      Vec16<TI> u;
-      u.u = ld_stream16(x + e0);
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) v[k][j] = u.v[j];
-    } else {
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) v[k][j] = (e0 + j < n) ? x[e0 + j] : TI(0);
-    }
+    for (int q = 0; q < STG; ++q) fill(q);
   }
-  // chunk aggregates (head seen, value after the last head)
-  TO cv[IPT];
-  unsigned ch[IPT];
-#pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    const int r0 = wb + (k * 32 + lane) * VEC;
-    TO a = O::id();
-    unsigned h = 0;
-#pragma unroll
-    for (int j = 0; j < VEC; ++j) {
-      const bool valid = tbase + r0 + j < n;
-      const unsigned hj = head(r0 + j);
-      if (hj) { a = O::id(); h = 1; }
-      if (valid) a = O::f(a, (TO)v[k][j]);
-    }
-    cv[k] = a;
-    ch[k] = h;
-  }
-  // warp segmented scan over chunks in (k, lane) order: exclusive carry per chunk
-  TO cin[IPT];
-  unsigned cinh[IPT];  // a head occurs in this warp before the chunk
-  TO carry = O::id();
-  unsigned carry_h = 0;
-#pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    TO iv = cv[k];
-    unsigned ih = ch[k];
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const TO ov = sh_up(iv, d);
-      const unsigned oh = sh_up(ih, d);
-      if (lane >= d) {
-        if (!ih) iv = O::f(ov, iv);
-        ih |= oh;
-      }
-    }
-    // exclusive within the row, then apply the row carry
-    TO ev = sh_up(iv, 1);
-    unsigned eh = sh_up(ih, 1);
-    if (lane == 0) { ev = O::id(); eh = 0; }
-    cin[k] = eh ? ev : O::f(carry, ev);
-    cinh[k] = eh | carry_h;
-    const TO rv = __shfl_sync(0xffffffffu, iv, 31);
-    const unsigned rh = __shfl_sync(0xffffffffu, ih, 31);
-    carry = rh ? rv : O::f(carry, rv);
-    carry_h |= rh;
-  }
-  if (lane == 0) { s_wv[warp] = carry; s_wh[warp] = carry_h; }
   __syncthreads();
-  // carry into this warp from earlier warps of the tile, and the tile aggregate
-  TO wpre = O::id(), tagg = O::id();
-  unsigned wpre_h = 0, tagg_h = 0;
-#pragma unroll
-  for (int w = 0; w < WARPS; ++w) {
-    if (w == warp) { wpre = tagg; wpre_h = tagg_h; }
-    tagg = s_wh[w] ? s_wv[w] : O::f(tagg, s_wv[w]);
-    tagg_h |= s_wh[w];
-  }
-  // ---- look-back: carry from predecessor tiles ------------------------------
-  const unsigned ep = S.epoch << 2;
-  TO excl = O::id();
-  if (tile == 0) {
-    if (threadIdx.x == 0) {
-      S.incl[0] = tagg;
-      st_release_u32(S.flags, ep | 2u);
+
+  if (warp >= WARPS) {
+    // ---- look-back warp k: the CTA's tile slots k, k + NLB, ... -------------
+    const int k = warp - WARPS;
+    while (true) {
+      bar_sync(SBAR_INFO + k, SBAR_HANDOFF);
+      const int64_t tile = s_info_tile[k];
+      if (tile >= S.ntiles) break;
+      const TO agg = s_info_agg[k];
+      const unsigned hf = s_info_h[k];
+      // No carry needed when the tile starts a segment, nor (reduce) when no
+      // segment ends in it: its aggregate is all that later tiles need.  A
+      // tile holding a head has published its prefix already.
+      const bool skip = tile == 0 || (hf & 2u) || (MODE == M_REDUCE && !(hf & 4u));
+      const TO excl = skip ? O::id() : look_back<TO, lb_k<TO>(), O>(S, tile, agg, !(hf & 1u), &bad);
+      if (lane == 0) s_excl[k] = excl;
+      bar_arrive(SBAR_PREFIX + k, SBAR_HANDOFF);
     }
   } else {
-    if (threadIdx.x == 0) {
-      S.agg[tile] = tagg;
-      st_release_u32(S.flags + tile, ep | (tagg_h ? 3u : 1u));
-    }
-    int64_t pt0 = tile - 1;
-    while (true) {
-      const int64_t pt = pt0 - threadIdx.x;
-      unsigned f = ep | 2u;
-      TO val = O::id();
-      if (threadIdx.x == 0) s_near = BLOCK;
-      __syncthreads();
-      if (pt >= 0) {
-        int64_t polls = 0;
-        unsigned ns = 0;
-        while (true) {
-          f = ld_relaxed_u32(S.flags + pt);
-          if ((f & ~3u) == ep && (f & 3u)) break;
-          if (++polls > S.wait_limit || *(volatile int*)&s_timeout) {
-            f = ep | 2u;
-            atomicExch(&s_timeout, 1);
-            break;
-          }
-          if (polls > 8) {
-            ns = ns ? (ns < 256 ? ns * 2 : 256) : 32;
-            __nanosleep(ns);
-          }
-        }
-        __threadfence();
-        if (!*(volatile int*)&s_timeout) val = ((f & 3u) == 2u) ? ld_relaxed_any(S.incl + pt) : ld_relaxed_any(S.agg + pt);
-      }
-      // stop at the nearest tile that is complete (P) or holds a segment head
-      if (f & 2u) atomicMin(&s_near, (int)threadIdx.x);  // prefix, or a tile holding a head
-      __syncthreads();
-      const int near = s_near;
-      TO c = ((int)threadIdx.x <= near) ? val : O::id();
+    // ---- compute warps ------------------------------------------------------
+    const int r0 = threadIdx.x * C;  // this thread's first element in the tile
+    auto load_vec = [&](int s, int64_t tbase, int jj, TI (&v)[VEC]) {
+      const int64_t e0 = tbase + r0 + jj * VEC;
+      const unsigned char* stg = dsm + (size_t)s * STAGE_BYTES;
+      if (FAST && tbase + TILE <= nin) {
+        Vec16<TI> u;
+        u.u = reinterpret_cast<const uint4*>(stg)[threadIdx.x * IPT + jj];
 #pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) c = O::f(c, __shfl_xor_sync(0xffffffffu, c, m));
-      if (lane == 0) s_wsum[warp] = c;
-      __syncthreads();
+        for (int q = 0; q < VEC; ++q) v[q] = u.v[q];
+      } else if (FAST) {
+        const TI* sv = reinterpret_cast<const TI*>(stg) + r0 + jj * VEC;
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) excl = O::f(excl, s_wsum[w]);
-      if (near < BLOCK) break;
-      pt0 -= BLOCK;
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      if (s_timeout) atomicOr(S.err, GBK_EBIT_TIMEOUT);
-      // inclusive prefix value at the end of this tile
-      S.incl[tile] = tagg_h ? tagg : O::f(excl, tagg);
-      st_release_u32(S.flags + tile, ep | 2u);
-    }
-  }
-  // ---- outputs ---------------------------------------------------------------
-  const TO wbase_v = wpre_h ? wpre : O::f(excl, wpre);
-#pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    const int r0 = wb + (k * 32 + lane) * VEC;
-    const int64_t e0 = tbase + r0;
-    // Carry into the chunk: cin[k] covers the warp's earlier chunks; the
-    // carry from earlier warps and tiles applies unless a head came first.
-    TO run = cin[k];
-    if (!cinh[k]) run = O::f(wbase_v, run);
-    TO o[VEC];
-#pragma unroll
-    for (int j = 0; j < VEC; ++j) {
-      const bool valid = e0 + j < n;
-      if (head(r0 + j)) run = O::id();
-      if (MODE == M_EXCL) o[j] = run;
-      if (valid) run = O::f(run, (TO)v[k][j]);
-      if (MODE == M_INCL) o[j] = run;
-      if (MODE == M_REDUCE && valid && head(r0 + j + 1)) {
-        // last element of its segment: find the (non-empty) segment s with
-        // offsets[s] <= e < offsets[s+1]
-        const int64_t e = e0 + j;
-        int64_t lo = s_lo > 0 ? s_lo - 1 : 0, hi = s_hi;  // s in [lo, hi)
-        while (hi - lo > 1) {
-          const int64_t mid = lo + (hi - lo) / 2;
-          if (offsets[mid] <= e) lo = mid; else hi = mid;
-        }
-        y[lo] = run;
-      }
-    }
-    if (MODE != M_REDUCE) {
-      if (ALIGNED && full) {
-        constexpr int OV = 16 / sizeof(TO);
-#pragma unroll
-        for (int j = 0; j < VEC; j += OV) {
-          Vec16<TO> u;
-#pragma unroll
-          for (int q = 0; q < OV; ++q) u.v[q] = o[j + q];
-          __stcs(reinterpret_cast<uint4*>(y + e0 + j), u.u);
-        }
+        for (int q = 0; q < VEC; ++q) v[q] = e0 + q < nin ? sv[q] : (e0 + q < n ? x[e0 + q] : TI(0));
       } else {
 #pragma unroll
-        for (int j = 0; j < VEC; ++j)
-          if (e0 + j < n) y[e0 + j] = o[j];
+        for (int q = 0; q < VEC; ++q) v[q] = e0 + q < n ? x[e0 + q] : TI(0);
       }
+    };
+    // Head bits of this thread's elements (bit k: element r0 + k) and the next.
+    auto head_bits = [&](int s) -> unsigned long long {
+      const unsigned* bm = reinterpret_cast<const unsigned*>(dsm + (size_t)s * STAGE_BYTES + IN_BYTES);
+      const int w = r0 >> 5;
+      return ((unsigned long long)bm[w] | ((unsigned long long)bm[w + 1] << 32)) >> (r0 & 31);
+    };
+    // Tile sums of the CTA's j-th tile: this thread's exclusive pair within
+    // its warp (eh, ev) and its warp's within the tile (wh, wv); thread 0
+    // publishes the tile's aggregate (its prefix, if it holds a head).
+    auto tile_sums = [&](int j, int64_t tile, unsigned& eh, TO& ev, unsigned& wh, TO& wv) {
+      const int s = j % STG;
+      if (!mbar_wait(&s_bar[s], (unsigned)(j / STG) & 1u, S.wait_limit)) bad = true;
+      const unsigned long long hb = head_bits(s);
+      const int64_t tbase = tile * TILE;
+      TO a = O::id();
+      unsigned h = 0;
+#pragma unroll
+      for (int jj = 0; jj < IPT; ++jj) {
+        TI v[VEC];
+        load_vec(s, tbase, jj, v);
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          const int kk = jj * VEC + q;
+          if ((hb >> kk) & 1u) {
+            a = O::id();
+            h = 1;
+          }
+          if (tbase + r0 + kk < n) a = O::f(a, (TO)v[q]);
+        }
+      }
+      TO iv = a;
+      unsigned ih = h;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const TO ov = sh_up(iv, d);
+        const unsigned oh = sh_up(ih, d);
+        if (lane >= d) {
+          if (!ih) iv = O::f(ov, iv);
+          ih |= oh;
+        }
+      }
+      ev = sh_up(iv, 1);
+      eh = sh_up(ih, 1);
+      if (lane == 0) {
+        ev = O::id();
+        eh = 0;
+      }
+      // Reduce: does a segment end among this warp's elements?  (A head at
+      // element r0 + k, k = 1..C, ends the segment at r0 + k - 1.)
+      bool my_end = false;
+      if (MODE == M_REDUCE) {
+        const int64_t e_first = tbase + r0;
+        my_end = e_first < n && ((((hb >> 1) & ((1ull << C) - 1ull)) != 0) || (n - 1 < e_first + C));
+      }
+      const unsigned wend = __any_sync(0xffffffffu, my_end) ? 2u : 0u;
+      if (lane == 31) {
+        s_wv[j & 1][warp] = iv;
+        s_wh[j & 1][warp] = ih | wend;
+      }
+      bar_sync(SBAR_COMPUTE, SEG_COMPUTE);
+      TO agg = O::id();
+      unsigned ah = 0, tend = 0;
+      wv = O::id();
+      wh = 0;
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) {
+        if (w == warp) {
+          wv = agg;
+          wh = ah;
+        }
+        const TO sv = s_wv[j & 1][w];
+        const unsigned shh = s_wh[j & 1][w];
+        agg = (shh & 1u) ? sv : O::f(agg, sv);
+        ah |= shh & 1u;
+        tend |= shh >> 1;
+      }
+      if (threadIdx.x == 0) {
+        lb_publish(S, tile, (tile == 0 || ah) ? LB_FLAG_P : LB_FLAG_A, agg);
+        s_info_tile[j % SEG_NLB] = tile;
+        s_info_agg[j % SEG_NLB] = agg;
+        // bit 0: a head in the tile, 1: a head at its first element (thread 0
+        // owns element 0), 2: a segment ends in it
+        s_info_h[j % SEG_NLB] = ah | ((unsigned)(hb & 1u) << 1) | (tend << 2);
+      }
+    };
+    auto hand_off = [&](int j) { bar_arrive(SBAR_INFO + j % SEG_NLB, SBAR_HANDOFF); };
+
+    unsigned q_eh = 0, q_wh = 0;  // pairs of the tile summed but not yet written
+    TO q_ev = O::id(), q_wv = O::id();
+    if (tile_of(0) < S.ntiles) {
+      tile_sums(0, tile_of(0), q_eh, q_ev, q_wh, q_wv);
+      hand_off(0);
+    }
+    int i = 0;
+    for (; tile_of(i) < S.ntiles; ++i) {
+      unsigned n_eh = 0, n_wh = 0;
+      TO n_ev = O::id(), n_wv = O::id();
+      if (tile_of(i + 1) < S.ntiles) {
+        tile_sums(i + 1, tile_of(i + 1), n_eh, n_ev, n_wh, n_wv);
+        hand_off(i + 1);
+      }
+      bar_sync(SBAR_PREFIX + i % SEG_NLB, SBAR_HANDOFF);
+      const TO excl = s_excl[i % SEG_NLB];
+
+      // ---- output pass of the CTA's i-th tile (stage i % STG) ----------------
+      const int s = i % STG;
+      const int64_t tile = tile_of(i);
+      const int64_t tbase = tile * TILE;
+      const unsigned long long hb = head_bits(s);
+      const TO v1 = q_wh ? q_wv : O::f(excl, q_wv);  // carry into this warp
+      TO run = q_eh ? q_ev : O::f(v1, q_ev);         // carry into this thread
+      const bool out_full = OUT_TILE && tbase + TILE <= nout;
+      // Reduce: nothing to write from a tile in which no segment ends.
+      const int passes = (MODE != M_REDUCE || (s_info_h[i % SEG_NLB] & 4u)) ? IPT : 0;
+#pragma unroll
+      for (int jj = 0; jj < IPT; ++jj) {
+        if (jj >= passes) break;
+        TI v[VEC];
+        load_vec(s, tbase, jj, v);
+        TO o[VEC];
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          const int kk = jj * VEC + q;
+          const int64_t e = tbase + r0 + kk;
+          if ((hb >> kk) & 1u) run = O::id();
+          if (MODE == M_EXCL) o[q] = run;
+          if (e < n) run = O::f(run, (TO)v[q]);
+          if (MODE == M_INCL) o[q] = run;
+          if (MODE == M_REDUCE && e < n && (((hb >> (kk + 1)) & 1u) || e == n - 1)) {
+            // Last element of its segment: the segment is the last s with
+            // offsets[s] <= e, among those that can touch this tile.
+            int64_t lo = __ldcg(A.tile_lo + tile) - 1, hi = __ldcg(A.tile_lo + tile + 1);
+            if (lo < 0) lo = 0;
+            if (hi > A.nseg) hi = A.nseg;
+            while (hi - lo > 1) {  // offsets[lo] <= e < offsets[hi] (or hi = nseg)
+              const int64_t mid = lo + (hi - lo) / 2;
+              if (__ldg(A.offsets + mid) <= e) lo = mid; else hi = mid;
+            }
+            y[lo] = run;
+          }
+        }
+        if (MODE != M_REDUCE) {
+          if (OUT_TILE) {
+            uint4* ov = reinterpret_cast<uint4*>(outt) + ((size_t)threadIdx.x * IPT + jj) * OVN;
+            if constexpr (OVN == 1) {
+              Vec16<TO> u;
+#pragma unroll
+              for (int q = 0; q < VEC; ++q) u.v[q] = o[q];
+              ov[0] = u.u;
+            } else {
+              // Lanes 4..7 of each quarter-warp write their second vector
+              // first: with the odd stride each step hits 8 bank groups.
+              Vec16<TO> a, b;
+#pragma unroll
+              for (int q = 0; q < OV; ++q) {
+                a.v[q] = o[q];
+                b.v[q] = o[OV + q];
+              }
+              const int flip = (lane >> 2) & 1;
+              ov[flip] = flip ? b.u : a.u;
+              ov[flip ^ 1] = flip ? a.u : b.u;
+            }
+            if (!out_full) {
+#pragma unroll
+              for (int q = 0; q < VEC; ++q) {
+                const int64_t e = tbase + r0 + jj * VEC + q;
+                if (e >= nout && e < n) y[e] = o[q];
+              }
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < VEC; ++q) {
+              const int64_t e = tbase + r0 + jj * VEC + q;
+              if (e < n) y[e] = o[q];
+            }
+          }
+        }
+      }
+      // Stage s (and the out tile) complete: refill the stage, and stream the
+      // out tile in warp-striped order (512 contiguous bytes per warp
+      // instruction).  The out tile is next written after the next prefix
+      // barrier.
+      bar_sync(SBAR_COMPUTE, SEG_COMPUTE);
+      if (threadIdx.x == 0) fill(i + STG);
+      if (OUT_TILE) {
+        const uint4* ov = reinterpret_cast<const uint4*>(outt);
+        uint4* yv = reinterpret_cast<uint4*>(y + tbase);
+        const int64_t left = nout - tbase < TILE ? nout - tbase : TILE;
+        const int64_t nvec = left > 0 ? left * (int64_t)sizeof(TO) / 16 : 0;
+#pragma unroll
+        for (int k = 0; k < IPT * OVN; ++k) {
+          const int q = k * SEG_COMPUTE + threadIdx.x;
+          if (out_full || q < nvec) __stcs(yv + q, ov[q]);
+        }
+      }
+      q_eh = n_eh;
+      q_ev = n_ev;
+      q_wh = n_wh;
+      q_wv = n_wv;
+    }
+    // i = the number of tiles handed off: one end mark per look-back warp.
+    for (int j = i; j < i + SEG_NLB; ++j) {
+      if (threadIdx.x == 0) s_info_tile[j % SEG_NLB] = S.ntiles;
+      hand_off(j);
+    }
+  }
+
+  if (bad) s_bad = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_bad) atomicOr(S.err, GBK_EBIT_TIMEOUT);
+    // The last CTA to leave resets the barrier counters for the next launch
+    // (every CTA has passed both barriers by then).
+    __threadfence();
+    if (atomicAdd(A.depart, 1u) == gridDim.x - 1) {
+      *A.arrive = 0u;
+      *A.depart = 0u;
     }
   }
 }
 
-template <class TI, class TO, int OP, int MODE, int IPT>
-int launch_seg_ipt(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t nseg, Workspace* w) {
-  constexpr int BLOCK = 256, VEC = 16 / sizeof(TI);
-  constexpr int64_t TILE = (int64_t)BLOCK * IPT * VEC;
-  cudaStream_t s = w->stream;
+// One cooperative launch (all CTAs co-resident: the grid barriers and the
+// static tile order need it): min(tiles, resident CTAs), or ctas_per_sm x SMs
+// when the tuning asks for fewer.
+template <class TI, class TO, int OP, int MODE, bool FAST, int IPT, int STG>
+int launch_k_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t nseg, Workspace* w, int cps) {
+  constexpr int VEC = 16 / sizeof(TI);
+  constexpr int64_t TILE = (int64_t)SEG_COMPUTE * IPT * VEC;
+  constexpr size_t IN_BYTES = (size_t)SEG_COMPUTE * IPT * 16;
+  constexpr size_t STAGE_BYTES = (IN_BYTES + TILE / 8 + 16 + 127) / 128 * 128;
+  constexpr size_t OUT_BYTES = (FAST && MODE != M_REDUCE) ? IN_BYTES * (sizeof(TO) / sizeof(TI)) : 0;
+  const size_t dyn = STG * STAGE_BYTES + OUT_BYTES;
   const int64_t nt = (n + TILE - 1) / TILE;
-  const int64_t ntiles = nt > 0 ? nt : 1;  // one tile still writes empty-segment identities
-  if (ntiles >= (int64_t)0x7FFFFFFF) return GBK_ERR_INVALID_ARGUMENT;
+  const int64_t ntiles = nt > 0 ? nt : 1;  // one tile still runs phase 0 (empty-segment identities)
+  if (ntiles >= ((int64_t)1 << 31)) return GBK_ERR_INVALID_ARGUMENT;
   int st = GBK_OK;
-  const size_t vb = ((size_t)ntiles * sizeof(TO) + 255) / 256 * 256;
-  char* scr = ws_scratch(w, 2 * vb, &st);
+  const size_t bm_bytes = (((size_t)(ntiles + 1) * (TILE / 32) + 4) * 4 + 255) / 256 * 256;
+  const size_t lo_bytes = ((size_t)(ntiles + 1) * 8 + 255) / 256 * 256;
+  char* scr = ws_scratch(w, bm_bytes + lo_bytes, &st);
   if (!scr) return st;
-  SegState<TO> S;
-  unsigned ep = 0;
-  S.flags = ws_flags(w, (size_t)ntiles, &ep, &st);
-  if (!S.flags) return st;
-  S.epoch = ep;
-  S.agg = (TO*)scr;
-  S.incl = (TO*)(scr + vb);
-  S.ticket = w->counters + SLOT_SEG;
+  LbState S;
+  S.desc = (TileDesc*)ws_flags(w, lb_flag_words(ntiles), &S.epoch, &st);
+  if (!S.desc) return st;
   S.err = w->err;
   S.ntiles = ntiles;
   S.wait_limit = wait_limit();
-  const bool aligned = ((uintptr_t)x % 16 == 0) && (MODE == M_REDUCE || (uintptr_t)y % 16 == 0);
-  if (aligned)
-    k_segmented<TI, TO, OP, MODE, true, BLOCK, IPT><<<(unsigned)ntiles, BLOCK, 0, s>>>(x, y, n, offsets, nseg, S);
-  else
-    k_segmented<TI, TO, OP, MODE, false, BLOCK, IPT><<<(unsigned)ntiles, BLOCK, 0, s>>>(x, y, n, offsets, nseg, S);
+  SegArgs A;
+  A.offsets = offsets;
+  A.nseg = nseg;
+  A.bitmap = (unsigned*)scr;
+  A.tile_lo = (int64_t*)(scr + bm_bytes);
+  A.arrive = w->counters + SLOT_SEG;
+  A.depart = w->counters + SLOT_SEG + 1;
+  auto kfn = k_seg<TI, TO, OP, MODE, FAST, IPT, STG>;
+  static int resident = 0;  // CTAs per SM, per instantiation
+  if (!resident) {
+    GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    int r = 0;
+    GBK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kfn, SEG_BLOCK, dyn));
+    if (r < 1) return GBK_ERR_UNSUPPORTED;
+    resident = r;
+  }
+  const int per_sm = cps > 0 && cps < resident ? cps : resident;
+  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)per_sm * sm_count());
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(SEG_BLOCK);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = w->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  GBK_CUDA_TRY(cudaLaunchKernelEx(&cfg, kfn, x, y, n, A, S));
   note_launch();
-  return cuda_status(cudaGetLastError());
+  return GBK_OK;
 }
 
-// items_per_thread (16-byte vectors per thread per tile): 2, 4 (default), 8.
+// items_per_thread (16-byte vectors per thread per tile): 7 (default) or 3.
 template <class TI, class TO, int OP, int MODE>
 int launch_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t nseg, Workspace* w,
                const gbk_tuning_t* t) {
-  const int ipt = t && t->items_per_thread ? t->items_per_thread : 4;
-  if (ipt == 2) return launch_seg_ipt<TI, TO, OP, MODE, 2>(x, y, n, offsets, nseg, w);
-  if (ipt == 8) return launch_seg_ipt<TI, TO, OP, MODE, 8>(x, y, n, offsets, nseg, w);
-  return launch_seg_ipt<TI, TO, OP, MODE, 4>(x, y, n, offsets, nseg, w);
+  const int want = t && t->items_per_thread > 0 ? t->items_per_thread : 7;
+  const int cps = t ? t->ctas_per_sm : 0;
+  const bool fast = (uintptr_t)x % 16 == 0 && (MODE == M_REDUCE || (uintptr_t)y % 16 == 0);
+  // Reduce has no out tile: a 3-deep ring keeps more of its input in flight
+  // (still two CTAs per SM; four stages of 7-vector tiles would allow one).
+  constexpr int STG = MODE == M_REDUCE ? 3 : 2;
+  if (!fast) return launch_k_seg<TI, TO, OP, MODE, false, 7, STG>(x, y, n, offsets, nseg, w, cps);
+  if (want <= 4) return launch_k_seg<TI, TO, OP, MODE, true, 3, STG>(x, y, n, offsets, nseg, w, cps);
+  return launch_k_seg<TI, TO, OP, MODE, true, 7, STG>(x, y, n, offsets, nseg, w, cps);
 }
 
 template <class T>
@@ -448,3 +588,4 @@ int gbk_segmented_scan(int inclusive, gbk_dtype_t din, gbk_dtype_t dout, const v
 }
 
 }  // extern "C"
+

@@ -29,7 +29,7 @@ KIND_REDUCE, KIND_SCAN, KIND_HIST, KIND_SEG = 0, 1, 2, 3
 REDUCE_CFGS = [(b, u, c) for (b, u) in [(256, 2), (256, 4), (256, 8), (512, 2), (512, 4), (128, 8), (1024, 2)]
                for c in (1, 2, 4, 8)]
 SCAN_CFGS = [(9, 0), (7, 0), (3, 0), (9, 1)]  # (vectors per thread, CTAs per SM; 0 = all resident)
-SEG_CFGS = [2, 4, 8]
+SEG_CFGS = [(7, 0), (3, 0), (7, 1)]  # (vectors per thread, CTAs per SM; 0 = all resident)
 # histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit, no privatisation
 HIST_CFGS_SMALL = [(0x01, 1), (0x01, 2), (0x11, 2), (0x20, 1), (0x30, 1), (0x40, 1)]
 HIST_CFGS_2E16 = [(0x02, 1), (0x12, 1), (0x04, 1), (0x20, 1), (0x30, 1), (0x40, 1)]
@@ -45,7 +45,7 @@ def candidates(w):
     if k == KIND_SCAN:
         return [{"block": 256, "ipt": u, "cps": c, "variant": 0} for (u, c) in SCAN_CFGS]
     if k == KIND_SEG:
-        return [{"block": 256, "ipt": u, "cps": 0, "variant": 0} for u in SEG_CFGS]
+        return [{"block": 256, "ipt": u, "cps": c, "variant": 0} for (u, c) in SEG_CFGS]
     cf = HIST_CFGS_2E16 if w["nbins"] > 24576 else HIST_CFGS_SMALL
     return [{"block": 0, "ipt": 0, "cps": c, "variant": v} for (v, c) in cf]
 
@@ -292,7 +292,7 @@ def default_cfg_index(w, cs):
             return i
         if k == KIND_SCAN and (c["ipt"], c["cps"]) == (9, 0):
             return i
-        if k == KIND_SEG and c["ipt"] == 4:
+        if k == KIND_SEG and (c["ipt"], c["cps"]) == (7, 0):
             return i
         if k == KIND_HIST:
             want = 0x20 if w["nbins"] > 24576 else 0x01

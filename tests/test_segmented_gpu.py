@@ -80,6 +80,74 @@ def test_segmented_vs_oracle(env, case):
     np.testing.assert_array_equal(y64.cpu().numpy(), inc - xi.astype(np.int64))
 
 
+@pytest.mark.parametrize("ipt,cps", [(7, 0), (7, 1), (3, 0), (3, 2)])
+def test_segmented_shapes(env, ipt, cps):
+    """Every tile shape of the persistent kernel (7 or 3 vectors per thread,
+    all-resident or fewer CTAs), with segment boundaries on the tile edges of
+    both shapes (7168 / 3072 elements for 4-byte types, 3584 / 1536 for
+    8-byte), empty segments next to them, and an unaligned input view."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    rng = np.random.default_rng(ipt * 10 + cps)
+    lens = np.concatenate([[7168, 7168, 0, 1, 7167, 3584, 3584, 0, 0, 3072, 1536, 5, 14336, 6144],
+                           rng.integers(0, 40, 400), [100000], rng.integers(0, 9000, 60)]).astype(np.int64)
+    offs = datagen.offsets_from_lengths(lens)
+    n = int(offs[-1])
+    nseg = lens.size
+    do = _dev(torch, offs)
+    tune = (256, ipt, cps, 0)
+    xi = datagen.uniform_i32(n + 1, 0, 255, seed=7)
+    xl = datagen.uniform_i64(n, -1000, 1000, seed=8)
+    for name, x in (("aligned", _dev(torch, xi[:n])), ("unaligned", _dev(torch, xi)[1:])):
+        xh = xi[:n] if name == "aligned" else xi[1:]
+        for op in ("sum", "min", "max"):
+            o = torch.empty(nseg, dtype=torch.int32, device="cuda")
+            gbk.segmented_reduce(op, x, do, o, tune=tune)
+            gbk.stream_check()
+            f = {"sum": np.sum, "min": np.min, "max": np.max}[op]
+            ident = {"sum": 0, "min": 2**31 - 1, "max": -2**31}[op]
+            w = np.array([f(xh[offs[s]:offs[s + 1]]) if lens[s] else ident for s in range(nseg)],
+                         dtype=np.int64).astype(np.int32)
+            np.testing.assert_array_equal(o.cpu().numpy(), w, err_msg=f"{name} {op}")
+        y = torch.empty(n, dtype=torch.int32, device="cuda")
+        gbk.segmented_scan(x, do, y, inclusive=True, tune=tune)
+        gbk.stream_check()
+        inc = oracle.seg_inclusive_scan_i32(np.ascontiguousarray(xh), offs, 4)
+        np.testing.assert_array_equal(y.cpu().numpy(), inc, err_msg=name)
+        y64 = torch.empty(n, dtype=torch.int64, device="cuda")
+        gbk.segmented_scan(x, do, y64, inclusive=False, tune=tune)
+        gbk.stream_check()
+        np.testing.assert_array_equal(y64.cpu().numpy(), inc.astype(np.int64) - xh.astype(np.int64), err_msg=name)
+    # 8-byte elements: tile edges at 3584 / 1536
+    o = torch.empty(nseg, dtype=torch.int64, device="cuda")
+    gbk.segmented_reduce("sum", _dev(torch, xl), do, o, tune=tune)
+    gbk.stream_check()
+    w = np.array([xl[offs[s]:offs[s + 1]].sum() for s in range(nseg)], dtype=np.int64)
+    np.testing.assert_array_equal(o.cpu().numpy(), w)
+    yl = torch.empty(n, dtype=torch.int64, device="cuda")
+    gbk.segmented_scan(_dev(torch, xl), do, yl, inclusive=True, tune=tune)
+    gbk.stream_check()
+    cs = np.cumsum(xl)
+    base = np.repeat(np.concatenate([[0], cs[offs[1:-1] - 1]]), lens) if n else cs
+    np.testing.assert_array_equal(yl.cpu().numpy(), cs - base)
+
+
+def test_segmented_all_empty(env):
+    """n = 0 with segments: every segment is empty and gets the identity."""
+    gbk, torch = env
+    offs = np.zeros(9, dtype=np.int64)
+    x = torch.empty(0, dtype=torch.float32, device="cuda")
+    o = torch.full((8,), 5.0, dtype=torch.float32, device="cuda")
+    gbk.segmented_reduce("sum", x, _dev(torch, offs), o)
+    gbk.stream_check()
+    assert o.cpu().numpy().tolist() == [0.0] * 8
+    om = torch.zeros(8, dtype=torch.float32, device="cuda")
+    gbk.segmented_reduce("max", x, _dev(torch, offs), om)
+    gbk.stream_check()
+    assert np.all(om.cpu().numpy() == np.float32(-3.402823466e38))
+
+
 def test_golden_team_reduce(env):
     """TeamPolicy league of per-segment sums (reference TeamThreadRange
     reduce) — the batched reduce gives the same sums within 1e-12."""
