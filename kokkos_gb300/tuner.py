@@ -126,6 +126,8 @@ class Bench:
         self.bins = torch.zeros(65536, dtype=torch.int64, device="cuda")
         self._ent = {}
         self.seg_cache = {}
+        # Written before every timed call: inputs start cold in L2, as in the bench.
+        self.flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def entropy(self, pool, nbins):
         key = (pool, nbins)
@@ -181,6 +183,8 @@ class Bench:
         if st:
             return float("inf")
         for r in range(reps):
+            with torch.cuda.stream(self.s):
+                self.flush.fill_(r & 255)
             e[2 * r].record(self.s)
             self.call(w, c)
             e[2 * r + 1].record(self.s)
@@ -342,28 +346,62 @@ def evaluate(model, rows):
     }
 
 
-def table_from_model(model, path):
-    """Tuning table over a grid of workload buckets, from the MLP's choices."""
-    lines = ["# kind op dtype log2n extra block items_per_thread ctas_per_sm variant"]
+def grid_workloads():
+    """The workload buckets of the tuning table (kind, op, dtype, log2 n, extra)."""
+    out = []
     for l2 in range(16, 29):
         for op, dt in REDUCE_OPS:
-            w = {"kind": KIND_REDUCE, "op": OPC[op], "dtype": dt, "n": 1 << l2}
-            cs = candidates(w)
-            c = cs[int(np.argmin(model.predict(np.stack([features(w, c) for c in cs]))))]
-            lines.append(f"0 {OPC[op]} {dt} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0")
+            if dt in (1, 5) and l2 > 27:
+                continue
+            out.append({"kind": KIND_REDUCE, "op": OPC[op], "opname": op, "dtype": dt, "n": 1 << l2,
+                        "inner_extent": 1})
         for inc in (0, 1):
-            w = {"kind": KIND_SCAN, "op": inc, "dtype": 0, "n": 1 << l2}
-            cs = candidates(w)
-            c = cs[int(np.argmin(model.predict(np.stack([features(w, c) for c in cs]))))]
-            lines.append(f"1 {inc} {0 * 8 + 1} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0")
-        for nb in (256, 4096, 65536):
-            w = {"kind": KIND_HIST, "op": 0, "dtype": 0, "n": 1 << l2, "nbins": nb, "entropy_bits": 10.0}
-            cs = candidates(w)
-            c = cs[int(np.argmin(model.predict(np.stack([features(w, c) for c in cs]))))]
-            lines.append(f"2 0 0 {l2} {int(math.log2(nb)) * 8} 0 0 {c['cps']} {c['variant']}")
+            out.append({"kind": KIND_SCAN, "op": inc, "dtype": 0, "n": 1 << l2})
+        if l2 <= 26:
+            for nb in (256, 4096, 65536):
+                out.append({"kind": KIND_HIST, "op": 0, "dtype": 0, "n": 1 << l2, "nbins": nb, "pool": 3})
+    return out
+
+
+def table_line(w, c):
+    l2 = int(round(math.log2(w["n"])))
+    if w["kind"] == KIND_REDUCE:
+        return f"0 {w['op']} {w['dtype']} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0"
+    if w["kind"] == KIND_SCAN:
+        return f"1 {w['op']} {0 * 8 + 1} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0"
+    return f"2 0 0 {l2} {int(math.log2(w['nbins'])) * 8} 0 0 {c['cps']} {c['variant']}"
+
+
+HEADER = "# kind op dtype log2n extra block items_per_thread ctas_per_sm variant"
+
+
+def table_exhaustive(grid_rows, path):
+    """Tuning table from the exhaustive autotuner: the fastest measured
+    candidate of every bucket."""
+    lines = [HEADER]
+    for (w, cs, ts) in grid_rows:
+        if np.isfinite(ts).any():
+            lines.append(table_line(w, cs[int(np.nanargmin(np.where(np.isfinite(ts), ts, np.nan)))]))
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
     return path
+
+
+def table_from_model(model, grid_rows, path):
+    """Tuning table from the MLP's choices on the same buckets, and the
+    throughput of those choices relative to the bucket's exhaustive best."""
+    lines = [HEADER]
+    ratios = []
+    for (w, cs, ts) in grid_rows:
+        ts = np.array(ts)
+        p = model.predict(np.stack([features(w, c) for c in cs]))
+        i = int(np.argmin(p))
+        lines.append(table_line(w, cs[i]))
+        if np.isfinite(ts).any() and np.isfinite(ts[i]):
+            ratios.append(float(ts[np.isfinite(ts)].min() / ts[i]))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return float(np.mean(ratios)) if ratios else float("nan")
 
 
 def main():
@@ -390,7 +428,10 @@ def main():
     rep = evaluate(model, eval_rows)
     rep.update({"train_timings": int(X.shape[0]), "eval_timings": int(sum(len(r[2]) for r in eval_rows)),
                 "collect_s": round(t_collect, 1), "train_s": round(t_train, 1), "loss_history": hist[::4] + hist[-1:]})
-    table_from_model(model, os.path.join(args.out, "tuning_table.txt"))
+    grid_rows = collect(grid_workloads(), bench, log_every=0)
+    table_exhaustive(grid_rows, os.path.join(args.out, "tuning_table.txt"))
+    rep["grid_buckets"] = len(grid_rows)
+    rep["mlp_grid_throughput_vs_best"] = table_from_model(model, grid_rows, os.path.join(args.out, "mlp_table.txt"))
     np.save(os.path.join(args.out, "mlp_params.npy"), model.params.cpu().numpy())
     with open(os.path.join(args.out, "tuner_eval.json"), "w") as f:
         json.dump(rep, f, indent=1)

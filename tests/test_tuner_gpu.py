@@ -30,10 +30,15 @@ def test_small_pipeline_and_table():
     assert rep["workloads"] == 40
     assert 0.0 < rep["default_mean_throughput_vs_best"] <= 1.0
     assert rep["mlp_mean_throughput_vs_best"] > 0.7
+    grid = tuner.collect(tuner.grid_workloads(), bench, log_every=0)
     with tempfile.TemporaryDirectory() as d:
-        path = tuner.table_from_model(m, os.path.join(d, "t.txt"))
+        ratio = tuner.table_from_model(m, grid, os.path.join(d, "mlp.txt"))
+        assert 0.0 < ratio <= 1.0
+        assert gbk.lib.gbk_tuner_load(os.path.join(d, "mlp.txt").encode()) == 0
+        path = tuner.table_exhaustive(grid, os.path.join(d, "t.txt"))
         assert gbk.lib.gbk_tuner_load(path.encode()) == 0
-    assert gbk.lib.gbk_tuner_size() > 100
+    # (sizes above the small bench's 2^22 fold into fewer buckets)
+    assert gbk.lib.gbk_tuner_size() >= 50
     gbk.lib.gbk_tuner_enable(1)
     try:
         # entry points called without a configuration now use the table;
