@@ -12,8 +12,8 @@ ScatterView workload:
 268 MB, larger than the 129 MB L2, so no flush is needed).  `e2e` times the
 same step through the C ABI from pinned HOST buffers: deep_copy of the view
 and the keys to the device, the four operations, and the results copied
-back, every step.  `roofline` is the dominant kernel (the flat reduce
-kernel the contiguous MDRange box collapses to).  `cpu_baseline` is the
+back, every step.  `roofline` is the dominant kernel (the flat ring reduce
+the contiguous MDRange box collapses to).  `cpu_baseline` is the
 oracle (CPU restatement of the reference OpenMP algorithms) on this host.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbk|reference]
@@ -44,6 +44,11 @@ NBINS = 1 << 16
 RED_BYTES = NX * 4
 HIST_BYTES = NKEYS * 4 + NBINS * 8
 STEP_BYTES = 3 * RED_BYTES + HIST_BYTES
+# The dominant kernel and its DRAM traffic per launch (dram__bytes_read.sum +
+# dram__bytes_write.sum from one ncu capture of the same launch, as recorded
+# in profiles/).
+ROOF_KERNEL = "k_reduce_tma (MinLoc/MaxLoc/Sum f32, shared-memory ring)"
+ROOF_TRAFFIC = None
 WORKLOAD = ("MDRange<Rank<3>> MinLoc+MaxLoc+Sum over LayoutLeft View<float***> 512x512x256 N(0,1) "
             "+ ScatterView histogram 2^26 int32 Zipf(1.1) keys -> 2^16 int64 bins")
 
@@ -371,10 +376,10 @@ def main():
         "config": {"workload": WORKLOAD, "step_bytes": STEP_BYTES, "l2": "inputs 268 MB each > 129 MB L2; no flush",
                    "parallelism": f"replicas x{world}",
                    "launch_config": "autotuner table" if tuned else "library defaults"},
-        "roofline": {"bound": "hbm", "kernel": "k_reduce_flat (MinLoc/MaxLoc/Sum f32)",
+        "roofline": {"bound": "hbm", "kernel": ROOF_KERNEL,
                      "achieved": round(red_gbs, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(red_gbs / hbm, 4), "peak_kind": peak_kind + " hbm_gbs (burst copy)",
-                     "traffic": None},
+                     "traffic": ROOF_TRAFFIC},
         "ops": per_op,
         "e2e": {"value": round(e2e_val, 1), "unit": "GB/s", "ms_per_step": round(e_ms, 3),
                 "h2d_bytes_per_step": NX * 4 + NKEYS * 4, "d2h_bytes_per_step": 192 + NBINS * 8},

@@ -125,6 +125,85 @@ __global__ void __launch_bounds__(BLOCK)
   grid_finish<R, BLOCK>(acc, partials, counter, out, sm);
 }
 
+// Flat reduce through a shared-memory ring (TMA engine): each CTA owns one
+// contiguous, equal share of the whole vectors and streams it in chunks of
+// CV 16-byte vectors by 1-D bulk copies into STAGES stages (mbarrier
+// completion), so STAGES - 1 chunks per CTA are in flight while the threads
+// fold the current one from shared memory (vector k * BLOCK + tid: striped,
+// conflict-free, and increasing per thread, as the ordered *Loc updates
+// want).  Head and tail elements and the grid finish are those of the flat
+// kernel.  x + head must be 16-byte aligned (it is, by construction of head).
+template <class R, class T, int BLOCK, int CV, int STAGES>
+__global__ void __launch_bounds__(BLOCK)
+    k_reduce_tma(const T* __restrict__ x, int64_t n, int64_t head, int64_t loc0, typename R::V* partials,
+                 unsigned* counter, typename R::V* out, int* err, int64_t wait_limit) {
+  using V = typename R::V;
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr unsigned CHUNK_BYTES = (unsigned)CV * 16;
+  static_assert(CV % BLOCK == 0, "whole rows of vectors per chunk");
+  extern __shared__ __align__(128) unsigned char ring[];
+  __shared__ __align__(8) unsigned long long s_bar[STAGES];
+  __shared__ V sm[BLOCK / 32];
+  V acc = R::init();
+  const int64_t gtid = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (gtid < head) R::template update<true>(acc, x[gtid], loc0 + gtid);
+  const T* xb = x + head;
+  const int64_t nvec = (n - head) / VEC;
+  const int64_t lb = loc0 + head;
+  const int64_t per = nvec / gridDim.x, rem = nvec % gridDim.x;
+  const int64_t v0 = (int64_t)blockIdx.x * per + ((int64_t)blockIdx.x < rem ? blockIdx.x : rem);
+  const int64_t v1 = v0 + per + ((int64_t)blockIdx.x < rem ? 1 : 0);
+  const int64_t nchunks = (v1 - v0 + CV - 1) / CV;
+  // Thread 0 only: start the copy of chunk c into its stage.
+  auto fill = [&](int64_t c) {
+    if (c >= nchunks) return;
+    const int s = (int)(c % STAGES);
+    const int64_t c0 = v0 + c * CV;
+    const int64_t cnt = v1 - c0 < CV ? v1 - c0 : CV;
+    mbar_arrive_expect_tx(&s_bar[s], (unsigned)(cnt * 16));
+    bulk_g2s(ring + (size_t)s * CHUNK_BYTES, xb + c0 * VEC, (unsigned)(cnt * 16), &s_bar[s]);
+  };
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < STAGES; ++s) mbar_init(&s_bar[s], 1);
+    fence_mbar_init();
+    for (int s = 0; s < STAGES; ++s) fill(s);
+  }
+  __syncthreads();
+  bool bad = false;
+  for (int64_t c = 0; c < nchunks; ++c) {
+    const int s = (int)(c % STAGES);
+    if (!mbar_wait(&s_bar[s], (unsigned)(c / STAGES) & 1u, wait_limit)) bad = true;
+    const int64_t c0 = v0 + c * CV;
+    const int cnt = (int)(v1 - c0 < CV ? v1 - c0 : CV);
+    const uint4* sv = reinterpret_cast<const uint4*>(ring + (size_t)s * CHUNK_BYTES);
+    if (cnt == CV) {
+#pragma unroll
+      for (int k = 0; k < CV / BLOCK; ++k) {
+        Vec16<T> u;
+        u.u = sv[k * BLOCK + threadIdx.x];
+        const int64_t e0 = lb + (c0 + k * BLOCK + threadIdx.x) * VEC;
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) R::template update<true>(acc, u.v[q], e0 + q);
+      }
+    } else {
+      for (int i = threadIdx.x; i < cnt; i += BLOCK) {
+        Vec16<T> u;
+        u.u = sv[i];
+        const int64_t e0 = lb + (c0 + i) * VEC;
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) R::template update<true>(acc, u.v[q], e0 + q);
+      }
+    }
+    __syncthreads();  // stage s fully read: refill it
+    if (threadIdx.x == 0) fill(c + STAGES);
+  }
+  const int64_t t0 = head + nvec * VEC;
+  if (t0 + gtid < n) R::template update<true>(acc, x[t0 + gtid], loc0 + t0 + gtid);
+  if (bad) atomicOr(err, GBK_EBIT_TIMEOUT);
+  grid_finish<R, BLOCK>(acc, partials, counter, out, sm);
+}
+
 template <class R>
 __global__ void k_write_identity(typename R::V* out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *out = R::init();
@@ -194,8 +273,51 @@ int launch_flat(const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, in
   return cuda_status(cudaGetLastError());
 }
 
+// Ring reduce: 256 threads, chunks of 1024 vectors (16 KiB), 4 stages: three
+// CTAs per SM keep about 144 KiB per SM in flight.
+template <class R, class T>
+int launch_tma(const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, int cps) {
+  using V = typename R::V;
+  constexpr int BLOCK = 256, CV = 1024, STAGES = 4;
+  constexpr int VEC = 16 / sizeof(T);
+  cudaStream_t s = w->stream;
+  const uintptr_t a = (uintptr_t)x;
+  int64_t head = (int64_t)(((16 - (a & 15)) & 15) / sizeof(T));
+  if (head > n) head = n;
+  const int64_t nvec = (n - head) / VEC;
+  auto kfn = k_reduce_tma<R, T, BLOCK, CV, STAGES>;
+  constexpr size_t dyn = (size_t)STAGES * CV * 16;
+  static int resident = 0;  // CTAs per SM, per instantiation
+  if (!resident) {
+    GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    int r = 0;
+    GBK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kfn, BLOCK, dyn));
+    resident = r > 0 ? r : 1;
+  }
+  const int per_sm = cps > 0 && cps < resident ? cps : resident;
+  int64_t grid = (int64_t)sm_count() * per_sm;
+  const int64_t chunks = (nvec + CV - 1) / CV;
+  if (grid > chunks) grid = chunks;
+  if (grid < 1) grid = 1;
+  const int64_t tail = (n - head) - nvec * VEC;
+  while (grid * BLOCK < head || grid * BLOCK < tail) ++grid;
+  int st = GBK_OK;
+  char* scr = ws_scratch(w, sizeof(V) * (size_t)grid + 256, &st);
+  if (!scr) return st;
+  kfn<<<(unsigned)grid, BLOCK, dyn, s>>>(x, n, head, loc0, (V*)scr, w->counters + SLOT_REDUCE, (V*)out, w->err,
+                                        wait_limit());
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+// variant 1: the load-pipelined kernel (block, items_per_thread, ctas_per_sm
+// from the tuning); variant 2: the ring kernel (ctas_per_sm); variant 0: the
+// ring kernel for inputs of 4 MiB and more, else the load-pipelined one.
 template <class R, class T>
 int launch_flat_cfg(const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, const gbk_tuning_t* t) {
+  const int variant = t ? t->variant : 0;
+  if (n > 0 && (variant == 2 || (variant == 0 && n * (int64_t)sizeof(T) >= ((int64_t)4 << 20))))
+    return launch_tma<R, T>(x, n, loc0, out, w, variant == 2 && t ? t->ctas_per_sm : 0);
   const int blk = t && t->block ? t->block : 256;
   const int un = t && t->items_per_thread ? t->items_per_thread : 4;
   const int cps = t && t->ctas_per_sm ? t->ctas_per_sm : (blk >= 512 ? 4 : 8);

@@ -111,7 +111,10 @@ __global__ void __launch_bounds__(BLOCK)
 }
 
 // One CTA per SM holding every bin as a 16-bit counter (two per 32-bit
-// word, 2^16 bins in 128 KiB).  The CTA walks its contiguous share of the
+// word, 2^16 bins in 128 KiB).  Word i holds bins i (low half) and
+// i + nwords (high half): bins next to each other land in different words,
+// so the few hot bins of a skewed key distribution (Zipf: bins 0, 1, 2, ...)
+// do not also collide on one word with their neighbours.  The CTA walks its contiguous share of the
 // keys in rounds of BLOCK*8 keys; after every DRAIN rounds (at most 32768
 // keys, so no half-word can pass 0xFFFF from below 0x8000) all threads sync
 // and every half-word that reached 0x8000 gives 0x8000 to the global bin.
@@ -145,7 +148,10 @@ __global__ void __launch_bounds__(BLOCK, 1)
       leader = ok && ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1));
       add = __popc(peers);
     }
-    if (leader) atomicAdd(sh + (k >> 1), add << ((k & 1) * 16));
+    if (leader) {
+      const bool hi = k >= nwords;
+      atomicAdd(sh + (hi ? k - nwords : k), add << (hi ? 16 : 0));
+    }
   };
   auto drain = [&]() {
     __syncthreads();
@@ -154,8 +160,8 @@ __global__ void __launch_bounds__(BLOCK, 1)
       const unsigned hi = w & 0x80008000u;
       if (hi) {
         sh[i] = w - hi;
-        if (hi & 0x8000u) red_add_u64(bins + 2 * i, 0x8000ull);
-        if (hi & 0x80000000u) red_add_u64(bins + 2 * i + 1, 0x8000ull);
+        if (hi & 0x8000u) red_add_u64(bins + i, 0x8000ull);
+        if (hi & 0x80000000u) red_add_u64(bins + nwords + i, 0x8000ull);
       }
     }
     __syncthreads();
@@ -194,8 +200,8 @@ __global__ void __launch_bounds__(BLOCK, 1)
   __syncthreads();
   for (int i = threadIdx.x; i < nwords; i += BLOCK) {
     const unsigned w = sh[i];
-    if (w & 0xFFFFu) red_add_u64(bins + 2 * i, (unsigned long long)(w & 0xFFFFu));
-    if ((w >> 16) && 2 * i + 1 < nbins) red_add_u64(bins + 2 * i + 1, (unsigned long long)(w >> 16));
+    if (w & 0xFFFFu) red_add_u64(bins + i, (unsigned long long)(w & 0xFFFFu));
+    if ((w >> 16) && nwords + i < nbins) red_add_u64(bins + nwords + i, (unsigned long long)(w >> 16));
   }
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, GBK_EBIT_KEY_RANGE);
 }

@@ -41,7 +41,9 @@ NFEAT = 24
 def candidates(w):
     k = w["kind"]
     if k == KIND_REDUCE:
-        return [{"block": b, "ipt": u, "cps": c, "variant": 0} for (b, u, c) in REDUCE_CFGS]
+        # variant 1: load-pipelined kernel; variant 2: shared-memory ring kernel
+        return [{"block": b, "ipt": u, "cps": c, "variant": 1} for (b, u, c) in REDUCE_CFGS] + \
+               [{"block": 256, "ipt": 4, "cps": c, "variant": 2} for c in (0, 2)]
     if k == KIND_SCAN:
         return [{"block": 256, "ipt": u, "cps": c, "variant": 0} for (u, c) in SCAN_CFGS]
     if k == KIND_SEG:
@@ -66,7 +68,8 @@ def features(w, c):
     f[18] = (math.log2(max(c["ipt"], 1)) - 2.0) / 1.5
     f[19] = (math.log2(max(c["cps"], 1)) - 2.0) / 2.0
     v = c["variant"]
-    f[20] = float((v & 0xF) > 1) if v and not (v & 0x60) else 0.0   # cluster-split bins
+    # histogram: cluster-split bins; reduce: the ring kernel (variant 2)
+    f[20] = float((v & 0xF) > 1) if v and not (v & 0x60) else 0.0
     f[21] = float((v & 0x10) != 0)                       # warp aggregation
     f[22] = float((v & 0x20) != 0)                       # 16-bit bins
     f[23] = float((v & 0x40) != 0)                       # no privatisation
@@ -292,8 +295,11 @@ def default_cfg_index(w, cs):
     """The configuration the library uses without tuning."""
     k = w["kind"]
     for i, c in enumerate(cs):
-        if k == KIND_REDUCE and (c["block"], c["ipt"], c["cps"]) == (256, 4, 8):
-            return i
+        if k == KIND_REDUCE:
+            size = {5: 8, 1: 8, 3: 8}.get(w["dtype"], 4) * w["n"]
+            if (size >= (4 << 20) and c["variant"] == 2 and c["cps"] == 0) or \
+                    (size < (4 << 20) and c["variant"] == 1 and (c["block"], c["ipt"], c["cps"]) == (256, 4, 8)):
+                return i
         if k == KIND_SCAN and (c["ipt"], c["cps"]) == (9, 0):
             return i
         if k == KIND_SEG and (c["ipt"], c["cps"]) == (7, 0):
@@ -366,7 +372,7 @@ def grid_workloads():
 def table_line(w, c):
     l2 = int(round(math.log2(w["n"])))
     if w["kind"] == KIND_REDUCE:
-        return f"0 {w['op']} {w['dtype']} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0"
+        return f"0 {w['op']} {w['dtype']} {l2} 0 {c['block']} {c['ipt']} {c['cps']} {c['variant']}"
     if w["kind"] == KIND_SCAN:
         return f"1 {w['op']} {0 * 8 + 1} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0"
     return f"2 0 0 {l2} {int(math.log2(w['nbins'])) * 8} 0 0 {c['cps']} {c['variant']}"
@@ -380,6 +386,7 @@ def table_exhaustive(grid_rows, path):
     candidate of every bucket."""
     lines = [HEADER]
     for (w, cs, ts) in grid_rows:
+        ts = np.array(ts)
         if np.isfinite(ts).any():
             lines.append(table_line(w, cs[int(np.nanargmin(np.where(np.isfinite(ts), ts, np.nan)))]))
     with open(path, "w") as f:
