@@ -48,7 +48,7 @@ STEP_BYTES = 3 * RED_BYTES + HIST_BYTES
 # dram__bytes_write.sum from one ncu capture of the same launch, as recorded
 # in profiles/).
 ROOF_KERNEL = "k_reduce_tma (MinLoc/MaxLoc/Sum f32, shared-memory ring)"
-ROOF_TRAFFIC = None
+ROOF_TRAFFIC = 271834880  # MinLoc f32 over the box: 268.48 MB read + 3.36 MB written
 WORKLOAD = ("MDRange<Rank<3>> MinLoc+MaxLoc+Sum over LayoutLeft View<float***> 512x512x256 N(0,1) "
             "+ ScatterView histogram 2^26 int32 Zipf(1.1) keys -> 2^16 int64 bins")
 
