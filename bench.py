@@ -92,6 +92,12 @@ def barrier(dist):
         dist.barrier()
 
 
+def job_gbs(world, steps, ms_total):
+    """Whole-job throughput of independent replicas: every rank processes
+    STEP_BYTES per step, the job takes the slowest rank's time."""
+    return world * STEP_BYTES * steps / (ms_total / 1e3) / 1e9
+
+
 class Clocks:
     """nvidia-smi sampler running during the timed region."""
 
@@ -325,7 +331,7 @@ def main():
     ms_total = t_start.elapsed_time(t_end)
     ms_total = max_over_ranks(dist, ms_total)
     ms_step = ms_total / args.steps
-    value = world * STEP_BYTES * args.steps / (ms_total / 1e3) / 1e9
+    value = job_gbs(world, args.steps, ms_total)
 
     per_op = {}
     hbm, peak_kind = peaks()
@@ -359,7 +365,7 @@ def main():
         e2e_step()
     e_ms = (time.perf_counter() - e0) * 1e3 / e2e_steps
     e_ms = max_over_ranks(dist, e_ms)
-    e2e_val = world * STEP_BYTES / (e_ms / 1e3) / 1e9
+    e2e_val = job_gbs(world, 1, e_ms)
     gbk.stream_check(stream)
 
     # correctness spot check of the last step's results (rank-local, cheap)
