@@ -1,7 +1,6 @@
-// Stable LSD radix sort (onesweep: Adinets & Merrill, "Onesweep: A Faster
-// Least Significant Digit Radix Sort for GPUs", 2022), sort_by_key and
-// BinSort.  Replaces Kokkos::sort / Experimental::sort_by_key on a device
-// space (algorithms/src/sorting/Kokkos_SortPublicAPI.hpp:31-196,
+// Stable LSD radix sort, sort_by_key and BinSort.  Replaces Kokkos::sort /
+// Experimental::sort_by_key on a device space
+// (algorithms/src/sorting/Kokkos_SortPublicAPI.hpp:31-196,
 // Kokkos_SortByKeyPublicAPI.hpp:30-114; the reference CUDA path calls
 // thrust::sort / thrust::sort_by_key, impl/Kokkos_SortImpl.hpp:204-219,
 // impl/Kokkos_SortByKeyImpl.hpp:125-138) and BinSort
@@ -12,20 +11,25 @@
 // the sign bit flipped otherwise (so -0.0 sorts before +0.0).  Keys are
 // moved with their original bits.
 //
-// 1. k_digit_hist: one read of the keys builds the 256-bin histogram of every
-//    8-bit digit position (shared-memory counters, a warp that sees one digit
-//    in all lanes adds once).  The host reads the KB*256 counts back (one
-//    16 KiB copy and a stream sync per sort) and skips every pass whose digit
-//    is the same for all keys.
-// 2. k_onesweep (one launch per remaining pass): tiles of BLOCK*KPT keys in
-//    ticket order.  Each warp ranks its keys row by row with eight ballots
-//    per row (lanes holding the same digit), keeping per-warp digit counters
-//    in shared memory, so the rank of a key is its position among equal
-//    digits: the pass is stable.  The tile's 256 digit counts are published
-//    for a per-digit decoupled look-back (one status word per tile and
-//    digit: 2 flag bits + 30 count bits, single-copy atomic), giving each
-//    digit's global start; the tile is reordered by digit in shared memory
-//    and written out in runs.  Waits are bounded.
+// The array is cut into G chunks of whole tiles (G <= 2 x the SM count, two
+// scatter CTAs per SM); chunk c belongs to CTA c of every scatter launch.
+// 1. k_digit_hist: one read of the keys counts every 8-bit digit position,
+//    for the whole array and per chunk.  The host reads the whole-array
+//    counts back (one 16 KiB copy and a stream sync per sort) and skips each
+//    pass whose digit is the same for all keys.
+// 2. Per remaining 8-bit pass:
+//    k_chunk_count (all passes but the first, whose counts come from step 1):
+//      per-chunk counts of the pass's digit; keys stream through a
+//      shared-memory ring filled by bulk copies.
+//    k_chunk_scatter: one persistent CTA per chunk.  Its running offset for
+//      digit d starts at d's global start plus d's counts in all earlier
+//      chunks.  It walks its tiles in order with bulk copies running
+//      STAGES tiles ahead, ranks each tile with warp ballots (stable: slot
+//      order = input order), reorders the tile by digit in place in shared
+//      memory and writes the runs of equal digits at the running offsets.
+//    No CTA waits for another: a pass costs one extra read of the keys (the
+//    counts) instead of an inter-tile look-back, whose walk grows with the
+//    number of tiles in flight.
 #include <algorithm>
 #include <vector>
 
@@ -33,11 +37,6 @@
 
 namespace gbk {
 namespace {
-
-constexpr unsigned SF_A = 1u << 30;  // aggregate
-constexpr unsigned SF_P = 2u << 30;  // inclusive prefix
-constexpr unsigned SF_MASK = 3u << 30;
-constexpr unsigned SV_MASK = (1u << 30) - 1;
 
 // radix images
 template <int DT> struct Radix;
@@ -56,240 +55,474 @@ template <> struct Radix<GBK_F64> {
   }
 };
 
-template <int DT, int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
-    k_digit_hist(const typename Radix<DT>::K* __restrict__ keys, int64_t n, unsigned long long* __restrict__ hist) {
-  using K = typename Radix<DT>::K;
-  constexpr int KB = sizeof(K);
-  __shared__ unsigned sh[KB * 256];
-  for (int i = threadIdx.x; i < KB * 256; i += BLOCK) sh[i] = 0u;
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  // Every warp runs the same trip count so the shuffles see all lanes.
-  const int64_t stride = (int64_t)gridDim.x * BLOCK;
-  const int64_t iters = (n + stride - 1) / stride;
-  for (int64_t it = 0; it < iters; ++it) {
-    const int64_t i = it * stride + (int64_t)blockIdx.x * BLOCK + threadIdx.x;
-    const bool ok = i < n;
-    const K img = ok ? Radix<DT>::img(keys[i]) : K(0);
-    const unsigned okm = __ballot_sync(0xffffffffu, ok);
-    if (!okm) continue;
-#pragma unroll
-    for (int p = 0; p < KB; ++p) {
-      const unsigned d = (unsigned)(img >> (8 * p)) & 255u;
-      const unsigned d0 = __shfl_sync(0xffffffffu, d, __ffs(okm) - 1);
-      const bool same = __all_sync(0xffffffffu, !ok || d == d0);
-      if (same) {
-        if (lane == __ffs(okm) - 1) atomicAdd(sh + p * 256 + d0, (unsigned)__popc(okm));
-      } else if (ok) {
-        atomicAdd(sh + p * 256 + d, 1u);
-      }
-    }
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < KB * 256; i += BLOCK)
-    if (sh[i]) atomicAdd(hist + i, (unsigned long long)sh[i]);
-}
-
 template <int VB> struct ValT;
 template <> struct ValT<0> { using T = char; };
 template <> struct ValT<4> { using T = uint32_t; };
 template <> struct ValT<8> { using T = uint64_t; };
 
-struct PassArgs {
-  unsigned* status;        // [ntiles][256]
-  const int64_t* offsets;  // [256] exclusive digit starts for this pass
-  unsigned* ticket;
+// Keys [lo, hi) of part `part` of chunk c when each chunk of `chunk_keys`
+// keys is split into `sub` parts starting on 4-key (16-byte) boundaries.
+__device__ __forceinline__ void chunk_part(int64_t n, int64_t chunk_keys, int c, int part, int sub, int64_t* lo,
+                                           int64_t* hi) {
+  const int64_t a = (int64_t)c * chunk_keys;
+  const int64_t b = a + chunk_keys < n ? a + chunk_keys : n;
+  const int64_t per = ((b - a + sub - 1) / sub + 3) & ~(int64_t)3;
+  const int64_t l = a + part * per;
+  *lo = l < b ? l : b;
+  *hi = *lo + per < b ? *lo + per : b;
+}
+
+// Lanes of the warp holding the same 8-bit digit d, within the lanes where
+// `ok` holds: eight ballots, one per digit bit.  No shared memory, and the
+// cost does not depend on how the digits repeat.
+__device__ __forceinline__ unsigned digit_peers(unsigned d, bool ok) {
+  unsigned m = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const unsigned v = __ballot_sync(0xffffffffu, bit);
+    m &= bit ? v : ~v;
+  }
+  return m;
+}
+
+// Stable rank of one row of 32 keys (one per lane) within a warp: the
+// warp's count of digit d before this row (cnt[d], per warp, shared) plus
+// the lanes below holding d.  The lowest lane of each digit group advances
+// cnt[d].
+__device__ __forceinline__ unsigned rank_row(unsigned short* cnt, unsigned d, bool ok, int lane) {
+  const unsigned m = digit_peers(d, ok);
+  const int leader = __ffs(m) - 1;
+  unsigned b = 0;
+  if (ok && lane == leader) {
+    b = cnt[d];
+    cnt[d] = (unsigned short)(b + (unsigned)__popc(m));
+  }
+  b = __shfl_sync(0xffffffffu, b, leader < 0 ? lane : leader);
+  __syncwarp();
+  return b + (unsigned)__popc(m & ((1u << lane) - 1u));
+}
+
+// After a wait that gave up: wait (bounded) for the bulk copies still in
+// flight into stages j in [from, to), so none lands after the CTA exits.
+__device__ __forceinline__ void drain_stages(unsigned long long* bars, int stages, int64_t from, int64_t to,
+                                             int64_t limit) {
+  for (int64_t j = from; j < to; ++j) mbar_wait(&bars[j % stages], (unsigned)(j / stages) & 1u, limit);
+}
+
+// ---- 1. all digit positions, whole array and per chunk ----------------------
+// hist[p*256 + d] (u64) and ccounts[(p*nchunks + c)*256 + d] (u32), both
+// zeroed by the caller.  Grid = nchunks * sub.
+template <int DT, int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    k_digit_hist(const typename Radix<DT>::K* __restrict__ keys, int64_t n, int64_t chunk_keys, int sub,
+                 int nchunks, unsigned long long* __restrict__ hist, unsigned* __restrict__ ccounts) {
+  using K = typename Radix<DT>::K;
+  constexpr int KB = sizeof(K);
+  constexpr int U = 4;  // keys per thread per step (loads in flight)
+  __shared__ unsigned sh[KB * 256];
+  for (int i = threadIdx.x; i < KB * 256; i += BLOCK) sh[i] = 0u;
+  __syncthreads();
+  const int c = blockIdx.x / sub;
+  int64_t lo, hi;
+  chunk_part(n, chunk_keys, c, blockIdx.x % sub, sub, &lo, &hi);
+  for (int64_t base = lo; base < hi; base += (int64_t)BLOCK * U) {
+    K img[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + u * BLOCK + threadIdx.x;
+      ok[u] = i < hi;
+      img[u] = ok[u] ? Radix<DT>::img(keys[i]) : K(0);
+    }
+    // Increments without a result: lanes of a warp on one counter are
+    // combined by the shared-memory atomic unit, so skewed keys stay fast.
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (ok[u]) {
+#pragma unroll
+        for (int p = 0; p < KB; ++p) atomicAdd(sh + p * 256 + ((unsigned)(img[u] >> (8 * p)) & 255u), 1u);
+      }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < KB * 256; i += BLOCK) {
+    const unsigned v = sh[i];
+    if (v) {
+      atomicAdd(hist + i, (unsigned long long)v);
+      atomicAdd(ccounts + ((int64_t)(i >> 8) * nchunks + c) * 256 + (i & 255), v);
+    }
+  }
+}
+
+// ---- 2a. per-chunk counts of one digit ----------------------------------------
+constexpr int CNT_BLOCK = 256;
+constexpr int CNT_STAGE_BYTES = 16384;
+constexpr int CNT_STAGES = 4;
+constexpr int CNT_SUB = 3;  // CTAs per chunk
+
+// counts[c*256 + d] (u32, zeroed by the caller).  Grid = nchunks * CNT_SUB.
+// TMA: keys 16-byte aligned, streamed through the ring; otherwise plain loads.
+template <int DT, bool TMA>
+__global__ void __launch_bounds__(CNT_BLOCK)
+    k_chunk_count(const typename Radix<DT>::K* __restrict__ keys, int64_t n, int64_t chunk_keys, int shift,
+                  unsigned* __restrict__ counts, int* err, int64_t wait_limit) {
+  using K = typename Radix<DT>::K;
+  constexpr int E = CNT_STAGE_BYTES / (int)sizeof(K);  // keys per stage
+  constexpr int WARPS = CNT_BLOCK / 32;
+  extern __shared__ __align__(128) unsigned char ring[];
+  __shared__ __align__(8) unsigned long long s_bar[CNT_STAGES];
+  __shared__ unsigned s_h[WARPS][256];
+  const int warp = threadIdx.x >> 5;
+  const int c = blockIdx.x / CNT_SUB;
+  int64_t lo, hi;
+  chunk_part(n, chunk_keys, c, blockIdx.x % CNT_SUB, CNT_SUB, &lo, &hi);
+  const int64_t nst = (hi - lo + E - 1) / E;
+  for (int i = threadIdx.x; i < WARPS * 256; i += CNT_BLOCK) (&s_h[0][0])[i] = 0u;
+  // Thread 0 only: start the copy of the whole 4-key groups of stage j.
+  auto fill = [&](int64_t j) {
+    if (j >= nst) return;
+    const int64_t s0 = lo + j * E;
+    const int64_t cnt = hi - s0 < E ? hi - s0 : E;
+    const unsigned bytes = (unsigned)((cnt & ~(int64_t)3) * (int64_t)sizeof(K));
+    unsigned long long* bar = &s_bar[j % CNT_STAGES];
+    mbar_arrive_expect_tx(bar, bytes);
+    if (bytes) bulk_g2s(ring + (size_t)(j % CNT_STAGES) * CNT_STAGE_BYTES, keys + s0, bytes, bar);
+  };
+  if (TMA && threadIdx.x == 0) {
+    for (int s = 0; s < CNT_STAGES; ++s) mbar_init(&s_bar[s], 1);
+    fence_mbar_init();
+    for (int s = 0; s < CNT_STAGES; ++s) fill(s);
+  }
+  __syncthreads();
+  int64_t failed = -1;
+  for (int64_t j = 0; j < nst; ++j) {
+    const int64_t s0 = lo + j * E;
+    const int cnt = (int)(hi - s0 < E ? hi - s0 : E);
+    const int cv = TMA ? (cnt & ~3) : 0;
+    const K* sk = reinterpret_cast<const K*>(ring + (size_t)(j % CNT_STAGES) * CNT_STAGE_BYTES);
+    bool bad = false;
+    if (TMA) bad = !mbar_wait(&s_bar[j % CNT_STAGES], (unsigned)(j / CNT_STAGES) & 1u, wait_limit);
+    if (cv == E) {
+#pragma unroll 4
+      for (int idx = threadIdx.x; idx < E; idx += CNT_BLOCK)
+        atomicAdd(&s_h[warp][(unsigned)(Radix<DT>::img(sk[idx]) >> shift) & 255u], 1u);
+    } else {
+      for (int idx = threadIdx.x; idx < cnt; idx += CNT_BLOCK) {
+        const K key = idx < cv ? sk[idx] : keys[s0 + idx];
+        atomicAdd(&s_h[warp][(unsigned)(Radix<DT>::img(key) >> shift) & 255u], 1u);
+      }
+    }
+    if (TMA) {
+      if (__syncthreads_or(bad)) {  // stage j fully read, or a copy never arrived
+        failed = j;
+        break;
+      }
+      if (threadIdx.x == 0) fill(j + CNT_STAGES);
+    }
+  }
+  if (failed >= 0) {
+    if (threadIdx.x == 0) {
+      drain_stages(s_bar, CNT_STAGES, failed, failed + CNT_STAGES < nst ? failed + CNT_STAGES : nst, wait_limit);
+      atomicOr(err, GBK_EBIT_TIMEOUT);
+    }
+    return;
+  }
+  __syncthreads();
+  {
+    const int d = threadIdx.x;  // CNT_BLOCK == 256: one digit per thread
+    unsigned v = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) v += s_h[w][d];
+    if (v) atomicAdd(counts + (int64_t)c * 256 + d, v);
+  }
+}
+
+// ---- 2b. persistent in-order scatter of each chunk ------------------------------
+// Launch shape: threads per CTA, keys per thread per tile (for 8- to 12-byte
+// keys+values; doubled for 4-byte keys alone) and CTAs per SM.  Threads
+// 0..255 also own one digit each.  The ring takes what shared memory is left
+// per CTA, at most 6 stages.  Measured on 2^27 u64 keys + u32 values (8
+// passes), uniform / low-entropy keys: 512 x 8, 1 CTA/SM: 10.3 / 6.8 ms;
+// 512 x 4, 2/SM: 12.5 / 7.0; 256 x 8, 3/SM: 13.2 / 6.1; 256 x 8, 2/SM:
+// 12.2 / 6.4; 1024 x 4, 1/SM: 11.2 / 7.4; 256 x 16, 2/SM: 9.8 / 6.0 (kept:
+// a 4096-key tile, and two CTAs per SM whose rank, reorder and store phases
+// overlap).
+template <int VAR> struct ScVar;
+template <> struct ScVar<0> { static constexpr int BLOCK = 256, KPT = 16, MINB = 2; };
+
+template <int KB, int VB, int VAR> struct ScShape {
+  static constexpr int BLOCK = ScVar<VAR>::BLOCK, MINB = ScVar<VAR>::MINB;
+  static constexpr int WARPS = BLOCK / 32;
+  static constexpr int STATIC_BYTES = WARPS * 256 * 4 + 256 * 8 + 256;  // counters, offsets, bases, misc
+  static constexpr int BUDGET = 233472 / MINB - 1024 - STATIC_BYTES;  // per CTA, 1 KiB reserved per CTA
+  // keys per thread: doubled for 4-byte keys alone, halved when two stages
+  // of the widest elements would not fit
+  static constexpr int KPT0 = (KB + VB) <= 4 ? 2 * ScVar<VAR>::KPT : ScVar<VAR>::KPT;
+  static constexpr int KPT = BUDGET / (BLOCK * KPT0 * (KB + VB)) >= 2 ? KPT0 : KPT0 / 2;
+  static constexpr int TILE = BLOCK * KPT;
+  static constexpr int KEY_BYTES = TILE * KB;
+  static constexpr int STAGE_BYTES = TILE * (KB + VB);
+  static constexpr int STAGES = BUDGET / STAGE_BYTES > 6 ? 6 : BUDGET / STAGE_BYTES;
+  static_assert(STAGES >= 2, "at least one tile in flight beside the one being sorted");
+  static_assert(KPT * 32 <= 65535 && TILE <= 65535, "16-bit tile offsets");
+};
+
+struct ScatterArgs {
+  const int64_t* digit_start;  // [256] global start of each digit in this pass
+  const unsigned* counts;      // [nchunks][256] per-chunk digit counts
   int* err;
-  int64_t ntiles;
+  int64_t tiles_per_chunk;
   int64_t wait_limit;
   int shift;
 };
 
-template <int DT, int VB, int BLOCK, int KPT>
-__global__ void __launch_bounds__(BLOCK)
-    k_onesweep(const typename Radix<DT>::K* __restrict__ kin, typename Radix<DT>::K* __restrict__ kout,
-               const typename ValT<VB>::T* __restrict__ vin, typename ValT<VB>::T* __restrict__ vout, int64_t n,
-               PassArgs A) {
+// Grid = nchunks, MINB CTAs per SM.  TMA: kin/vin 16-byte aligned, tiles
+// streamed through the ring; otherwise tiles are loaded with plain loads and
+// stage 0 only holds the reorder.
+template <int DT, int VB, bool TMA, int VAR>
+__global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
+    k_chunk_scatter(const typename Radix<DT>::K* __restrict__ kin, typename Radix<DT>::K* __restrict__ kout,
+                    const typename ValT<VB>::T* __restrict__ vin, typename ValT<VB>::T* __restrict__ vout, int64_t n,
+                    ScatterArgs A) {
   using K = typename Radix<DT>::K;
   using V = typename ValT<VB>::T;
-  constexpr int WARPS = BLOCK / 32;
-  constexpr int TILE = BLOCK * KPT;
-  static_assert(BLOCK == 256, "one thread per digit");
-  __shared__ unsigned s_whist[WARPS][256];
-  __shared__ unsigned s_start[256];
-  __shared__ long long s_gbase[256];
-  __shared__ unsigned s_wsum[WARPS];
-  __shared__ int s_timeout;
-  __shared__ unsigned s_tile;
-  extern __shared__ __align__(16) unsigned char s_dyn[];
-  K* s_keys = reinterpret_cast<K*>(s_dyn);
-  V* s_vals = reinterpret_cast<V*>(s_dyn + sizeof(K) * TILE);
-
+  using Sh = ScShape<(int)sizeof(K), VB, VAR>;
+  constexpr int BLOCK = Sh::BLOCK, KPT = Sh::KPT, TILE = Sh::TILE, STAGES = Sh::STAGES, WARPS = Sh::WARPS;
+  extern __shared__ __align__(128) unsigned char ring[];
+  __shared__ __align__(8) unsigned long long s_bar[STAGES];
+  __shared__ unsigned short s_cnt[WARPS][256];  // per-warp digit counts of the tile (rank_row)
+  __shared__ unsigned short s_off[WARPS][256];  // tile-local slot of each warp's first key of each digit
+  __shared__ long long s_gb[256];               // global position of tile slot 0 of each digit
+  __shared__ unsigned s_wsum[8];
+  __shared__ int s_oob;  // a digit range of the current tile falls outside [0, n)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    const unsigned t = atomicAdd(A.ticket, 1u);
-    if ((int64_t)t == A.ntiles - 1) *A.ticket = 0u;
-    s_tile = t;
-    s_timeout = 0;
+  const int64_t ntiles = (n + TILE - 1) / TILE;
+  const int64_t t0 = (int64_t)blockIdx.x * A.tiles_per_chunk;
+  const int64_t nt = (t0 + A.tiles_per_chunk < ntiles ? t0 + A.tiles_per_chunk : ntiles) - t0;
+  // Thread 0 only: start the copies of the whole 4-key groups of tile j.
+  auto fill = [&](int64_t j) {
+    if (j >= nt) return;
+    const int64_t base = (t0 + j) * TILE;
+    const int64_t cnt = n - base < TILE ? n - base : TILE;
+    const int64_t cv = cnt & ~(int64_t)3;
+    unsigned char* st = ring + (size_t)(j % STAGES) * Sh::STAGE_BYTES;
+    unsigned long long* bar = &s_bar[j % STAGES];
+    mbar_arrive_expect_tx(bar, (unsigned)(cv * (int64_t)(sizeof(K) + VB)));
+    if (cv) {
+      bulk_g2s(st, kin + base, (unsigned)(cv * (int64_t)sizeof(K)), bar);
+      if (VB) bulk_g2s(st + Sh::KEY_BYTES, vin + base, (unsigned)(cv * VB), bar);
+    }
+  };
+  if (TMA && threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(&s_bar[s], 1);
+    fence_mbar_init();
+    for (int s = 0; s < STAGES; ++s) fill(s);
   }
-  for (int i = lane; i < 256; i += 32) s_whist[warp][i] = 0u;
+  // Running global offset of digit threadIdx.x: its start plus its counts in
+  // the earlier chunks (loads batched 16 at a time).
+  long long run = 0;
+  if (threadIdx.x < 256) {
+    long long r = A.digit_start[threadIdx.x];
+    const unsigned* cp = A.counts + threadIdx.x;
+    const int64_t nc = blockIdx.x;
+    int64_t q = 0;
+    for (; q + 16 <= nc; q += 16) {
+      unsigned v[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) v[u] = cp[(q + u) * 256];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) r += v[u];
+    }
+    for (; q < nc; ++q) r += cp[q * 256];
+    run = r;
+  }
+  for (int i = threadIdx.x; i < WARPS * 256; i += BLOCK) (&s_cnt[0][0])[i] = 0;
+  if (threadIdx.x == 0) s_oob = 0;
   __syncthreads();
-  const int64_t tile = s_tile;
-  const int64_t tbase = tile * (int64_t)TILE;
-  const int cnt = (int)((n - tbase) < TILE ? (n - tbase) : TILE);
-  const int wb = warp * 32 * KPT;  // warp's first slot in the tile
-
-  // ---- load (warp-striped) and rank within the warp ------------------------
-  K key[KPT];
-  V val[KPT];
-  unsigned short rk[KPT];
-  const unsigned lt = (1u << lane) - 1u;
+  const int wb = warp * 32 * KPT;  // the warp's first slot in the tile
+  int64_t failed = -1;
+  bool out_of_range = false;
+  for (int64_t j = 0; j < nt; ++j) {
+    const int64_t base = (t0 + j) * TILE;
+    const int cnt = (int)(n - base < TILE ? n - base : TILE);
+    const int cv = TMA ? (cnt & ~3) : 0;
+    unsigned char* st = ring + (size_t)(TMA ? j % STAGES : 0) * Sh::STAGE_BYTES;
+    K* s_keys = reinterpret_cast<K*>(st);
+    V* s_vals = reinterpret_cast<V*>(st + Sh::KEY_BYTES);
+    bool bad = false;
+    if (TMA) bad = !mbar_wait(&s_bar[j % STAGES], (unsigned)(j / STAGES) & 1u, A.wait_limit);
+    // ---- load (warp-contiguous slots) and rank within the warp -------------
+    const bool full = cv == TILE;  // every tile but the array's last
+    K key[KPT];
+    V val[KPT];
+    unsigned char dig[KPT];
+    unsigned short rk[KPT];
 #pragma unroll
-  for (int k = 0; k < KPT; ++k) {
-    const int slot = wb + k * 32 + lane;
-    const bool ok = slot < cnt;
-    key[k] = ok ? kin[tbase + slot] : K(0);
-    if (VB) val[k] = ok ? vin[tbase + slot] : V(0);
-  }
-#pragma unroll
-  for (int k = 0; k < KPT; ++k) {
-    const int slot = wb + k * 32 + lane;
-    const bool ok = slot < cnt;
-    const unsigned d = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
-    unsigned m = __ballot_sync(0xffffffffu, ok);
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const unsigned bb = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-      m &= ((d >> b) & 1u) ? bb : ~bb;
-    }
-    unsigned base = 0;
-    const int leader = __ffs(m) - 1;
-    if (ok && lane == leader) {
-      base = s_whist[warp][d];
-      s_whist[warp][d] = base + __popc(m);
-    }
-    base = __shfl_sync(0xffffffffu, base, leader < 0 ? lane : leader);
-    rk[k] = (unsigned short)(base + __popc(m & lt));
-    __syncwarp();
-  }
-  __syncthreads();
-  // ---- per-digit totals, warp offsets and tile-local starts ----------------
-  const unsigned d_me = threadIdx.x;  // this thread's digit
-  unsigned tot = 0;
-#pragma unroll
-  for (int w = 0; w < WARPS; ++w) {
-    const unsigned c = s_whist[w][d_me];
-    s_whist[w][d_me] = tot;
-    tot += c;
-  }
-  {
-    // exclusive scan of tot over the 256 digits
-    unsigned inc = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += y;
-    }
-    if (lane == 31) s_wsum[warp] = inc;
-    __syncthreads();
-    unsigned pre = 0;
-#pragma unroll
-    for (int w = 0; w < WARPS; ++w)
-      if (w < warp) pre += s_wsum[w];
-    s_start[d_me] = pre + inc - tot;
-  }
-  // ---- per-digit decoupled look-back ---------------------------------------
-  unsigned* st = A.status + tile * 256;
-  long long excl = 0;
-  if (tile == 0) {
-    st_release_u32(st + d_me, SF_P | tot);
-  } else {
-    st_release_u32(st + d_me, SF_A | tot);
-    int64_t pt = tile - 1;
-    while (true) {
-      unsigned s = 0;
-      int64_t polls = 0;
-      unsigned ns = 0;
-      while (true) {
-        s = ld_acquire_u32(A.status + pt * 256 + d_me);
-        if (s & SF_MASK) break;
-        if (++polls > A.wait_limit || *(volatile int*)&s_timeout) {
-          s = SF_P;
-          atomicExch(&s_timeout, 1);
-          break;
-        }
-        if (polls > 4) {
-          ns = ns ? (ns < 256 ? ns * 2 : 256) : 32;
-          __nanosleep(ns);
-        }
+    for (int k = 0; k < KPT; ++k) {
+      const int slot = wb + k * 32 + lane;
+      if (full) {
+        key[k] = s_keys[slot];
+        if (VB) val[k] = s_vals[slot];
+      } else {
+        const bool ok = slot < cnt;
+        key[k] = slot < cv ? s_keys[slot] : (ok ? kin[base + slot] : K(0));
+        if (VB) val[k] = slot < cv ? s_vals[slot] : (ok ? vin[base + slot] : V(0));
       }
-      excl += (long long)(s & SV_MASK);
-      if ((s & SF_MASK) == SF_P) break;
-      --pt;
+      dig[k] = (unsigned char)(Radix<DT>::img(key[k]) >> A.shift);
     }
-    st_release_u32(st + d_me, SF_P | (unsigned)((excl + tot) & SV_MASK));
-  }
-  s_gbase[d_me] = (long long)A.offsets[d_me] + excl - (long long)s_start[d_me];
-  __syncthreads();
-  if (threadIdx.x == 0 && s_timeout) atomicOr(A.err, GBK_EBIT_TIMEOUT);
-  // ---- reorder the tile by digit in shared memory --------------------------
 #pragma unroll
-  for (int k = 0; k < KPT; ++k) {
-    const int slot = wb + k * 32 + lane;
-    if (slot < cnt) {
-      const unsigned d = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
-      const unsigned r = s_start[d] + s_whist[warp][d] + rk[k];
-      s_keys[r] = key[k];
-      if (VB) s_vals[r] = val[k];
+    for (int k = 0; k < KPT; ++k)
+      rk[k] = (unsigned short)rank_row(s_cnt[warp], dig[k], full || wb + k * 32 + lane < cnt, lane);
+    if (__syncthreads_or(bad)) {  // counts complete and every key read, or a copy never arrived
+      failed = j;
+      break;
     }
+    // ---- digit totals, tile-local starts, global positions ------------------
+    if (threadIdx.x < 256) {
+      const unsigned d = threadIdx.x;
+      unsigned tot = 0;
+      unsigned short wpre[WARPS];  // exclusive prefix over warps
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) {
+        const unsigned c = s_cnt[w][d];
+        s_cnt[w][d] = 0;  // ready for the next tile
+        wpre[w] = (unsigned short)tot;
+        tot += c;
+      }
+      unsigned inc = tot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+      }
+      if (lane == 31) s_wsum[warp] = inc;
+      bar_sync(1, 256);
+      unsigned pre = 0;
+#pragma unroll
+      for (int w = 0; w < 8; ++w)
+        if (w < warp) pre += s_wsum[w];
+      const unsigned start = pre + inc - tot;
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) s_off[w][d] = (unsigned short)(start + wpre[w]);
+      s_gb[d] = run - (long long)start;
+      // this tile writes [run, run + tot) for digit d: inside [0, n) unless
+      // the counts and the keys disagree (keys changed under the sort)
+      if (tot && (run < 0 || run + (long long)tot > n)) s_oob = 1;
+      run += tot;
+    }
+    __syncthreads();
+    // ---- reorder the tile by digit, in place ---------------------------------
+#pragma unroll
+    for (int k = 0; k < KPT; ++k) {
+      if (full || wb + k * 32 + lane < cnt) {
+        const unsigned r = (unsigned)s_off[warp][dig[k]] + rk[k];
+        s_keys[r] = key[k];
+        if (VB) s_vals[r] = val[k];
+      }
+    }
+    __syncthreads();
+    // ---- write the runs of equal digits ---------------------------------------
+    auto emit = [&](int i) {
+      const K kk = s_keys[i];
+      const long long pos = s_gb[(unsigned)(Radix<DT>::img(kk) >> A.shift) & 255u] + i;
+      kout[pos] = kk;
+      if (VB) vout[pos] = s_vals[i];
+    };
+    if (s_oob) {
+      out_of_range = true;  // write nothing of this tile
+    } else if (full) {
+#pragma unroll
+      for (int q = 0; q < KPT; ++q) emit(q * BLOCK + threadIdx.x);
+    } else {
+      for (int i = threadIdx.x; i < cnt; i += BLOCK) emit(i);
+    }
+    if (TMA) fence_proxy_async_smem();  // generic writes of the stage before the next bulk copy into it
+    __syncthreads();
+    if (TMA && threadIdx.x == 0) fill(j + STAGES);
   }
-  __syncthreads();
-  // ---- write runs of equal digits -------------------------------------------
-  for (int i = threadIdx.x; i < cnt; i += BLOCK) {
-    const K kk = s_keys[i];
-    const unsigned d = (unsigned)(Radix<DT>::img(kk) >> A.shift) & 255u;
-    const long long pos = s_gbase[d] + i;
-    kout[pos] = kk;
-    if (VB) vout[pos] = s_vals[i];
+  if (failed >= 0 && threadIdx.x == 0) {
+    drain_stages(s_bar, STAGES, failed, failed + STAGES < nt ? failed + STAGES : nt, A.wait_limit);
+    atomicOr(A.err, GBK_EBIT_TIMEOUT);
   }
+  if (out_of_range) atomicOr(A.err, GBK_EBIT_BAD_STATE);
 }
 
 // ---- host driver ------------------------------------------------------------
-template <int DT, int VB>
-int sort_impl(void* keys, void* vals, int64_t n, Workspace* w) {
+constexpr int HIST_BLOCK = 512;
+constexpr int HIST_SUB = 4;  // CTAs per chunk for the all-digit histogram
+
+template <int DT, int VB, bool TMA, int VAR>
+int launch_pass(const void* kin, void* kout, const void* vin, void* vout, int64_t n, int64_t nchunks,
+                int64_t chunk_keys, const ScatterArgs& A, unsigned* counts, bool count_first, Workspace* w) {
   using K = typename Radix<DT>::K;
   using V = typename ValT<VB>::T;
-  constexpr int KB = sizeof(K);
-  constexpr int BLOCK = 256, KPT = 16, TILE = BLOCK * KPT;
+  using Sh = ScShape<(int)sizeof(K), VB, VAR>;
   cudaStream_t s = w->stream;
-  if (n <= 1) return GBK_OK;
-  if (n >= (int64_t)SV_MASK) return GBK_ERR_INVALID_ARGUMENT;  // 30-bit status counts
-  const int64_t ntiles = (n + TILE - 1) / TILE;
-  // scratch: histogram | offsets | status | key temp | value temp
-  const size_t hb = (size_t)KB * 256 * 8, ob = (size_t)KB * 256 * 8;
-  const size_t sb = ((size_t)ntiles * 256 * 4 + 255) / 256 * 256;
-  const size_t kb = ((size_t)n * sizeof(K) + 255) / 256 * 256;
-  const size_t vb = VB ? ((size_t)n * VB + 255) / 256 * 256 : 0;
-  int st = GBK_OK;
-  char* scr = ws_scratch(w, hb + ob + sb + kb + vb, &st);
-  if (!scr) return st;
-  unsigned long long* d_hist = (unsigned long long*)scr;
-  int64_t* d_off = (int64_t*)(scr + hb);
-  unsigned* d_status = (unsigned*)(scr + hb + ob);
-  K* ktmp = (K*)(scr + hb + ob + sb);
-  V* vtmp = VB ? (V*)(scr + hb + ob + sb + kb) : nullptr;
-
-  GBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, hb, s));
-  {
-    int64_t grid = (int64_t)sm_count() * 4;
-    const int64_t need = (n + BLOCK * 4 - 1) / (BLOCK * 4);
-    if (grid > need) grid = need;
-    if (grid < 1) grid = 1;
-    k_digit_hist<DT, 512><<<(unsigned)grid, 512, 0, s>>>((const K*)keys, n, d_hist);
+  if (count_first) {
+    auto cfn = k_chunk_count<DT, TMA>;
+    constexpr size_t cdyn = TMA ? (size_t)CNT_STAGES * CNT_STAGE_BYTES : 0;
+    static bool cset = false;
+    if (!cset && cdyn) {
+      GBK_CUDA_TRY(cudaFuncSetAttribute(cfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cdyn));
+      cset = true;
+    }
+    GBK_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)nchunks * 256 * 4, s));
+    cfn<<<(unsigned)(nchunks * CNT_SUB), CNT_BLOCK, cdyn, s>>>((const K*)kin, n, chunk_keys, A.shift, counts, w->err,
+                                                               A.wait_limit);
     note_launch();
     GBK_CUDA_TRY(cudaGetLastError());
   }
+  auto sfn = k_chunk_scatter<DT, VB, TMA, VAR>;
+  constexpr size_t sdyn = (size_t)(TMA ? Sh::STAGES : 1) * Sh::STAGE_BYTES;
+  static bool sset = false;
+  if (!sset) {
+    GBK_CUDA_TRY(cudaFuncSetAttribute(sfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sdyn));
+    sset = true;
+  }
+  ScatterArgs a = A;
+  a.counts = counts;
+  sfn<<<(unsigned)nchunks, Sh::BLOCK, sdyn, s>>>((const K*)kin, (K*)kout, (const V*)vin, (V*)vout, n, a);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+template <int DT, int VB, int VAR>
+int sort_var(void* keys, void* vals, int64_t n, Workspace* w) {
+  using K = typename Radix<DT>::K;
+  using V = typename ValT<VB>::T;
+  using Sh = ScShape<(int)sizeof(K), VB, VAR>;
+  constexpr int KB = sizeof(K), TILE = Sh::TILE;
+  static_assert(CNT_BLOCK == 256, "one digit per counting thread");
+  cudaStream_t s = w->stream;
+  if (n <= 1) return GBK_OK;
+  if (n >= ((int64_t)1 << 38)) return GBK_ERR_INVALID_ARGUMENT;  // per-chunk counts are u32
+  const int64_t ntiles = (n + TILE - 1) / TILE;
+  int64_t nchunks = std::min<int64_t>((int64_t)sm_count() * Sh::MINB, ntiles);
+  const int64_t tpc = (ntiles + nchunks - 1) / nchunks;
+  nchunks = (ntiles + tpc - 1) / tpc;  // every chunk non-empty
+  const int64_t chunk_keys = tpc * TILE;
+  // scratch: histogram | digit starts | per-chunk counts of every digit |
+  // per-chunk counts of one digit | key temp | value temp
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t hb = (size_t)KB * 256 * 8, ob = (size_t)KB * 256 * 8;
+  const size_t ccb = up((size_t)KB * nchunks * 256 * 4), c1b = up((size_t)nchunks * 256 * 4);
+  const size_t kb = up((size_t)n * sizeof(K)), vb = VB ? up((size_t)n * VB) : 0;
+  int st = GBK_OK;
+  char* scr = ws_scratch(w, hb + ob + ccb + c1b + kb + vb, &st);
+  if (!scr) return st;
+  unsigned long long* d_hist = (unsigned long long*)scr;
+  int64_t* d_off = (int64_t*)(scr + hb);
+  unsigned* d_cc = (unsigned*)(scr + hb + ob);
+  unsigned* d_c1 = (unsigned*)(scr + hb + ob + ccb);
+  K* ktmp = (K*)(scr + hb + ob + ccb + c1b);
+  V* vtmp = VB ? (V*)(scr + hb + ob + ccb + c1b + kb) : nullptr;
+
+  GBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, hb, s));
+  GBK_CUDA_TRY(cudaMemsetAsync(d_cc, 0, ccb, s));
+  k_digit_hist<DT, HIST_BLOCK><<<(unsigned)(nchunks * HIST_SUB), HIST_BLOCK, 0, s>>>(
+      (const K*)keys, n, chunk_keys, HIST_SUB, (int)nchunks, d_hist, d_cc);
+  note_launch();
+  GBK_CUDA_TRY(cudaGetLastError());
   std::vector<unsigned long long> h(KB * 256);
   GBK_CUDA_TRY(cudaMemcpyAsync(h.data(), d_hist, hb, cudaMemcpyDeviceToHost, s));
   GBK_CUDA_TRY(cudaStreamSynchronize(s));
@@ -310,27 +543,27 @@ int sort_impl(void* keys, void* vals, int64_t n, Workspace* w) {
   GBK_CUDA_TRY(cudaMemcpyAsync(d_off, offs.data(), ob, cudaMemcpyHostToDevice, s));
   // The host vector must outlive the copy.
   GBK_CUDA_TRY(cudaStreamSynchronize(s));
-  const size_t dyn = (size_t)TILE * (sizeof(K) + (VB ? VB : 0));
-  auto kfn = k_onesweep<DT, VB, BLOCK, KPT>;
-  GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  // Bulk copies want 16-byte aligned sources: the caller's buffers may not be.
+  const bool user_aligned = (uintptr_t)keys % 16 == 0 && (!VB || (uintptr_t)vals % 16 == 0);
   K* kin = (K*)keys;
   K* kout = ktmp;
   V* vin = (V*)vals;
   V* vout = vtmp;
   for (size_t i = 0; i < passes.size(); ++i) {
     const int p = passes[i];
-    GBK_CUDA_TRY(cudaMemsetAsync(d_status, 0, (size_t)ntiles * 256 * 4, s));
-    PassArgs A;
-    A.status = d_status;
-    A.offsets = d_off + p * 256;
-    A.ticket = w->counters + SLOT_SORT;
+    ScatterArgs A;
+    A.digit_start = d_off + p * 256;
+    A.counts = nullptr;
     A.err = w->err;
-    A.ntiles = ntiles;
+    A.tiles_per_chunk = tpc;
     A.wait_limit = wait_limit();
     A.shift = 8 * p;
-    kfn<<<(unsigned)ntiles, BLOCK, dyn, s>>>(kin, kout, vin, vout, n, A);
-    note_launch();
-    GBK_CUDA_TRY(cudaGetLastError());
+    // the first pass uses the per-chunk counts of the all-digit histogram
+    unsigned* counts = i == 0 ? d_cc + (size_t)p * nchunks * 256 : d_c1;
+    const bool tma = kin != (K*)keys || user_aligned;
+    st = tma ? launch_pass<DT, VB, true, VAR>(kin, kout, vin, vout, n, nchunks, chunk_keys, A, counts, i > 0, w)
+             : launch_pass<DT, VB, false, VAR>(kin, kout, vin, vout, n, nchunks, chunk_keys, A, counts, i > 0, w);
+    if (st) return st;
     std::swap(kin, kout);
     std::swap(vin, vout);
   }
@@ -339,6 +572,11 @@ int sort_impl(void* keys, void* vals, int64_t n, Workspace* w) {
     if (VB) GBK_CUDA_TRY(cudaMemcpyAsync(vals, vin, (size_t)n * VB, cudaMemcpyDeviceToDevice, s));
   }
   return GBK_OK;
+}
+
+template <int DT, int VB>
+int sort_impl(void* keys, void* vals, int64_t n, Workspace* w) {
+  return sort_var<DT, VB, 0>(keys, vals, n, w);
 }
 
 template <int DT>

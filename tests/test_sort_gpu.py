@@ -116,6 +116,62 @@ def test_sort_key_types_vs_oracle(env, kdt, n):
         check_stable_sort(k, k[perm], perm)
 
 
+@pytest.mark.parametrize("kdt,vbytes", [(np.uint32, 0), (np.uint32, 4), (np.uint32, 8), (np.uint64, 0),
+                                        (np.uint64, 4), (np.uint64, 8)])
+@pytest.mark.parametrize("n", [152 * 4096 * 2 + 3, (1 << 21) + 1, 5 * 8192 - 1])
+def test_sort_ragged_chunks(env, kdt, vbytes, n):
+    """Sizes that give many chunks of whole tiles with a ragged last tile and
+    a tail shorter than one 16-byte group, for every key / payload width."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    k = datagen.bits_u64(n, seed=n + vbytes).astype(kdt)
+    code = 2 if kdt == np.uint32 else 3
+    dk = _dev(torch, k)
+    if vbytes == 0:
+        gbk.sort(dk, dt=code)
+        gbk.stream_check()
+        assert _host(dk, kdt).tobytes() == np.sort(k, kind="stable").tobytes()
+        return
+    dv = torch.arange(n, dtype=torch.int32 if vbytes == 4 else torch.int64, device="cuda")
+    gbk.sort_by_key(dk, dv, dt=code)
+    gbk.stream_check()
+    check_stable_sort(k, _host(dk, kdt), dv.cpu().numpy())
+
+
+@pytest.mark.parametrize("kdt,off", [(np.uint64, 1), (np.uint32, 1), (np.uint32, 3)])
+def test_sort_unaligned_buffers(env, kdt, off):
+    """Caller buffers that start off a 16-byte boundary: the passes that read
+    them use plain loads instead of bulk copies."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    n = 300007
+    k = datagen.bits_u64(n, seed=7).astype(kdt)
+    base = _dev(torch, np.concatenate([np.zeros(off, dtype=kdt), k]))
+    dk = base[off:]
+    assert dk.data_ptr() % 16 != 0
+    vbase = torch.arange(-1, n, dtype=torch.int32, device="cuda")
+    dv = vbase[1:]
+    assert dv.data_ptr() % 16 != 0
+    gbk.sort_by_key(dk, dv, dt=2 if kdt == np.uint32 else 3)
+    gbk.stream_check()
+    check_stable_sort(k, _host(dk, kdt), dv.cpu().numpy())
+    assert int(vbase[0].item()) == -1 and _host(base[:off], kdt).tolist() == [0] * off
+
+
+@pytest.mark.parametrize("ndistinct", [1, 2, 3, 255, 257])
+def test_sort_few_distinct_keys(env, ndistinct):
+    """Heavy duplicates: every tile holds long runs of one digit."""
+    gbk, torch = env
+    n = 1 << 20
+    rng = np.random.default_rng(ndistinct)
+    vals = rng.integers(0, 1 << 63, size=ndistinct, dtype=np.uint64)
+    k = vals[rng.integers(0, ndistinct, size=n)]
+    dk, dv = _dev(torch, k), torch.arange(n, dtype=torch.int32, device="cuda")
+    gbk.sort_by_key(dk, dv, dt=3)
+    gbk.stream_check()
+    check_stable_sort(k, _host(dk, np.uint64), dv.cpu().numpy())
+
+
 def test_all_keys_equal_and_one_varying_digit(env):
     gbk, torch = env
     n = 100003
