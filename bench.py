@@ -204,10 +204,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tuning-table", action="store_true",
                     help="use the library defaults instead of the autotuner's table (kokkos_gb300/tuning_table.txt)")
-    ap.add_argument("--only", default=None, choices=["minloc", "maxloc", "sum", "hist", "sum_f64", "exscan"],
+    ap.add_argument("--only", default=None,
+                    choices=["minloc", "maxloc", "sum", "hist", "sum_f64", "exscan", "sort"],
                     help="run just this operation warmup+steps times (for profiler captures): the bench ops on the "
                          "bench inputs, or sum_f64 / exscan on 2^24 doubles / int32 (the RangePolicy Sum and "
-                         "exclusive_scan i32->i64 workload)")
+                         "exclusive_scan i32->i64 workload), or sort: sort_by_key of --sort-n uniform uint64 keys "
+                         "with an int32 iota payload (the sort_by_key workload, 2^27 by default)")
+    ap.add_argument("--sort-n", type=int, default=1 << 27)
+    ap.add_argument("--sort-keys", default="uniform", choices=["uniform", "lowentropy"],
+                    help="--only sort keys: uniform 64-bit, or a seeded base pattern with 8 random bit positions")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -229,6 +234,29 @@ def main():
     if not args.no_tuning_table and os.path.exists(table):
         tuned = lib.gbk_tuner_load(table.encode()) == 0 and lib.gbk_tuner_enable(1) == 0
 
+    if args.only == "sort":
+        n = args.sort_n
+        kh = datagen.bits_u64(n, seed=0) if args.sort_keys == "uniform" else datagen.lowentropy_u64(n, 8, seed=0)[0]
+        k0 = torch.from_numpy(kh.view(np.int64)).to(dev)
+        iota = torch.arange(n, dtype=torch.int32, device=dev)
+        dk, dv = torch.empty_like(k0), torch.empty_like(iota)
+        evs = []
+        for _ in range(args.warmup + args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                # refill on the sort's own stream: the previous sort must finish before its input changes
+                dk.copy_(k0)
+                dv.copy_(iota)
+                e0.record(stream)
+                gbk.check(lib.gbk_sort_by_key(3, ctypes.c_void_p(dk.data_ptr()), 4, ctypes.c_void_p(dv.data_ptr()),
+                                              n, sp), "sort_by_key")
+                e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        gbk.stream_check(stream)
+        ms = [a.elapsed_time(b) for a, b in evs[args.warmup:]]
+        print(json.dumps({"only": "sort", "keys": args.sort_keys, "n": n, "ms": ms, "Gpairs/s": [round(n / m / 1e6, 3) for m in ms]}))
+        return
     if args.only in ("sum_f64", "exscan"):
         n = 1 << 24
         res = torch.zeros(64, dtype=torch.uint8, device=dev)

@@ -217,6 +217,83 @@ template <class T> struct RMinMaxLoc {
   }
 };
 
+// Ordered update by one 16-byte vector of consecutive elements at locs l0,
+// l0 + 1, ...: the same result as update<true> element by element.  The
+// *Loc reducers fold the vector to its extremum first (fminf / fmaxf skip a
+// NaN, as the strict comparisons of update<true> do) and touch (val, loc)
+// only when that beats the running value, taking the first element equal to
+// it (the first occurrence, as the element-wise strict update keeps; -0.0
+// and +0.0 compare equal there too).  A running extremum changes rarely, so
+// the common cost is VEC - 1 min/max operations and one comparison.
+__device__ __forceinline__ float ext_min(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double ext_min(double a, double b) { return fmin(a, b); }
+template <class T> __device__ __forceinline__ T ext_min(T a, T b) { return b < a ? b : a; }
+__device__ __forceinline__ float ext_max(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double ext_max(double a, double b) { return fmax(a, b); }
+template <class T> __device__ __forceinline__ T ext_max(T a, T b) { return b > a ? b : a; }
+
+template <class T, int VEC, bool MIN>
+__device__ __forceinline__ void vec_extreme(const T* v, T& e) {
+  e = v[0];
+#pragma unroll
+  for (int q = 1; q < VEC; ++q) e = MIN ? ext_min(e, v[q]) : ext_max(e, v[q]);
+}
+// First q with v[q] == e (e is one of the v[q]), with that element.
+template <class T, int VEC>
+__device__ __forceinline__ void vec_first_equal(const T* v, T e, T& val, int& q) {
+  val = v[VEC - 1];
+  q = VEC - 1;
+#pragma unroll
+  for (int k = VEC - 2; k >= 0; --k)
+    if (v[k] == e) { val = v[k]; q = k; }
+}
+
+template <class R, class T, int VEC> struct VecUpd {
+  __device__ static void run(typename R::V& acc, const T* v, int64_t l0) {
+#pragma unroll
+    for (int q = 0; q < VEC; ++q) R::template update<true>(acc, v[q], l0 + q);
+  }
+};
+template <class T, int VEC> struct VecUpd<RMinLoc<T>, T, VEC> {
+  __device__ static void run(ValLoc<T>& acc, const T* v, int64_t l0) {
+    T e;
+    vec_extreme<T, VEC, true>(v, e);
+    if (e < acc.val) {
+      int q;
+      vec_first_equal<T, VEC>(v, e, acc.val, q);
+      acc.loc = l0 + q;
+    }
+  }
+};
+template <class T, int VEC> struct VecUpd<RMaxLoc<T>, T, VEC> {
+  __device__ static void run(ValLoc<T>& acc, const T* v, int64_t l0) {
+    T e;
+    vec_extreme<T, VEC, false>(v, e);
+    if (e > acc.val) {
+      int q;
+      vec_first_equal<T, VEC>(v, e, acc.val, q);
+      acc.loc = l0 + q;
+    }
+  }
+};
+template <class T, int VEC> struct VecUpd<RMinMaxLoc<T>, T, VEC> {
+  __device__ static void run(MinMaxLocV<T>& acc, const T* v, int64_t l0) {
+    T lo, hi;
+    vec_extreme<T, VEC, true>(v, lo);
+    vec_extreme<T, VEC, false>(v, hi);
+    if (lo < acc.min_val) {
+      int q;
+      vec_first_equal<T, VEC>(v, lo, acc.min_val, q);
+      acc.min_loc = l0 + q;
+    }
+    if (hi > acc.max_val) {
+      int q;
+      vec_first_equal<T, VEC>(v, hi, acc.max_val, q);
+      acc.max_loc = l0 + q;
+    }
+  }
+};
+
 // Warp tree.  32-bit integer Sum/Min/Max/BAnd/BOr use redux.sync (one
 // instruction); everything else a butterfly of shuffles.
 template <class R> struct WarpRed {

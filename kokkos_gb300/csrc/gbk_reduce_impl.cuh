@@ -105,8 +105,7 @@ __global__ void __launch_bounds__(BLOCK)
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       const int64_t e0 = lb + (vb + (int64_t)u * BLOCK) * VEC;
-#pragma unroll
-      for (int k = 0; k < VEC; ++k) R::template update<true>(acc, cur[u].v[k], e0 + k);
+      VecUpd<R, T, VEC>::run(acc, cur[u].v, e0);
     }
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) cur[u] = nxt[u];
@@ -116,8 +115,7 @@ __global__ void __launch_bounds__(BLOCK)
   for (; vb < v1; vb += BLOCK) {
     Vec16<T> v;
     v.u = ld_stream16(xb + vb * VEC);
-#pragma unroll
-    for (int k = 0; k < VEC; ++k) R::template update<true>(acc, v.v[k], lb + vb * VEC + k);
+    VecUpd<R, T, VEC>::run(acc, v.v, lb + vb * VEC);
   }
   // Tail elements after the last whole vector.
   const int64_t t0 = head + nvec * VEC;
@@ -178,25 +176,26 @@ __global__ void __launch_bounds__(BLOCK)
     const int cnt = (int)(v1 - c0 < CV ? v1 - c0 : CV);
     const uint4* sv = reinterpret_cast<const uint4*>(ring + (size_t)s * CHUNK_BYTES);
     if (cnt == CV) {
+      // Take the chunk into registers and hand the stage back to the copy
+      // engine before folding, so the refill overlaps the fold.
+      Vec16<T> u[CV / BLOCK];
 #pragma unroll
-      for (int k = 0; k < CV / BLOCK; ++k) {
-        Vec16<T> u;
-        u.u = sv[k * BLOCK + threadIdx.x];
-        const int64_t e0 = lb + (c0 + k * BLOCK + threadIdx.x) * VEC;
+      for (int k = 0; k < CV / BLOCK; ++k) u[k].u = sv[k * BLOCK + threadIdx.x];
+      __syncthreads();  // stage s fully read: refill it
+      if (threadIdx.x == 0) fill(c + STAGES);
 #pragma unroll
-        for (int q = 0; q < VEC; ++q) R::template update<true>(acc, u.v[q], e0 + q);
-      }
+      for (int k = 0; k < CV / BLOCK; ++k)
+        VecUpd<R, T, VEC>::run(acc, u[k].v, lb + (c0 + k * BLOCK + threadIdx.x) * VEC);
     } else {
       for (int i = threadIdx.x; i < cnt; i += BLOCK) {
         Vec16<T> u;
         u.u = sv[i];
         const int64_t e0 = lb + (c0 + i) * VEC;
-#pragma unroll
-        for (int q = 0; q < VEC; ++q) R::template update<true>(acc, u.v[q], e0 + q);
+        VecUpd<R, T, VEC>::run(acc, u.v, e0);
       }
+      __syncthreads();  // stage s fully read: refill it
+      if (threadIdx.x == 0) fill(c + STAGES);
     }
-    __syncthreads();  // stage s fully read: refill it
-    if (threadIdx.x == 0) fill(c + STAGES);
   }
   const int64_t t0 = head + nvec * VEC;
   if (t0 + gtid < n) R::template update<true>(acc, x[t0 + gtid], loc0 + t0 + gtid);

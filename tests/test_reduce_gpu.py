@@ -212,3 +212,38 @@ def test_tuning_configs_agree(env):
         gs = gbk.decode_result(gbk.reduce("sum", df, tune=(blk, un, cps, 0)).cpu().numpy(), 0, 4)
         ok, info = sum_ok(gs, xf, 1e-5)
         assert ok, info
+
+
+@pytest.mark.parametrize("n", [4099, (1 << 21) + 7, (1 << 22) + 3])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32])
+def test_loc_ties_nan_signed_zero(env, n, dtype):
+    """*Loc reducers on data full of ties (few distinct values), NaNs and
+    signed zeros, through the flat (< 4 MiB) and the ring kernel: the value
+    and the first-occurrence loc equal the oracle's element-by-element strict
+    comparison."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    t = np.dtype(dtype)
+    x = datagen.uniform_i64(n, -3, 3, seed=n + 11).astype(t)
+    if t.kind == "f":
+        x[x == 0] = -0.0
+        x[::7] = 0.0
+        x[5::13] = np.nan
+        x[: min(n, 64)] = np.nan  # a NaN-only prefix: the running value stays the identity for a while
+    cases = [x]
+    if t.kind == "f":
+        z = (x > 0).astype(t)  # minimum 0: the first zero wins, whatever its sign
+        zi = np.flatnonzero(z == 0)
+        z[zi[::2]] = -0.0
+        z[5::13] = np.nan
+        z[: min(n, 64)] = np.nan
+        cases.append(z)
+    for i, a in enumerate(cases):
+        d = _dev(torch, a)
+        # plain Min over {-0.0, +0.0} may return either zero (partials join in tree order); the *Loc
+        # reducers return the first occurrence, sign included
+        for op in ("minloc", "maxloc", "minmaxloc") + (("min", "max") if i == 0 else ()):
+            got = gbk.reduce_value(op, d)
+            want = oracle.reduce(op, a, 1)
+            compare(op, got, want, a)
