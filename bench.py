@@ -15,6 +15,11 @@ and the keys to the device, the four operations, and the results copied
 back, every step.  `roofline` is the dominant kernel (the flat ring reduce
 the contiguous MDRange box collapses to).  `cpu_baseline` is the
 oracle (CPU restatement of the reference OpenMP algorithms) on this host.
+`other_configs` (N = 1 only) times the other headline workloads after the
+step, outside the timed region: the RangePolicy Sum and exclusive_scan of
+2^24 values, the batched segmented Sum / inclusive_scan over 10,000
+lognormal segments against the one-launch-per-segment loop, and
+sort_by_key of 2^27 uint64 keys with an int32 payload.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbk|reference]
 
@@ -48,7 +53,7 @@ STEP_BYTES = 3 * RED_BYTES + HIST_BYTES
 # dram__bytes_write.sum from one ncu capture of the same launch, as recorded
 # in profiles/).
 ROOF_KERNEL = "k_reduce_tma (MinLoc/MaxLoc/Sum f32, shared-memory ring)"
-ROOF_TRAFFIC = 271834880  # MinLoc f32 over the box: 268.48 MB read + 3.36 MB written
+ROOF_TRAFFIC = 272138240  # MinLoc f32 over the box: 268.48 MB read + 3.66 MB written
 WORKLOAD = ("MDRange<Rank<3>> MinLoc+MaxLoc+Sum over LayoutLeft View<float***> 512x512x256 N(0,1) "
             "+ ScatterView histogram 2^26 int32 Zipf(1.1) keys -> 2^16 int64 bins")
 
@@ -178,6 +183,156 @@ def cpu_baseline(budget_s=12.0):
             "sample": f"{steps} full-size steps ({el:.1f} s) of the same workload, OpenMP threads={P}"}
 
 
+def other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind, reps=10):
+    """The other headline workloads of the path, timed after the step with CUDA
+    events around each call on the launching stream (not part of `value`):
+      c1: Sum over 2^24 uniform doubles and exclusive_scan int32 -> int64 of
+          2^24 values 0..15, inputs rotated over 4 copies (each call starts
+          with its input out of L2), 40 calls back to back between two events;
+      c3: 10,000 lognormal segments (median 2,048, max 2^21, total ~2^28):
+          per-segment Sum f32 and inclusive_scan int32, one launch each (10
+          back to back; inputs of 1 GB), and one pass of the
+          one-launch-per-segment loop for comparison;
+      c4: sort_by_key of 2^27 uint64 keys + int32 iota payload, uniform and
+          low-entropy keys (inputs refilled on the stream before each sort);
+      data movement: deep_copy of 1 GiB device to device (read + write
+          bytes), deep_copy(view, value) of 1 GiB, permute (gather) of 2^26
+          int32 by a random permutation (4 + 8 + 4 bytes per element)."""
+    lib = gbk.lib
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    P = ctypes.c_void_p
+    out = {}
+
+    def timed(calls, n_reps, prep=None, batch=False):
+        """Median per-call ms with events around each call, or (batch) the
+        mean over n_reps back-to-back calls between two events."""
+        evs = []
+        with torch.cuda.stream(stream):
+            for c in calls:
+                if prep:
+                    prep(c)
+                c()
+            if batch:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for r in range(n_reps):
+                    calls[r % len(calls)]()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                gbk.stream_check(stream)
+                return e0.elapsed_time(e1) / n_reps
+            for r in range(n_reps):
+                c = calls[r % len(calls)]
+                if prep:
+                    prep(c)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                c()
+                e1.record(stream)
+                evs.append((e0, e1))
+        torch.cuda.synchronize()
+        gbk.stream_check(stream)
+        return float(np.median([a.elapsed_time(b) for a, b in evs]))
+
+    def rate(nbytes, ms):
+        g = nbytes / (ms / 1e3) / 1e9
+        return {"ms": round(ms, 5), "GB/s": round(g, 1), "frac_of_" + peak_kind + "_hbm": round(g / hbm, 4)}
+
+    # ---- c1 -----------------------------------------------------------------
+    n = 1 << 24
+    res = torch.zeros(64, dtype=torch.uint8, device=dev)
+    xs = [torch.from_numpy(datagen.uniform_f64(n, seed=c)).to(dev) for c in range(4)]
+    calls = [lambda x=x: gbk.check(lib.gbk_reduce(0, 5, P(x.data_ptr()), n, P(res.data_ptr()), sp, None), "sum")
+             for x in xs]
+    out["c1_sum_f64_2^24"] = rate(n * 8, timed(calls, 40, batch=True))
+    del xs, calls
+    iv = ctypes.c_int64(0)
+    xi = [torch.from_numpy(datagen.uniform_i32(n, 0, 15, seed=c)).to(dev) for c in range(4)]
+    ys = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(4)]
+    calls = [lambda x=x, y=y: gbk.check(lib.gbk_scan(0, 0, 1, P(x.data_ptr()), n, ctypes.byref(iv), P(y.data_ptr()),
+                                                     None, sp, None), "exscan") for x, y in zip(xi, ys)]
+    out["c1_exclusive_scan_i32_i64_2^24"] = rate(n * 12, timed(calls, 40, batch=True))
+    del xi, ys, calls
+
+    # ---- c3 -----------------------------------------------------------------
+    lens, sigma = datagen.lognormal_lengths(10000, median=2048.0, max_len=1 << 21, target_total=1 << 28, seed=0)
+    offs = datagen.offsets_from_lengths(lens)
+    ns, nseg = int(offs[-1]), len(lens)
+    do = torch.from_numpy(offs).to(dev)
+    xf = torch.from_numpy(datagen.normal_f32(ns, seed=0)).to(dev)
+    xq = torch.from_numpy(datagen.uniform_i32(ns, 0, 255, seed=0)).to(dev)
+    segout = torch.empty(nseg, dtype=torch.float32, device=dev)
+    yq = torch.empty(ns, dtype=torch.int32, device=dev)
+    ms_sum = timed([lambda: gbk.check(lib.gbk_segmented_reduce(0, 4, P(xf.data_ptr()), P(do.data_ptr()), nseg, ns,
+                                                                P(segout.data_ptr()), sp, None), "seg sum")], reps,
+                   batch=True)
+    ms_scan = timed([lambda: gbk.check(lib.gbk_segmented_scan(1, 0, 0, P(xq.data_ptr()), P(do.data_ptr()), nseg, ns,
+                                                               P(yq.data_ptr()), sp, None), "seg scan")], reps,
+                    batch=True)
+    ob = [int(v) for v in offs]
+
+    def loop_sum():
+        for s_ in range(nseg):
+            gbk.check(lib.gbk_reduce(0, 4, P(xf.data_ptr() + 4 * ob[s_]), ob[s_ + 1] - ob[s_],
+                                     P(segout.data_ptr() + 4 * s_), sp, None), "loop sum")
+
+    def loop_scan():
+        for s_ in range(nseg):
+            gbk.check(lib.gbk_scan(1, 0, 0, P(xq.data_ptr() + 4 * ob[s_]), ob[s_ + 1] - ob[s_], None,
+                                   P(yq.data_ptr() + 4 * ob[s_]), None, sp, None), "loop scan")
+
+    ms_lsum = timed([loop_sum], 1)
+    ms_lscan = timed([loop_scan], 1)
+    ob_bytes = (nseg + 1) * 8
+    out["c3_segmented_sum_f32"] = dict(rate(ns * 4 + ob_bytes + nseg * 4, ms_sum), per_segment_loop_ms=round(ms_lsum, 3),
+                                       speedup=round(ms_lsum / ms_sum, 1))
+    out["c3_segmented_inclusive_scan_i32"] = dict(rate(ns * 8 + ob_bytes, ms_scan),
+                                                  per_segment_loop_ms=round(ms_lscan, 3),
+                                                  speedup=round(ms_lscan / ms_scan, 1))
+    out["c3_data"] = {"segments": nseg, "elements": ns, "lognormal_sigma": round(float(sigma), 4)}
+    del xf, xq, yq, do, segout
+
+    # ---- c4 -----------------------------------------------------------------
+    n = 1 << 27
+    iota = torch.arange(n, dtype=torch.int32, device=dev)
+    dk, dv = torch.empty(n, dtype=torch.int64, device=dev), torch.empty_like(iota)
+    for name, kh in (("uniform", datagen.bits_u64(n, seed=0)), ("lowentropy", datagen.lowentropy_u64(n, 8, seed=0)[0])):
+        passes = sum(1 for p_ in range(8) if np.any(((kh >> np.uint64(8 * p_)) & np.uint64(255)) !=
+                                                  ((kh[0] >> np.uint64(8 * p_)) & np.uint64(255))))
+        k0 = torch.from_numpy(kh.view(np.int64)).to(dev)
+
+        def refill(_c, k0=k0):
+            dk.copy_(k0)
+            dv.copy_(iota)
+
+        ms = timed([lambda: gbk.check(lib.gbk_sort_by_key(3, P(dk.data_ptr()), 4, P(dv.data_ptr()), n, sp),
+                                      "sort_by_key")], 3, prep=refill)
+        pass_bytes = n * 8 + max(passes - 1, 0) * n * 8 + passes * n * 24
+        out["c4_sort_by_key_u64_i32_2^27_" + name] = dict(
+            rate(pass_bytes, ms), digit_passes=passes, Gpairs_per_s=round(n / (ms / 1e3) / 1e9, 3),
+            min_bytes_GBps=round(n * 24 / (ms / 1e3) / 1e9, 1))
+        del k0
+    del iota, dk, dv
+
+    # ---- data movement either side of the path --------------------------------
+    nb = 1 << 30
+    a_ = torch.empty(nb // 4, dtype=torch.int32, device=dev)
+    b_ = torch.empty_like(a_)
+    a_.fill_(1)
+    v32 = np.array([7], dtype=np.int32)
+    out["deep_copy_d2d_1GiB"] = rate(2 * nb, timed(
+        [lambda: gbk.check(lib.gbk_deep_copy(P(b_.data_ptr()), P(a_.data_ptr()), nb, sp), "deep_copy")], reps))
+    out["fill_i32_1GiB"] = rate(nb, timed(
+        [lambda: gbk.check(lib.gbk_fill(P(b_.data_ptr()), P(v32.ctypes.data), 4, nb // 4, sp), "fill")], reps))
+    np_ = 1 << 26
+    perm = torch.from_numpy(np.random.default_rng(0).permutation(np_).astype(np.int64)).to(dev)
+    out["permute_i32_2^26_random"] = rate(np_ * 16, timed(
+        [lambda: gbk.check(lib.gbk_permute(4, P(a_.data_ptr()), P(perm.data_ptr()), np_, P(b_.data_ptr()), sp),
+                           "permute")], reps))
+    del a_, b_, perm
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference's CPU implementation of the path on
     this host.  The reference build (oracle/_ref) is produced in a container
@@ -202,6 +357,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbk", choices=["gbk", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other headline workloads (C1 sum/scan, C3 segmented, C4 sort) timed after the step")
     ap.add_argument("--no-tuning-table", action="store_true",
                     help="use the library defaults instead of the autotuner's table (kokkos_gb300/tuning_table.txt)")
     ap.add_argument("--only", default=None,
@@ -422,6 +579,8 @@ def main():
         "clocks": clk,
         "result_check": ok,
     }
+    if world == 1 and not args.no_configs:
+        line["other_configs"] = other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:

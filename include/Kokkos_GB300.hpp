@@ -21,6 +21,7 @@
 #include "gb300/scan.hpp"
 #include "gb300/scatter_sort.hpp"
 #include "gb300/algorithms.hpp"
+#include "gb300/unordered_map.hpp"
 
 #ifndef GBK_NO_KOKKOS_NAMESPACE
 namespace Kokkos = gb300k;

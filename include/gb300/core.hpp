@@ -258,6 +258,23 @@ void deep_copy(const View<D1, P1...>& dst, const View<D2, P2...>& src) {
         "deep_copy");
   check_cuda(cudaStreamSynchronize(nullptr), "deep_copy");
 }
+// deep_copy(view, value): every element becomes value (the reference's
+// ViewFill, core/src/Kokkos_CopyViews.hpp:58-260, 897); device views are
+// filled by gbk_fill with 16-byte streaming stores.
+template <class D, class... P>
+void deep_copy(const View<D, P...>& dst, const typename View<D, P...>::value_type& value) {
+  using T = typename View<D, P...>::value_type;
+  const int64_t n = (int64_t)dst.size();
+  if (View<D, P...>::is_device && (sizeof(T) == 1 || sizeof(T) == 2 || sizeof(T) == 4 || sizeof(T) == 8 ||
+                                   sizeof(T) == 16)) {
+    check(gbk_fill(dst.data(), &value, (int)sizeof(T), n, nullptr), "deep_copy(view, value)");
+    check_cuda(cudaStreamSynchronize(nullptr), "deep_copy(view, value)");
+  } else if (View<D, P...>::is_device) {
+    throw std::runtime_error("deep_copy(view, value): element size must be 1, 2, 4, 8 or 16 bytes");
+  } else {
+    for (int64_t i = 0; i < n; ++i) dst.data()[i] = value;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Policies
@@ -322,8 +339,30 @@ class MDRangePolicy {
   int64_t lo_[4] = {0, 0, 0, 0}, up_[4] = {0, 0, 0, 0};
 };
 
+// Kokkos::pair (core/src/Kokkos_Pair.hpp): a host-device pair.
+template <class T1, class T2>
+struct pair {
+  using first_type = T1;
+  using second_type = T2;
+  T1 first;
+  T2 second;
+  KOKKOS_FORCEINLINE_FUNCTION constexpr pair() : first(), second() {}
+  KOKKOS_FORCEINLINE_FUNCTION constexpr pair(const T1& a, const T2& b) : first(a), second(b) {}
+};
+template <class T1, class T2>
+KOKKOS_FORCEINLINE_FUNCTION constexpr pair<T1, T2> make_pair(T1 a, T2 b) {
+  return pair<T1, T2>(a, b);
+}
+
 struct AUTO_t {};
 constexpr AUTO_t AUTO{};
+
+namespace Impl {
+// Team collectives of TeamMember, defined in parallel.hpp.
+template <class Red, class V> __device__ V team_allreduce(const Red& red, V v);
+template <class T> __device__ T team_exclusive_sum(const T& v, T* global_accum);
+template <class T> __device__ void team_bcast(T& v, int root);
+}  // namespace Impl
 
 // Team member: one team = one CTA (team_size threads), league ranks
 // distributed over the grid (core/src/Cuda/Kokkos_Cuda_Team.hpp:72-360 is the
@@ -353,6 +392,54 @@ class TeamMember {
 #ifdef __CUDA_ARCH__
     __syncthreads();
 #endif
+  }
+  // Every thread receives the root thread's value
+  // (core/src/Cuda/Kokkos_Cuda_Team.hpp:123-170).
+  template <class T>
+  KOKKOS_INLINE_FUNCTION void team_broadcast(T& val, int root) const {
+#ifdef __CUDA_ARCH__
+    Impl::team_bcast(val, root);
+#endif
+  }
+  template <class F, class T>
+  KOKKOS_INLINE_FUNCTION void team_broadcast(const F& f, T& val, int root) const {
+#ifdef __CUDA_ARCH__
+    f(val);
+    Impl::team_bcast(val, root);
+#endif
+  }
+  // Join of every thread's reducer.reference() (or `value`) over the team;
+  // every thread's reducer.reference() receives the result
+  // (Kokkos_Cuda_Team.hpp:188-210).
+  template <class Red>
+  KOKKOS_INLINE_FUNCTION void team_reduce(const Red& red) const {
+#ifdef __CUDA_ARCH__
+    red.reference() = Impl::team_allreduce(red, red.reference());
+#endif
+  }
+  template <class Red>
+  KOKKOS_INLINE_FUNCTION void team_reduce(const Red& red, const typename Red::value_type& value) const {
+#ifdef __CUDA_ARCH__
+    red.reference() = Impl::team_allreduce(red, value);
+#endif
+  }
+  // Exclusive prefix sum of `value` in team_rank order.  With global_accum,
+  // the last thread adds the team's total to *global_accum atomically and
+  // every thread's result is offset by the value it held before
+  // (Kokkos_Cuda_Team.hpp:223-262; the order of teams is unspecified).
+  template <class T>
+  KOKKOS_INLINE_FUNCTION T team_scan(const T& value, T* global_accum) const {
+#ifdef __CUDA_ARCH__
+    return Impl::team_exclusive_sum(value, global_accum);
+#else
+    (void)value;
+    (void)global_accum;
+    return T();
+#endif
+  }
+  template <class T>
+  KOKKOS_INLINE_FUNCTION T team_scan(const T& value) const {
+    return team_scan<T>(value, nullptr);
   }
 
  private:

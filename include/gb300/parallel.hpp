@@ -336,6 +336,15 @@ __device__ V team_allreduce(const Red& red, V v) {
   __syncthreads();
   return v;
 }
+// Every thread receives the root thread's value.
+template <class T>
+__device__ void team_bcast(T& v, int root) {
+  __shared__ __align__(16) unsigned char raw[sizeof(T)];
+  __syncthreads();  // earlier readers of raw are done
+  if ((int)threadIdx.x == root) *reinterpret_cast<T*>(raw) = v;
+  __syncthreads();
+  v = *reinterpret_cast<T*>(raw);
+}
 template <class T>
 struct DevSum {
   using value_type = T;
@@ -375,11 +384,20 @@ template <class F>
 KOKKOS_INLINE_FUNCTION void parallel_for(const ThreadVectorRangeBoundaries& r, const F& f) {
   for (int64_t i = r.begin; i < r.end; ++i) f(i);
 }
-template <class F, class T>
+template <class F, class T, std::enable_if_t<!Impl::is_reducer<T>::value, bool> = true>
 KOKKOS_INLINE_FUNCTION void parallel_reduce(const ThreadVectorRangeBoundaries& r, const F& f, T& result) {
   T v = T(0);
   for (int64_t i = r.begin; i < r.end; ++i) f(i, v);
   result = v;
+}
+template <class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
+KOKKOS_INLINE_FUNCTION void parallel_reduce(const ThreadVectorRangeBoundaries& r, const F& f, const Red& red) {
+#ifdef __CUDA_ARCH__
+  typename Red::value_type v;
+  red.init(v);
+  for (int64_t i = r.begin; i < r.end; ++i) f(i, v);
+  red.reference() = v;
+#endif
 }
 
 }  // namespace gb300k

@@ -142,6 +142,127 @@ struct MinMaxLoc : Impl::ReducerBase<MinMaxLoc<T, I, Space>, MinMaxLocScalar<T, 
   }
 };
 
+// Reducers of the std min_element / max_element / minmax_element
+// (Kokkos_Parallel_Reduce.hpp:679-1100): equal values keep the smaller loc,
+// except the max of MinMaxFirstLastLoc, which keeps the larger (std
+// minmax_element returns the last largest element).  Comp(a, b) = "a is
+// less than b" (std::less by default); the reducer's identity is an empty
+// record (loc = the index type's maximum, or minimum for the last-loc max),
+// joined by loc only when the values are equivalent.
+namespace Impl {
+struct Less {
+  template <class T>
+  __host__ __device__ bool operator()(const T& a, const T& b) const { return a < b; }
+};
+}  // namespace Impl
+
+template <class T, class I = int64_t, class Comp = Impl::Less, class Space = GB300Space>
+struct MinFirstLocCustomComparator : Impl::ReducerBase<MinFirstLocCustomComparator<T, I, Comp, Space>, ValLocScalar<T, I>> {
+  using V = ValLocScalar<T, I>;
+  using reducer = MinFirstLocCustomComparator;
+  using value_type = V;
+  Comp comp;
+  __host__ __device__ MinFirstLocCustomComparator(V& r, Comp c = Comp()) : Impl::ReducerBase<MinFirstLocCustomComparator, V>(r), comp(c) {}
+  template <class D, class... P>
+  MinFirstLocCustomComparator(const View<D, P...>& v, Comp c = Comp()) : Impl::ReducerBase<MinFirstLocCustomComparator, V>(v), comp(c) {}
+  __device__ void init(V& v) const { v.val = gbk::lim<T>::hi(); v.loc = Impl::loc_identity<I>(); }
+  __device__ void join(V& a, const V& b) const {
+    if (b.loc == Impl::loc_identity<I>()) return;
+    if (a.loc == Impl::loc_identity<I>() || comp(b.val, a.val)) { a = b; return; }
+    if (!comp(a.val, b.val) && b.loc < a.loc) a.loc = b.loc;
+  }
+};
+template <class T, class I = int64_t, class Comp = Impl::Less, class Space = GB300Space>
+struct MaxFirstLocCustomComparator : Impl::ReducerBase<MaxFirstLocCustomComparator<T, I, Comp, Space>, ValLocScalar<T, I>> {
+  using V = ValLocScalar<T, I>;
+  using reducer = MaxFirstLocCustomComparator;
+  using value_type = V;
+  Comp comp;
+  __host__ __device__ MaxFirstLocCustomComparator(V& r, Comp c = Comp()) : Impl::ReducerBase<MaxFirstLocCustomComparator, V>(r), comp(c) {}
+  template <class D, class... P>
+  MaxFirstLocCustomComparator(const View<D, P...>& v, Comp c = Comp()) : Impl::ReducerBase<MaxFirstLocCustomComparator, V>(v), comp(c) {}
+  __device__ void init(V& v) const { v.val = gbk::lim<T>::lo(); v.loc = Impl::loc_identity<I>(); }
+  __device__ void join(V& a, const V& b) const {
+    if (b.loc == Impl::loc_identity<I>()) return;
+    if (a.loc == Impl::loc_identity<I>() || comp(a.val, b.val)) { a = b; return; }
+    if (!comp(b.val, a.val) && b.loc < a.loc) a.loc = b.loc;
+  }
+};
+template <class T, class I = int64_t, class Comp = Impl::Less, class Space = GB300Space>
+struct MinMaxFirstLastLocCustomComparator
+    : Impl::ReducerBase<MinMaxFirstLastLocCustomComparator<T, I, Comp, Space>, MinMaxLocScalar<T, I>> {
+  using V = MinMaxLocScalar<T, I>;
+  using reducer = MinMaxFirstLastLocCustomComparator;
+  using value_type = V;
+  Comp comp;
+  __host__ __device__ MinMaxFirstLastLocCustomComparator(V& r, Comp c = Comp())
+      : Impl::ReducerBase<MinMaxFirstLastLocCustomComparator, V>(r), comp(c) {}
+  template <class D, class... P>
+  MinMaxFirstLastLocCustomComparator(const View<D, P...>& v, Comp c = Comp())
+      : Impl::ReducerBase<MinMaxFirstLastLocCustomComparator, V>(v), comp(c) {}
+  __device__ void init(V& v) const {
+    v.min_val = gbk::lim<T>::hi();
+    v.max_val = gbk::lim<T>::lo();
+    v.min_loc = Impl::loc_identity<I>();
+    v.max_loc = gbk::lim<I>::lo();
+  }
+  __device__ void join(V& a, const V& b) const {
+    if (b.min_loc != Impl::loc_identity<I>()) {
+      if (a.min_loc == Impl::loc_identity<I>() || comp(b.min_val, a.min_val)) {
+        a.min_val = b.min_val;
+        a.min_loc = b.min_loc;
+      } else if (!comp(a.min_val, b.min_val) && b.min_loc < a.min_loc) {
+        a.min_loc = b.min_loc;
+      }
+    }
+    if (b.max_loc != gbk::lim<I>::lo()) {
+      if (a.max_loc == gbk::lim<I>::lo() || comp(a.max_val, b.max_val)) {
+        a.max_val = b.max_val;
+        a.max_loc = b.max_loc;
+      } else if (!comp(b.max_val, a.max_val) && b.max_loc > a.max_loc) {
+        a.max_loc = b.max_loc;
+      }
+    }
+  }
+};
+template <class T, class I = int64_t, class Space = GB300Space>
+using MinFirstLoc = MinFirstLocCustomComparator<T, I, Impl::Less, Space>;
+template <class T, class I = int64_t, class Space = GB300Space>
+using MaxFirstLoc = MaxFirstLocCustomComparator<T, I, Impl::Less, Space>;
+template <class T, class I = int64_t, class Space = GB300Space>
+using MinMaxFirstLastLoc = MinMaxFirstLastLocCustomComparator<T, I, Impl::Less, Space>;
+
+namespace Impl {
+// A custom joiner with no neutral element (std transform_reduce / reduce with
+// a user joiner): the value carries a "has a value" flag, the identity is an
+// empty value, and join applies the joiner only to two non-empty values
+// (the reference's ReducerWithArbitraryJoinerNoNeutralElement).
+template <class T>
+struct Opt {
+  T val;
+  int has;
+};
+template <class T, class Op>
+struct OptJoin : ReducerBase<OptJoin<T, Op>, Opt<T>> {
+  using reducer = OptJoin;
+  using value_type = Opt<T>;
+  Op op;
+  OptJoin(Opt<T>& r, Op o) : ReducerBase<OptJoin, Opt<T>>(r), op(o) {}
+  __device__ void init(Opt<T>& v) const {
+    v.val = T();
+    v.has = 0;
+  }
+  __device__ void join(Opt<T>& a, const Opt<T>& b) const {
+    if (!b.has) return;
+    if (!a.has) {
+      a = b;
+      return;
+    }
+    a.val = op(a.val, b.val);
+  }
+};
+}  // namespace Impl
+
 namespace Impl {
 // Is R a reducer class (has a nested `reducer` type)?
 template <class R, class = void> struct is_reducer : std::false_type {};

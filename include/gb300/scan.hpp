@@ -71,8 +71,58 @@ __device__ V warp_excl_scan(V v, V* total) {
   return inc - v;
 }
 
-template <class F, class V, int ITEMS>
-__global__ void __launch_bounds__(kBlock) k_range_scan(F f, int64_t b, int64_t n, HdrScan<V> S, V* total) {
+// The scan's join: zero() and add(a, b) with a before b in index order
+// (no commutativity assumed).  PlusJ is the functor-update default.
+template <class V>
+struct PlusJ {
+  __device__ V zero() const { return V(0); }
+  __device__ V add(const V& a, const V& b) const { return a + b; }
+};
+
+template <class V>
+__device__ __forceinline__ V shfl_up_any(const V& v, int d) {
+  V o;
+  const unsigned* s = reinterpret_cast<const unsigned*>(&v);
+  unsigned* dd = reinterpret_cast<unsigned*>(&o);
+#pragma unroll
+  for (int w = 0; w < (int)(sizeof(V) / 4); ++w) dd[w] = __shfl_up_sync(0xffffffffu, s[w], d);
+  return o;
+}
+template <class V>
+__device__ __forceinline__ V shfl_down_any(const V& v, int d) {
+  V o;
+  const unsigned* s = reinterpret_cast<const unsigned*>(&v);
+  unsigned* dd = reinterpret_cast<unsigned*>(&o);
+#pragma unroll
+  for (int w = 0; w < (int)(sizeof(V) / 4); ++w) dd[w] = __shfl_down_sync(0xffffffffu, s[w], d);
+  return o;
+}
+template <class V>
+__device__ __forceinline__ V shfl_idx_any(const V& v, int l) {
+  V o;
+  const unsigned* s = reinterpret_cast<const unsigned*>(&v);
+  unsigned* dd = reinterpret_cast<unsigned*>(&o);
+#pragma unroll
+  for (int w = 0; w < (int)(sizeof(V) / 4); ++w) dd[w] = __shfl_sync(0xffffffffu, s[w], l);
+  return o;
+}
+// Ordered warp scan: exclusive prefix of v over lower lanes, warp total.
+template <class V, class J>
+__device__ V warp_excl_scan_j(const J& j, V v, V* total) {
+  const int lane = threadIdx.x & 31;
+  V inc = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const V o = shfl_up_any(inc, d);
+    if (lane >= d) inc = j.add(o, inc);
+  }
+  *total = shfl_idx_any(inc, 31);
+  const V ex = shfl_up_any(inc, 1);
+  return lane == 0 ? j.zero() : ex;
+}
+
+template <class F, class V, int ITEMS, class J>
+__global__ void __launch_bounds__(kBlock) k_range_scan(F f, J j, int64_t b, int64_t n, HdrScan<V> S, V* total) {
   constexpr int TILE = kBlock * ITEMS;
   constexpr int WARPS = kBlock / 32;
   __shared__ int64_t s_tile;
@@ -88,20 +138,20 @@ __global__ void __launch_bounds__(kBlock) k_range_scan(F f, int64_t b, int64_t n
   const int64_t tile = s_tile;
   const int64_t i0 = tile * TILE + (int64_t)threadIdx.x * ITEMS;
   const int64_t i1 = i0 + ITEMS < n ? i0 + ITEMS : n;
-  V part = V(0);
+  V part = j.zero();
   for (int64_t i = i0; i < i1; ++i) f(b + i, part, false);
   V wtot;
-  const V wex = warp_excl_scan(part, &wtot);
+  const V wex = warp_excl_scan_j(j, part, &wtot);
   if (lane == 0) s_w[warp] = wtot;
   __syncthreads();
-  V wpre = V(0), agg = V(0);
+  V wpre = j.zero(), agg = j.zero();
 #pragma unroll
   for (int w = 0; w < WARPS; ++w) {
     if (w == warp) wpre = agg;
-    agg = agg + s_w[w];
+    agg = j.add(agg, s_w[w]);
   }
   if (warp == 0) {
-    V excl = V(0);
+    V excl = j.zero();
     if (tile == 0) {
       if (lane == 0) {
         S.incl[0] = agg;
@@ -117,7 +167,7 @@ __global__ void __launch_bounds__(kBlock) k_range_scan(F f, int64_t b, int64_t n
       while (true) {
         const int64_t pt = pt0 - lane;
         unsigned fl = 2u;
-        V val = V(0);
+        V val = j.zero();
         if (pt >= 0) {
           int64_t polls = 0;
           while ((fl = gbk::ld_acquire_u32(S.flags + pt)) == 0u) {
@@ -129,23 +179,21 @@ __global__ void __launch_bounds__(kBlock) k_range_scan(F f, int64_t b, int64_t n
         gave_up = __any_sync(0xffffffffu, gave_up);
         const unsigned pm = __ballot_sync(0xffffffffu, fl == 2u);
         const int last = pm ? __ffs(pm) - 1 : 31;
-        V c = lane <= last ? val : V(0);
+        // lane l holds tile pt0 - l: fold from the farthest tile to the
+        // nearest (lane 0 ends with the window's ordered total)
+        V c = lane <= last ? val : j.zero();
 #pragma unroll
-        for (int m = 16; m >= 1; m >>= 1) {
-          V o;
-          const unsigned* s = reinterpret_cast<const unsigned*>(&c);
-          unsigned* dd = reinterpret_cast<unsigned*>(&o);
-#pragma unroll
-          for (int w = 0; w < (int)(sizeof(V) / 4); ++w) dd[w] = __shfl_xor_sync(0xffffffffu, s[w], m);
-          c = c + o;
+        for (int m = 1; m < 32; m <<= 1) {
+          const V o = shfl_down_any(c, m);
+          if (lane + m < 32) c = j.add(o, c);
         }
-        excl = excl + c;
+        excl = j.add(c, excl);
         if (pm) break;
         pt0 -= 32;
       }
       if (lane == 0) {
         if (gave_up) atomicOr(S.err, 1);
-        S.incl[tile] = excl + agg;
+        S.incl[tile] = j.add(excl, agg);
         gbk::st_release_u32(S.flags + tile, 2u);
       }
     }
@@ -153,22 +201,22 @@ __global__ void __launch_bounds__(kBlock) k_range_scan(F f, int64_t b, int64_t n
   }
   __syncthreads();
   const V tpre = s_pre;
-  if (total && tile == S.ntiles - 1 && threadIdx.x == 0) *total = tpre + agg;
-  V up = tpre + wpre + wex;
+  if (total && tile == S.ntiles - 1 && threadIdx.x == 0) *total = j.add(tpre, agg);
+  V up = j.add(j.add(tpre, wpre), wex);
   for (int64_t i = i0; i < i1; ++i) f(b + i, up, true);
 }
 
 }  // namespace Impl
 
-template <class V, class P, class F>
-void parallel_scan_impl(const P& p, const F& f, V* host_total) {
+template <class V, class P, class F, class J = Impl::PlusJ<V>>
+void parallel_scan_impl(const P& p, const F& f, V* host_total, J j = J()) {
   static_assert(sizeof(V) % 4 == 0, "scan value size must be a multiple of 4 bytes");
   constexpr int ITEMS = 8;
   constexpr int64_t TILE = Impl::kBlock * ITEMS;
   const int64_t n = p.end() - p.begin();
   cudaStream_t s = p.space().stream();
   if (n <= 0) {
-    if (host_total) *host_total = V(0);
+    if (host_total) *host_total = V{};
     return;
   }
   const int64_t nt = (n + TILE - 1) / TILE;
@@ -184,7 +232,7 @@ void parallel_scan_impl(const P& p, const F& f, V* host_total) {
   S.wait_limit = int64_t(1) << 22;
   check_cuda(cudaMemsetAsync(S.flags, 0, (size_t)nt * 4, s), "parallel_scan");
   V* dtot = host_total ? reinterpret_cast<V*>(sc.base) : nullptr;
-  Impl::k_range_scan<F, V, ITEMS><<<(unsigned)nt, Impl::kBlock, 0, s>>>(f, p.begin(), n, S, dtot);
+  Impl::k_range_scan<F, V, ITEMS, J><<<(unsigned)nt, Impl::kBlock, 0, s>>>(f, j, p.begin(), n, S, dtot);
   Impl::launched(cudaGetLastError(), "parallel_scan");
   if (host_total) {
     check_cuda(cudaMemcpyAsync(host_total, dtot, sizeof(V), cudaMemcpyDeviceToHost, s), "parallel_scan");
@@ -246,5 +294,51 @@ KOKKOS_INLINE_FUNCTION void parallel_scan(const TeamThreadRangeBoundaries<>& r, 
   for (int64_t i = a; i < e; ++i) f(i, up, true);
 #endif
 }
+
+// Scan over a ThreadVectorRange: vector length 1, so the thread calls the
+// functor in index order with final = true.
+template <class F>
+KOKKOS_INLINE_FUNCTION void parallel_scan(const ThreadVectorRangeBoundaries& r, const F& f) {
+  using T = Impl::scan_value_t<F>;
+  T v = T(0);
+  for (int64_t i = r.begin; i < r.end; ++i) f(i, v, true);
+}
+
+namespace Impl {
+template <class T>
+__device__ T atomic_add_old(T* p, T v) {
+  if constexpr (std::is_integral<T>::value && sizeof(T) == 8)
+    return (T)atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+  else if constexpr (std::is_integral<T>::value && sizeof(T) == 4)
+    return (T)atomicAdd(reinterpret_cast<unsigned*>(p), (unsigned)v);
+  else
+    return atomicAdd(p, v);  // float, double
+}
+// TeamMember::team_scan: exclusive prefix sum in team_rank order, offset by
+// the old *global_accum when given (the last thread adds the team total).
+template <class T>
+__device__ T team_exclusive_sum(const T& v, T* global_accum) {
+  __shared__ __align__(16) unsigned char raw[33 * sizeof(T)];
+  T* sm = reinterpret_cast<T*>(raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  T wtot;
+  const T wex = warp_excl_scan(v, &wtot);
+  __syncthreads();  // earlier readers of sm are done
+  if (lane == 0) sm[warp] = wtot;
+  __syncthreads();
+  T wpre = T(0), tot = T(0);
+  for (int w = 0; w < nw; ++w) {
+    if (w < warp) wpre = wpre + sm[w];
+    tot = tot + sm[w];
+  }
+  T base = T(0);
+  if (global_accum) {
+    if ((int)threadIdx.x == (int)blockDim.x - 1) sm[32] = atomic_add_old(global_accum, tot);
+    __syncthreads();
+    base = sm[32];
+  }
+  return base + wpre + wex;
+}
+}  // namespace Impl
 
 }  // namespace gb300k

@@ -115,6 +115,12 @@ int gbk_deep_copy(void* dst, const void* src, int64_t bytes, gbk_stream_t stream
 /* deep_copy(view, value) for a byte value (e.g. zeroing bins before a
  * ScatterView contribution). */
 int gbk_memset(void* dst, int value, int64_t bytes, gbk_stream_t stream);
+/* deep_copy(view, value) for a contiguous device view of n elements of
+ * elem_bytes (1, 2, 4, 8 or 16) bytes: every element becomes *value (a host
+ * pointer to one element).  dst must be aligned to elem_bytes
+ * (core/src/Kokkos_CopyViews.hpp:897 deep_copy(const View&, value_type) and
+ * its ViewFill functors, Kokkos_CopyViews.hpp:58-260). */
+int gbk_fill(void* dst, const void* value, int elem_bytes, int64_t n, gbk_stream_t stream);
 
 /* ---- reduce over a RangePolicy of a contiguous array -------------------- */
 /* parallel_reduce(RangePolicy(0,n), [=](i, v){ v op= x[i]; }, Reducer(r))

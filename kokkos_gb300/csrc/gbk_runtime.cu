@@ -129,6 +129,33 @@ unsigned* ws_flags(Workspace* w, size_t count, unsigned* epoch, int* status) {
 
 }  // namespace gbk
 
+namespace gbk {
+namespace {
+// deep_copy(view, value): 16-byte streaming stores of a pattern that repeats
+// the value (its size divides 16, so every aligned vector holds whole
+// values in phase); grid-stride over the vectors.
+__global__ void k_fill16(uint4* __restrict__ d, int64_t nvec, uint4 pat) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nvec; i += stride) __stcs(d + i, pat);
+}
+// The elements before the first and after the last whole vector: element e
+// of [0, nhead) at head, of [nhead, nhead + ntail) at tail.
+__global__ void k_fill_edges(unsigned char* head, int64_t nhead, unsigned char* tail, int64_t ntail, int eb,
+                             uint4 pat) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nhead + ntail) return;
+  unsigned char* p = e < nhead ? head + e * eb : tail + (e - nhead) * eb;
+  const unsigned char* v = reinterpret_cast<const unsigned char*>(&pat);
+  switch (eb) {
+    case 1: *p = v[0]; break;
+    case 2: *reinterpret_cast<unsigned short*>(p) = *reinterpret_cast<const unsigned short*>(v); break;
+    case 4: *reinterpret_cast<unsigned*>(p) = pat.x; break;
+    default: *reinterpret_cast<unsigned long long*>(p) = *reinterpret_cast<const unsigned long long*>(v); break;
+  }
+}
+}  // namespace
+}  // namespace gbk
+
 using namespace gbk;
 
 extern "C" {
@@ -317,6 +344,39 @@ int gbk_memset(void* dst, int value, int64_t bytes, gbk_stream_t stream) {
   if (bytes < 0 || (bytes > 0 && !dst)) return GBK_ERR_INVALID_ARGUMENT;
   if (bytes == 0) return GBK_OK;
   GBK_CUDA_TRY(cudaMemsetAsync(dst, value, (size_t)bytes, (cudaStream_t)stream));
+  return GBK_OK;
+}
+
+int gbk_fill(void* dst, const void* value, int elem_bytes, int64_t n, gbk_stream_t stream) {
+  if (n < 0 || !value || (elem_bytes != 1 && elem_bytes != 2 && elem_bytes != 4 && elem_bytes != 8 && elem_bytes != 16))
+    return GBK_ERR_INVALID_ARGUMENT;
+  if (n == 0) return GBK_OK;
+  if (!dst || (uintptr_t)dst % (uintptr_t)elem_bytes) return GBK_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  uint4 pat;
+  unsigned char* pb = reinterpret_cast<unsigned char*>(&pat);
+  for (int o = 0; o < 16; o += elem_bytes) std::memcpy(pb + o, value, (size_t)elem_bytes);
+  unsigned char* d = (unsigned char*)dst;
+  int64_t nhead = (int64_t)(((16 - ((uintptr_t)d & 15)) & 15) / (uintptr_t)elem_bytes);
+  if (nhead > n) nhead = n;
+  const int64_t body_bytes = (n - nhead) * elem_bytes;
+  const int64_t nvec = body_bytes / 16;
+  const int64_t ntail = (body_bytes - nvec * 16) / elem_bytes;
+  unsigned char* body = d + nhead * elem_bytes;
+  if (nvec > 0) {
+    int64_t grid = (nvec + 255) / 256;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    if (grid > cap) grid = cap;
+    k_fill16<<<(unsigned)grid, 256, 0, s>>>(reinterpret_cast<uint4*>(body), nvec, pat);
+    note_launch();
+    GBK_CUDA_TRY(cudaGetLastError());
+  }
+  if (nhead + ntail > 0) {
+    k_fill_edges<<<(unsigned)((nhead + ntail + 255) / 256), 256, 0, s>>>(d, nhead, body + nvec * 16, ntail,
+                                                                          elem_bytes, pat);
+    note_launch();
+    GBK_CUDA_TRY(cudaGetLastError());
+  }
   return GBK_OK;
 }
 

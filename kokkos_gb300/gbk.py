@@ -55,6 +55,7 @@ _SIGS = {
     "gbk_launch_count": ([], i64),
     "gbk_deep_copy": ([vp, vp, i64, vp], ci),
     "gbk_memset": ([vp, ci, i64, vp], ci),
+    "gbk_fill": ([vp, vp, ci, i64, vp], ci),
     "gbk_reduce": ([ci, ci, vp, i64, vp, vp, TP], ci),
     "gbk_reduce_host": ([ci, ci, vp, i64, vp, vp, TP], ci),
     "gbk_mdrange_reduce": ([ci, ci, vp, ci, vp, vp, vp, vp, vp, TP], ci),
@@ -280,6 +281,16 @@ def binsort(keys, nbins, kmin, mul, sort_within_bins=False, stream=None):
                               ctypes.c_void_p(offs.data_ptr()), ctypes.c_void_p(perm.data_ptr()), _stream(stream)),
           "binsort")
     return counts, offs, perm
+
+
+def fill(dst, value, stream=None):
+    """deep_copy(view, value) on a contiguous device tensor: the value is
+    converted to the tensor's dtype on the host and its bytes replicated."""
+    import torch
+    v = np.ascontiguousarray(torch.tensor([value], dtype=dst.dtype).numpy())
+    check(lib.gbk_fill(ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(v.ctypes.data), dst.element_size(), dst.numel(),
+                       _stream(stream)), "fill")
+    return dst
 
 
 def permute(src, perm, stream=None):

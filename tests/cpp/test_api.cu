@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <limits>
 #include <numeric>
 #include <vector>
 
@@ -360,6 +361,228 @@ static void test_std_algorithms() {
   report(ok, "std_inclusive_scan_i32");
 }
 
+static void test_team_collectives() {
+  // TestTeamScan.hpp / TestTeamReductionScan.hpp style: member team_reduce
+  // (Sum and MaxLoc), team_scan with and without a global accumulator,
+  // team_broadcast
+  using TP = Kokkos::TeamPolicy<>;
+  const int64_t league = 300;
+  const int ts = 128;
+  Kokkos::View<int64_t*> red("red", league), mloc("mloc", league), scan("scan", league * ts),
+      gscan("gscan", league * ts), bc("bc", league * ts), gacc("gacc", 1);
+  Kokkos::parallel_for(TP(league, ts), KOKKOS_LAMBDA(const TP::member_type& t) {
+    const int64_t lr = t.league_rank();
+    const int r = t.team_rank();
+    const int64_t v = (lr * 7 + r * 3) % 11;
+    int64_t s = v;
+    t.team_reduce(Kokkos::Sum<int64_t>(s));
+    Kokkos::ValLocScalar<int64_t, int> vl{v, r};
+    t.team_reduce(Kokkos::MaxLoc<int64_t, int>(vl));
+    if (r == 0) {
+      red(lr) = s;
+      mloc(lr) = vl.loc;
+    }
+    scan(lr * ts + r) = t.team_scan(v);
+    gscan(lr * ts + r) = t.team_scan(v, &gacc(0));
+    int64_t b = r * 10 + lr;
+    t.team_broadcast(b, 5);
+    bc(lr * ts + r) = b;
+  });
+  auto hred = to_host(red), hml = to_host(mloc), hs = to_host(scan), hg = to_host(gscan), hb = to_host(bc),
+       ha = to_host(gacc);
+  bool ok_red = true, ok_ml = true, ok_scan = true, ok_bc = true, ok_g = true;
+  int64_t total = 0;
+  std::vector<std::pair<int64_t, int64_t>> bases;  // (global base, team total) per team
+  for (int64_t lr = 0; lr < league; ++lr) {
+    int64_t run = 0, best = -1, bl = 0;
+    for (int r = 0; r < ts; ++r) {
+      const int64_t v = (lr * 7 + r * 3) % 11;
+      ok_scan = ok_scan && hs[lr * ts + r] == run;
+      ok_bc = ok_bc && hb[lr * ts + r] == 50 + lr;
+      // global: the team's base plus the in-team exclusive prefix
+      ok_g = ok_g && hg[lr * ts + r] - hg[lr * ts] == run;
+      if (v > best) { best = v; bl = r; }
+      run += v;
+    }
+    ok_red = ok_red && hred[lr] == run;
+    ok_ml = ok_ml && hml[lr] == bl;
+    total += run;
+    bases.push_back({hg[lr * ts], run});
+  }
+  // the team bases are the exclusive prefix of the team totals in some order
+  std::sort(bases.begin(), bases.end());
+  int64_t acc = 0;
+  for (auto& p : bases) { ok_g = ok_g && p.first == acc; acc += p.second; }
+  report(ok_red, "team_reduce_sum");
+  report(ok_ml, "team_reduce_maxloc_first");
+  report(ok_scan, "team_scan_exclusive");
+  report(ok_g && ha[0] == total, "team_scan_global_accum");
+  report(ok_bc, "team_broadcast");
+}
+
+static void test_std_more() {
+  // TestStdAlgorithmsMinMaxElementOps.cpp / TestStdAlgorithmsTransformReduce /
+  // TestStdAlgorithmsTransform{Inclusive,Exclusive}Scan style: host std:: results
+  namespace KE = Kokkos::Experimental;
+  KE::GB300 ex;
+  Rng r{21};
+  const int64_t n = (1 << 20) + 3;
+  std::vector<int32_t> x(n);
+  for (auto& v : x) v = (int32_t)(r.next() % 1000) - 500;
+  std::vector<float> f(n);
+  for (auto& v : f) v = (float)((int)(r.next() % 200) - 100);
+  auto dx = to_device(x);
+  auto df = to_device(f);
+  const int64_t imin = KE::min_element(ex, KE::cbegin(dx), KE::cend(dx)) - KE::cbegin(dx);
+  const int64_t imax = KE::max_element(ex, KE::cbegin(dx), KE::cend(dx)) - KE::cbegin(dx);
+  report(imin == std::min_element(x.begin(), x.end()) - x.begin(), "std_min_element_first");
+  report(imax == std::max_element(x.begin(), x.end()) - x.begin(), "std_max_element_first");
+  auto absless = KOKKOS_LAMBDA(float a, float b) { return (a < 0 ? -a : a) < (b < 0 ? -b : b); };
+  auto habsless = [](float a, float b) { return std::fabs(a) < std::fabs(b); };
+  const int64_t cmin = KE::min_element(ex, KE::cbegin(df), KE::cend(df), absless) - KE::cbegin(df);
+  report(cmin == std::min_element(f.begin(), f.end(), habsless) - f.begin(), "std_min_element_comparator");
+  auto mm = KE::minmax_element(ex, KE::cbegin(dx), KE::cend(dx));
+  auto hmm = std::minmax_element(x.begin(), x.end());
+  report(mm.first - KE::cbegin(dx) == hmm.first - x.begin() && mm.second - KE::cbegin(dx) == hmm.second - x.begin(),
+         "std_minmax_element_first_min_last_max");
+  auto mmc = KE::minmax_element(ex, KE::cbegin(df), KE::cend(df), absless);
+  auto hmmc = std::minmax_element(f.begin(), f.end(), habsless);
+  report(mmc.first - KE::cbegin(df) == hmmc.first - f.begin() && mmc.second - KE::cbegin(df) == hmmc.second - f.begin(),
+         "std_minmax_element_comparator");
+  // transform_reduce: sum of squares (unary), dot product (binary default), max of products (custom)
+  std::vector<int64_t> y(n);
+  for (auto& v : y) v = (int64_t)(r.next() % 64) - 32;
+  auto dy = to_device(y);
+  auto plus = KOKKOS_LAMBDA(int64_t a, int64_t b) { return a + b; };
+  auto sq = KOKKOS_LAMBDA(int32_t a) { return (int64_t)a * a; };
+  int64_t hsq = 11, hdot = -5, hmx = std::numeric_limits<int64_t>::min();
+  for (int64_t i = 0; i < n; ++i) {
+    hsq += (int64_t)x[i] * x[i];
+    hdot += (int64_t)x[i] * y[i];
+    hmx = std::max(hmx, (int64_t)x[i] * y[i]);
+  }
+  report(KE::transform_reduce(ex, KE::cbegin(dx), KE::cend(dx), (int64_t)11, plus, sq) == hsq,
+         "std_transform_reduce_unary");
+  report(KE::transform_reduce(ex, KE::cbegin(dx), KE::cend(dx), KE::cbegin(dy), (int64_t)-5) == hdot,
+         "std_transform_reduce_dot");
+  auto mx = KOKKOS_LAMBDA(int64_t a, int64_t b) { return a > b ? a : b; };
+  auto mul = KOKKOS_LAMBDA(int32_t a, int64_t b) { return (int64_t)a * b; };
+  report(KE::transform_reduce(ex, KE::cbegin(dx), KE::cend(dx), KE::cbegin(dy), std::numeric_limits<int64_t>::min(),
+                              mx, mul) == hmx,
+         "std_transform_reduce_binary_custom");
+  report(KE::reduce(ex, KE::cbegin(dy), KE::cend(dy), (int64_t)-1000, mx) ==
+             *std::max_element(y.begin(), y.end()),
+         "std_reduce_custom_joiner");
+  // scans with a binary op: transform_exclusive_scan (plus, x*2, init 5), transform_inclusive_scan
+  // with init, inclusive_scan with max (running maximum)
+  Kokkos::View<int64_t*> o1("o1", n), o2("o2", n), o3("o3", n);
+  auto dbl = KOKKOS_LAMBDA(int32_t a) { return (int64_t)2 * a; };
+  KE::transform_exclusive_scan(ex, KE::cbegin(dx), KE::cend(dx), KE::begin(o1), (int64_t)5, plus, dbl);
+  KE::transform_inclusive_scan(ex, KE::cbegin(dx), KE::cend(dx), KE::begin(o2), plus, dbl, (int64_t)-7);
+  KE::inclusive_scan(ex, KE::cbegin(dy), KE::cend(dy), KE::begin(o3), mx);
+  auto h1 = to_host(o1), h2 = to_host(o2), h3 = to_host(o3);
+  bool ok1 = h1[0] == 5, ok2 = true, ok3 = true;
+  int64_t ex1 = 0, in2 = 0, rm = std::numeric_limits<int64_t>::min();
+  for (int64_t i = 0; i < n; ++i) {
+    if (i > 0) ok1 = ok1 && h1[i] == ex1 + 5;
+    ex1 += 2 * (int64_t)x[i];
+    in2 += 2 * (int64_t)x[i];
+    ok2 = ok2 && h2[i] == in2 - 7;
+    rm = std::max(rm, y[i]);
+    ok3 = ok3 && h3[i] == rm;
+  }
+  report(ok1, "std_transform_exclusive_scan");
+  report(ok2, "std_transform_inclusive_scan_init");
+  report(ok3, "std_inclusive_scan_custom_op");
+}
+
+static void test_unordered_map() {
+  // TestUnorderedMap.hpp / TestBitset.hpp style: inserts with duplicates
+  // (success vs existing counts), find / exists / key_at / value_at,
+  // AtomicAdd accumulation, a full table then rehash, erase, Bitset.
+  const int64_t n = 1 << 20;
+  const uint64_t nkeys = 1 << 18;  // every residue of i * odd mod 2^18 appears 4 times
+  Kokkos::UnorderedMap<uint64_t, int64_t> map((uint32_t)nkeys);
+  Kokkos::View<int64_t*> cnt("cnt", 3);
+  Kokkos::parallel_for(n, KOKKOS_LAMBDA(int64_t i) {
+    const uint64_t r = ((uint64_t)i * 2654435761ull) % nkeys;
+    const auto res = map.insert(r * 7919ull + 13ull, (int64_t)i);
+    Kokkos::atomic_add(&cnt(res.success() ? 0 : res.existing() ? 1 : 2), (int64_t)1);
+  });
+  auto hc = to_host(cnt);
+  report(hc[0] == (int64_t)nkeys && hc[1] == n - (int64_t)nkeys && hc[2] == 0 && map.size() == nkeys &&
+             !map.failed_insert() && map.capacity() >= nkeys,
+         "unordered_map_insert_success_existing");
+  int64_t bad = 0;
+  Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, (int64_t)nkeys), KOKKOS_LAMBDA(int64_t r, int64_t& u) {
+    const uint64_t k = (uint64_t)r * 7919ull + 13ull;
+    const uint32_t idx = map.find(k);
+    const bool ok = map.valid_at(idx) && map.key_at(idx) == k &&
+                    ((uint64_t)map.value_at(idx) * 2654435761ull) % nkeys == (uint64_t)r &&
+                    !map.exists(k + 1);
+    u += ok ? 0 : 1;
+  }, bad);
+  report(bad == 0, "unordered_map_find_exists_values");
+  // AtomicAdd: a histogram of i % 3001 in a map
+  Kokkos::UnorderedMap<int32_t, int64_t> hist(4096);
+  using AddOp = Kokkos::UnorderedMapInsertOpTypes<Kokkos::View<int64_t*>, uint32_t>::AtomicAdd;
+  Kokkos::parallel_for(n, KOKKOS_LAMBDA(int64_t i) { hist.insert((int32_t)(i % 3001), (int64_t)1, AddOp()); });
+  bad = 0;
+  Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, 3001), KOKKOS_LAMBDA(int64_t k, int64_t& u) {
+    const uint32_t idx = hist.find((int32_t)k);
+    const int64_t want = n / 3001 + (k < n % 3001 ? 1 : 0);
+    u += (hist.valid_at(idx) && hist.value_at(idx) == want) ? 0 : 1;
+  }, bad);
+  report(bad == 0 && hist.size() == 3001, "unordered_map_atomic_add");
+  // a set that overflows, then rehash and erase
+  Kokkos::UnorderedMap<uint32_t, void> set(100);
+  const uint32_t cap0 = set.capacity();
+  Kokkos::parallel_for(1000, KOKKOS_LAMBDA(int64_t i) { set.insert((uint32_t)(i * 3 + 1)); });
+  const bool full = set.failed_insert() && set.size() == cap0;
+  const bool grown = set.rehash(2000);
+  set.reset_failed_insert_flag();
+  Kokkos::parallel_for(1000, KOKKOS_LAMBDA(int64_t i) { set.insert((uint32_t)(i * 3 + 1)); });
+  report(full && grown && !set.failed_insert() && set.size() == 1000 && set.capacity() >= 2000,
+         "unordered_set_full_then_rehash");
+  set.begin_erase();
+  Kokkos::parallel_for(1000, KOKKOS_LAMBDA(int64_t i) {
+    if (i % 2 == 0) set.erase((uint32_t)(i * 3 + 1));
+  });
+  set.end_erase();
+  bad = 0;
+  Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, 1000), KOKKOS_LAMBDA(int64_t i, int64_t& u) {
+    u += set.exists((uint32_t)(i * 3 + 1)) == (i % 2 == 1) ? 0 : 1;
+  }, bad);
+  report(bad == 0 && set.size() == 500, "unordered_set_erase");
+  // Bitset
+  const unsigned nb = 1000003;
+  Kokkos::Bitset<> bs(nb);
+  Kokkos::parallel_for((int64_t)nb, KOKKOS_LAMBDA(int64_t i) {
+    if (i % 3 == 0) bs.set((unsigned)i);
+  });
+  const unsigned c3 = bs.count();
+  Kokkos::parallel_for((int64_t)nb, KOKKOS_LAMBDA(int64_t i) {
+    if (i % 6 == 0) bs.reset((unsigned)i);
+  });
+  const unsigned c6 = bs.count();
+  bad = 0;
+  Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, (int64_t)nb), KOKKOS_LAMBDA(int64_t i, int64_t& u) {
+    const bool want = (i % 3 == 0) && (i % 6 != 0);
+    u += bs.test((unsigned)i) == want ? 0 : 1;
+    if (i % 977 == 0) {
+      const auto f = bs.find_any_unset_near((unsigned)i);
+      const auto g = bs.find_any_set_near((unsigned)i);
+      u += (!f.first || !bs.test(f.second)) ? 0 : 1;
+      u += (!g.first || bs.test(g.second)) ? 0 : 1;
+    }
+  }, bad);
+  bs.set();
+  const unsigned call = bs.count();
+  bs.reset();
+  report(c3 == (nb + 2) / 3 && c6 == (nb + 2) / 3 - (nb + 5) / 6 && bad == 0 && call == nb && bs.count() == 0,
+         "bitset_set_reset_count_find");
+}
+
 static void test_graph() {
   // TestGraph.hpp-style: a chain of nodes, submitted more than once
   cudaStream_t st;
@@ -425,6 +648,9 @@ int main(int argc, char** argv) {
     test_scatter();
     test_sorts();
     test_std_algorithms();
+    test_team_collectives();
+    test_std_more();
+    test_unordered_map();
     test_graph();
     test_errors();
   }

@@ -67,3 +67,12 @@ def test_datagen_deterministic_and_blocked():
     lens, sigma = datagen.lognormal_lengths(10000, seed=0)
     assert abs(lens.sum() - (1 << 28)) / (1 << 28) < 0.02 and lens.max() <= (1 << 21) and lens.min() >= 1
     assert abs(np.median(lens) - 2048) / 2048 < 0.1 and 1.5 < sigma < 3.5
+
+
+def test_fill_argument_errors_without_device(gbk):
+    v = ctypes.c_int64(7)
+    assert gbk.lib.gbk_fill(None, ctypes.byref(v), 8, -1, None) == 1
+    assert gbk.lib.gbk_fill(None, ctypes.byref(v), 3, 4, None) == 1  # element size
+    assert gbk.lib.gbk_fill(None, None, 8, 4, None) == 1
+    assert gbk.lib.gbk_fill(ctypes.c_void_p(12), ctypes.byref(v), 8, 4, None) == 1  # misaligned element
+    assert gbk.lib.gbk_fill(None, ctypes.byref(v), 8, 0, None) == 0
