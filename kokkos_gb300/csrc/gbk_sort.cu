@@ -73,10 +73,11 @@ __device__ __forceinline__ void chunk_part(int64_t n, int64_t chunk_keys, int c,
 }
 
 // Lanes of the warp holding the same 8-bit digit d, within the lanes where
-// `ok` holds: eight ballots, one per digit bit.  No shared memory, and the
-// cost does not depend on how the digits repeat.
+// `ok` holds (ALL: every lane): eight ballots, one per digit bit.  No shared
+// memory, and the cost does not depend on how the digits repeat.
+template <bool ALL>
 __device__ __forceinline__ unsigned digit_peers(unsigned d, bool ok) {
-  unsigned m = __ballot_sync(0xffffffffu, ok);
+  unsigned m = ALL ? 0xffffffffu : __ballot_sync(0xffffffffu, ok);
 #pragma unroll
   for (int b = 0; b < 8; ++b) {
     const bool bit = (d >> b) & 1u;
@@ -90,8 +91,9 @@ __device__ __forceinline__ unsigned digit_peers(unsigned d, bool ok) {
 // warp's count of digit d before this row (cnt[d], per warp, shared) plus
 // the lanes below holding d.  The lowest lane of each digit group advances
 // cnt[d].
+template <bool ALL>
 __device__ __forceinline__ unsigned rank_row(unsigned short* cnt, unsigned d, bool ok, int lane) {
-  const unsigned m = digit_peers(d, ok);
+  const unsigned m = digit_peers<ALL>(d, ok);
   const int leader = __ffs(m) - 1;
   unsigned b = 0;
   if (ok && lane == leader) {
@@ -355,24 +357,30 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
     const bool full = cv == TILE;  // every tile but the array's last
     K key[KPT];
     V val[KPT];
-    unsigned char dig[KPT];
-    unsigned short rk[KPT];
+    unsigned dig[KPT];
+    unsigned rk[KPT];
+    if (full) {  // every key of the tile present: no bounds, no validity ballot
 #pragma unroll
-    for (int k = 0; k < KPT; ++k) {
-      const int slot = wb + k * 32 + lane;
-      if (full) {
+      for (int k = 0; k < KPT; ++k) {
+        const int slot = wb + k * 32 + lane;
         key[k] = s_keys[slot];
         if (VB) val[k] = s_vals[slot];
-      } else {
+        dig[k] = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
+      }
+#pragma unroll
+      for (int k = 0; k < KPT; ++k) rk[k] = rank_row<true>(s_cnt[warp], dig[k], true, lane);
+    } else {
+#pragma unroll
+      for (int k = 0; k < KPT; ++k) {
+        const int slot = wb + k * 32 + lane;
         const bool ok = slot < cnt;
         key[k] = slot < cv ? s_keys[slot] : (ok ? kin[base + slot] : K(0));
         if (VB) val[k] = slot < cv ? s_vals[slot] : (ok ? vin[base + slot] : V(0));
+        dig[k] = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
       }
-      dig[k] = (unsigned char)(Radix<DT>::img(key[k]) >> A.shift);
-    }
 #pragma unroll
-    for (int k = 0; k < KPT; ++k)
-      rk[k] = (unsigned short)rank_row(s_cnt[warp], dig[k], full || wb + k * 32 + lane < cnt, lane);
+      for (int k = 0; k < KPT; ++k) rk[k] = rank_row<false>(s_cnt[warp], dig[k], wb + k * 32 + lane < cnt, lane);
+    }
     if (__syncthreads_or(bad)) {  // counts complete and every key read, or a copy never arrived
       failed = j;
       break;
@@ -412,12 +420,21 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
     }
     __syncthreads();
     // ---- reorder the tile by digit, in place ---------------------------------
+    if (full) {
 #pragma unroll
-    for (int k = 0; k < KPT; ++k) {
-      if (full || wb + k * 32 + lane < cnt) {
+      for (int k = 0; k < KPT; ++k) {
         const unsigned r = (unsigned)s_off[warp][dig[k]] + rk[k];
         s_keys[r] = key[k];
         if (VB) s_vals[r] = val[k];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < KPT; ++k) {
+        if (wb + k * 32 + lane < cnt) {
+          const unsigned r = (unsigned)s_off[warp][dig[k]] + rk[k];
+          s_keys[r] = key[k];
+          if (VB) s_vals[r] = val[k];
+        }
       }
     }
     __syncthreads();
