@@ -61,7 +61,7 @@ int64_t wait_limit();
 void note_launch(int64_t k = 1);
 int cuda_status(cudaError_t e);
 // Counter slots
-enum { SLOT_REDUCE = 0, SLOT_SCAN_TILE = 1, SLOT_MISC = 2, SLOT_SEG = 3, SLOT_SORT = 8 };
+enum { SLOT_REDUCE = 0, SLOT_SCAN_TILE = 1, SLOT_MISC = 2, SLOT_SEG = 3, SLOT_SEGRED = 5, SLOT_SORT = 8 };
 
 // ---------------------------------------------------------------------------
 // dtype mapping

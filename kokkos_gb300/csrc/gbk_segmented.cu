@@ -441,6 +441,330 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
   }
 }
 
+// ---- segmented reduce over contiguous CTA shares -----------------------------
+// One launch with no waits between CTAs (a plain grid, any residency).  CTA b
+// owns a contiguous, balanced share [a, e) of the elements (whole 16-byte
+// vectors; the last CTA also the tail) and streams it in 16 KiB chunks by bulk
+// copies through a 4-stage ring, walking the segments in order:
+//  * a chunk that lies inside the current segment (next segment start >= the
+//    chunk's end: the common case when segments are longer than a chunk) is
+//    taken into registers, its stage handed back, and folded into per-thread
+//    accumulators, as the flat reduce does;
+//  * a chunk holding segment starts is cut at them: the current segment's
+//    piece before the first start and the piece after the last start are
+//    folded by the whole CTA (element-striped, masked); every piece between
+//    two starts is a whole segment, folded by one warp (pieces round-robin
+//    over the warps) and written; starts are read from the offsets 256 at a
+//    time;
+//  * a segment that begins and ends inside the CTA is written directly; the
+//    pieces of a segment that crosses a CTA boundary go to two records per
+//    CTA, and the last CTA to finish (one ticket) joins each run of records
+//    of one segment in CTA order and writes it.
+// Empty segments get the identity in a grid-stride pre-pass.  Every join
+// happens in a fixed order, so results are deterministic for a given grid.
+template <class T>
+struct SegRec {
+  int64_t seg;  // < 0: no record
+  T val;
+};
+
+struct SegRedArgs {
+  const int64_t* offsets;
+  int64_t nseg, n, nvec;
+  void* recs;        // SegRec<T>[2 * gridDim.x]
+  unsigned* ticket;  // zero between launches
+  int* err;
+  int64_t wait_limit;
+};
+
+constexpr int SR_BLOCK = 256, SR_CV = 1024, SR_STAGES = 4;
+
+template <class R, class T>
+struct SegRedCta {
+  using V = typename R::V;
+  static constexpr int VEC = 16 / sizeof(T);
+  static constexpr int WARPS = SR_BLOCK / 32;
+  int64_t* s_win;
+  V* s_red0;
+  V* s_red1;
+  int64_t* s_cur;
+  int64_t* s_next;
+  V* s_carry;
+  int* s_started;
+  SegRec<T>* rec_first;
+
+  // A chunk [c0, c1) that holds at least one segment start; get(i) reads
+  // element i.  `acc` (the per-thread partials of the current segment) is
+  // folded into the carry first and reset.
+  template <class Get>
+  __device__ void slow(const Get& get, int64_t c0, int64_t c1, V& acc, T* out, const SegRedArgs& A) const {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const V pend = block_reduce<R, SR_BLOCK>(acc, s_red0);
+    if (tid == 0) R::join(*s_carry, pend);
+    acc = R::init();
+    int64_t kb = *s_cur + 1;  // index of the next start not yet consumed
+    int64_t seg = *s_cur, prev = c0, first_b = c0, last_b = c0, next_start = 0;
+    bool first_window = true;
+    while (true) {
+      __syncthreads();  // earlier readers of s_win are done
+      const int64_t wv = kb + tid <= A.nseg ? A.offsets[kb + tid] : (int64_t)0x7FFFFFFFFFFFFFFFLL;
+      s_win[tid] = wv;
+      const int m = __syncthreads_count(wv < c1);  // offsets are sorted: the first m of the window
+      for (int j = warp; j < m; j += WARPS) {
+        if (first_window && j == 0) continue;  // the first piece: folded by the whole CTA below
+        const int64_t lo = j == 0 ? prev : s_win[j - 1], hi = s_win[j];
+        if (hi <= lo) continue;  // empty segment: identity from the pre-pass
+        V v = R::init();
+        for (int64_t i = lo + lane; i < hi; i += 32) R::template update<true>(v, get(i), 0);
+        v = WarpRed<R>::run(v);
+        if (lane == 0) out[seg + j] = v;  // a whole segment inside this chunk
+      }
+      if (m > 0) {
+        if (first_window) first_b = s_win[0];
+        last_b = s_win[m - 1];
+        prev = last_b;
+      }
+      seg += m;
+      kb += m;
+      first_window = false;
+      if (m < SR_BLOCK) {
+        next_start = s_win[m];
+        break;
+      }
+    }
+    V fp = R::init(), lp = R::init();
+    for (int64_t i = c0 + tid; i < c1; i += SR_BLOCK) {
+      if (i < first_b) R::template update<true>(fp, get(i), 0);
+      else if (i >= last_b) R::template update<true>(lp, get(i), 0);
+    }
+    const V F = block_reduce<R, SR_BLOCK>(fp, s_red0);
+    const V L = block_reduce<R, SR_BLOCK>(lp, s_red1);
+    if (tid == 0) {
+      V tot = *s_carry;
+      R::join(tot, F);
+      if (*s_started) {
+        out[*s_cur] = tot;
+      } else {  // began before this CTA's share: the fix-up joins it
+        rec_first->seg = *s_cur;
+        rec_first->val = tot;
+      }
+      *s_cur = seg;
+      *s_carry = L;
+      *s_started = 1;
+      *s_next = next_start;
+    }
+    __syncthreads();
+  }
+};
+
+template <class T>
+struct SmemGet {
+  const T* s;
+  int64_t c0;
+  __device__ T operator()(int64_t i) const { return s[i - c0]; }
+};
+template <class T>
+struct GlobalGet {
+  const T* x;
+  __device__ T operator()(int64_t i) const { return x[i]; }
+};
+
+template <class R, class T>
+__global__ void __launch_bounds__(SR_BLOCK) k_segred(const T* __restrict__ x, T* __restrict__ out, SegRedArgs A) {
+  using V = typename R::V;
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr unsigned CHUNK_BYTES = (unsigned)SR_CV * 16;
+  constexpr int WARPS = SR_BLOCK / 32;
+  extern __shared__ __align__(128) unsigned char ring[];
+  __shared__ __align__(8) unsigned long long s_bar[SR_STAGES];
+  __shared__ int64_t s_win[SR_BLOCK];
+  __shared__ V s_red0[WARPS], s_red1[WARPS];
+  __shared__ int64_t s_cur, s_next, s_lo, s_hi;
+  __shared__ V s_carry;
+  __shared__ int s_started;
+  __shared__ unsigned s_ticket;
+  SegRec<T>* recs = (SegRec<T>*)A.recs;
+  const int tid = threadIdx.x;
+  const int64_t G = gridDim.x, b = blockIdx.x;
+  const int64_t per = A.nvec / G, rem = A.nvec % G;
+  const int64_t v0 = b * per + (b < rem ? b : rem);
+  const int64_t v1 = v0 + per + (b < rem ? 1 : 0);
+  const int64_t a = v0 * VEC;
+  const int64_t e = b == G - 1 ? A.n : v1 * VEC;
+  const int64_t nchunks = (v1 - v0 + SR_CV - 1) / SR_CV;
+  // Thread 0 only: start the copy of chunk c into its stage.
+  auto fill = [&](int64_t c) {
+    if (c >= nchunks) return;
+    const int st = (int)(c % SR_STAGES);
+    const int64_t cv0 = v0 + c * SR_CV;
+    const int64_t cnt = v1 - cv0 < SR_CV ? v1 - cv0 : SR_CV;
+    mbar_arrive_expect_tx(&s_bar[st], (unsigned)(cnt * 16));
+    bulk_g2s(ring + (size_t)st * CHUNK_BYTES, x + cv0 * VEC, (unsigned)(cnt * 16), &s_bar[st]);
+  };
+  if (tid == 0) {
+#pragma unroll
+    for (int st = 0; st < SR_STAGES; ++st) mbar_init(&s_bar[st], 1);
+    fence_mbar_init();
+    for (int st = 0; st < SR_STAGES; ++st) fill(st);
+    recs[2 * b].seg = -1;
+    recs[2 * b + 1].seg = -1;
+    s_lo = 0;
+    s_hi = A.nseg;
+  }
+  for (int64_t sg = b * SR_BLOCK + tid; sg < A.nseg; sg += G * SR_BLOCK)
+    if (A.offsets[sg] == A.offsets[sg + 1]) out[sg] = R::init();
+  __syncthreads();
+  // The segment of element a: the largest s with offsets[s] <= a
+  // (offsets[0] = 0 <= a < n = offsets[nseg]), by rounds of 256 probes.
+  while (true) {
+    const int64_t lo = s_lo, hi = s_hi;
+    if (hi - lo <= 1) break;
+    const int64_t step = (hi - lo + SR_BLOCK - 1) / SR_BLOCK;
+    const int64_t p = lo + (int64_t)tid * step;
+    const int cnt = __syncthreads_count(p < hi && A.offsets[p] <= a);
+    if (tid == 0) {
+      s_lo = lo + (int64_t)(cnt - 1) * step;
+      const int64_t h2 = lo + (int64_t)cnt * step;
+      s_hi = h2 < hi ? h2 : hi;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    s_cur = s_lo;
+    s_next = A.offsets[s_lo + 1];
+    s_started = A.offsets[s_lo] == a;
+    s_carry = R::init();
+  }
+  __syncthreads();
+  const SegRedCta<R, T> cta{s_win, s_red0, s_red1, &s_cur, &s_next, &s_carry, &s_started, &recs[2 * b]};
+  V acc = R::init();
+  bool bad = false;
+  for (int64_t c = 0; c < nchunks; ++c) {
+    const int st = (int)(c % SR_STAGES);
+    if (!mbar_wait(&s_bar[st], (unsigned)(c / SR_STAGES) & 1u, A.wait_limit)) bad = true;
+    const int64_t cv0 = v0 + c * SR_CV;
+    const int cnt = (int)(v1 - cv0 < SR_CV ? v1 - cv0 : SR_CV);
+    const int64_t c0 = cv0 * VEC, c1 = c0 + (int64_t)cnt * VEC;
+    const unsigned char* stage = ring + (size_t)st * CHUNK_BYTES;
+    if (s_next >= c1) {
+      if (cnt == SR_CV) {
+        Vec16<T> u[SR_CV / SR_BLOCK];
+#pragma unroll
+        for (int k = 0; k < SR_CV / SR_BLOCK; ++k) u[k].u = reinterpret_cast<const uint4*>(stage)[k * SR_BLOCK + tid];
+        __syncthreads();  // stage fully read: refill it
+        if (tid == 0) fill(c + SR_STAGES);
+#pragma unroll
+        for (int k = 0; k < SR_CV / SR_BLOCK; ++k)
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) R::template update<true>(acc, u[k].v[q], 0);
+      } else {
+        for (int i = tid; i < cnt; i += SR_BLOCK) {
+          Vec16<T> u;
+          u.u = reinterpret_cast<const uint4*>(stage)[i];
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) R::template update<true>(acc, u.v[q], 0);
+        }
+        __syncthreads();
+        if (tid == 0) fill(c + SR_STAGES);
+      }
+    } else {
+      cta.slow(SmemGet<T>{reinterpret_cast<const T*>(stage), c0}, c0, c1, acc, out, A);
+      if (tid == 0) fill(c + SR_STAGES);  // slow() ends with a barrier: the stage is fully read
+    }
+  }
+  // The tail after the last whole vector (last CTA).
+  const int64_t t0 = v1 * VEC;
+  if (e > t0) {
+    if (s_next >= e) {
+      if (t0 + tid < e) R::template update<true>(acc, x[t0 + tid], 0);
+    } else {
+      cta.slow(GlobalGet<T>{x}, t0, e, acc, out, A);
+    }
+  }
+  const V tot = block_reduce<R, SR_BLOCK>(acc, s_red0);
+  if (tid == 0) {
+    V cry = s_carry;
+    R::join(cry, tot);
+    if (s_started && s_next == e) {
+      out[s_cur] = cry;  // began and ended inside this share
+    } else {
+      recs[2 * b + 1].seg = s_cur;
+      recs[2 * b + 1].val = cry;
+    }
+    if (bad) atomicOr(A.err, GBK_EBIT_TIMEOUT);
+    __threadfence();
+    s_ticket = atomicAdd(A.ticket, 1u);
+  }
+  __syncthreads();
+  if (s_ticket != (unsigned)(G - 1)) return;
+  // Last CTA: every share has written its records.  Stage them in shared
+  // memory (the ring is idle: every copy has landed), then each record that
+  // ends a run of one segment joins the run in CTA order.
+  __threadfence();
+  const int64_t nr = 2 * G;
+  int64_t* r_seg = reinterpret_cast<int64_t*>(ring);
+  V* r_val = reinterpret_cast<V*>(ring + (size_t)nr * 8);
+  for (int64_t r = tid; r < nr; r += SR_BLOCK) {
+    const volatile SegRec<T>* vr = recs + r;
+    r_seg[r] = vr->seg;
+    r_val[r] = vr->val;
+  }
+  __syncthreads();
+  for (int64_t r = tid; r < nr; r += SR_BLOCK) {
+    const int64_t sg = r_seg[r];
+    if (sg < 0) continue;
+    int64_t q = r + 1;
+    while (q < nr && r_seg[q] < 0) ++q;
+    if (q < nr && r_seg[q] == sg) continue;  // not the run's last record
+    int64_t f = r;
+    for (int64_t p = r - 1; p >= 0; --p) {
+      if (r_seg[p] < 0) continue;
+      if (r_seg[p] != sg) break;
+      f = p;
+    }
+    V v = R::init();
+    for (int64_t p = f; p <= r; ++p)
+      if (r_seg[p] == sg) R::join(v, r_val[p]);
+    out[sg] = v;
+  }
+  if (tid == 0) *A.ticket = 0u;
+}
+
+template <class R, class T>
+int launch_segred(const T* x, T* out, int64_t n, const int64_t* offsets, int64_t nseg, Workspace* w) {
+  constexpr int VEC = 16 / sizeof(T);
+  const int64_t nvec = n / VEC;
+  const int64_t chunks = (nvec + SR_CV - 1) / SR_CV;
+  auto kfn = k_segred<R, T>;
+  constexpr size_t dyn = (size_t)SR_STAGES * SR_CV * 16;
+  static int resident = 0;  // CTAs per SM, per instantiation
+  if (!resident) {
+    GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    int r = 0;
+    GBK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kfn, SR_BLOCK, dyn));
+    resident = r > 0 ? r : 1;
+  }
+  int64_t grid = std::min<int64_t>(chunks, (int64_t)sm_count() * resident);
+  if (grid < 1) grid = 1;
+  // the fix-up stages 2 records per CTA (8 + sizeof(T) bytes each) in the ring
+  if (grid * 2 * (8 + (int64_t)sizeof(T)) > (int64_t)dyn) grid = (int64_t)dyn / (2 * (8 + (int64_t)sizeof(T)));
+  int st = GBK_OK;
+  char* scr = ws_scratch(w, sizeof(SegRec<T>) * 2 * (size_t)grid + 256, &st);
+  if (!scr) return st;
+  SegRedArgs A;
+  A.offsets = offsets;
+  A.nseg = nseg;
+  A.n = n;
+  A.nvec = nvec;
+  A.recs = scr;
+  A.ticket = w->counters + SLOT_SEGRED;
+  A.err = w->err;
+  A.wait_limit = wait_limit();
+  kfn<<<(unsigned)grid, SR_BLOCK, dyn, w->stream>>>(x, out, A);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
 // One cooperative launch (all CTAs co-resident: the grid barriers and the
 // static tile order need it): min(tiles, resident CTAs), or ctas_per_sm x SMs
 // when the tuning asks for fewer.
@@ -514,9 +838,21 @@ int launch_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t ns
   return launch_k_seg<TI, TO, OP, MODE, true, 7, STG>(x, y, n, offsets, nseg, w, cps);
 }
 
+// Variant 0 (default): the contiguous-share kernel for 16-byte aligned input
+// of at least one chunk; variant 1 (or other input): the tile pipeline.
 template <class T>
 int seg_reduce_t(int op, const void* x, const int64_t* offs, int64_t nseg, int64_t n, void* out, Workspace* w,
                  const gbk_tuning_t* t) {
+  const bool shares = (uintptr_t)x % 16 == 0 && n >= (int64_t)SR_CV * (16 / (int64_t)sizeof(T)) &&
+                      !(t && t->variant == 1);
+  if (shares) {
+    switch (op) {
+      case GBK_SUM: return launch_segred<RSum<T>, T>((const T*)x, (T*)out, n, offs, nseg, w);
+      case GBK_MIN: return launch_segred<RMin<T>, T>((const T*)x, (T*)out, n, offs, nseg, w);
+      case GBK_MAX: return launch_segred<RMax<T>, T>((const T*)x, (T*)out, n, offs, nseg, w);
+    }
+    return GBK_ERR_UNSUPPORTED;
+  }
   switch (op) {
     case GBK_SUM: return launch_seg<T, T, GBK_SUM, M_REDUCE>((const T*)x, (T*)out, n, offs, nseg, w, t);
     case GBK_MIN: return launch_seg<T, T, GBK_MIN, M_REDUCE>((const T*)x, (T*)out, n, offs, nseg, w, t);

@@ -233,3 +233,71 @@ def test_graph_chain_of_dependent_nodes(env):
         np.testing.assert_array_equal(res.cpu().numpy(), want[0])
         np.testing.assert_array_equal(bufs[3].cpu().numpy(), want[1])
     gbk.stream_check(s)
+
+
+def share_cases():
+    rng = np.random.default_rng(11)
+    yield "one_segment_with_tail", np.array([(1 << 22) + 3])
+    yield "empty_at_both_ends", np.concatenate([[0, 0, 0], rng.integers(1000, 200000, 40), [0, 0]])
+    # more than 256 starts inside one 4096-element chunk (several windows of starts)
+    yield "tiny_run", np.concatenate([rng.integers(5000, 100000, 20), rng.integers(0, 4, 30000),
+                                      rng.integers(5000, 100000, 20), [7]])
+    yield "random_sizes", rng.integers(0, 20000, 800)
+    yield "chunk_multiples", np.array([4096] * 300 + [1024] * 100 + [24576] * 50 + [0, 4096, 0])
+
+
+def _seg_expect(x, offs, op):
+    lens = np.diff(offs)
+    if op == "sum":
+        cs = np.concatenate([[0], np.cumsum(x.astype(np.int64))])
+        return (cs[offs[1:]] - cs[offs[:-1]]).astype(x.dtype)
+    info = np.iinfo(x.dtype)
+    out = np.full(lens.size, info.max if op == "min" else info.min, dtype=x.dtype)
+    nz = lens > 0
+    f = np.minimum if op == "min" else np.maximum
+    out[nz] = f.reduceat(x, offs[:-1][nz])
+    return out
+
+
+@pytest.mark.parametrize("case", list(share_cases()), ids=lambda c: c[0])
+def test_segmented_reduce_contiguous_shares(env, case):
+    """The contiguous-share segmented reduce (the default for 16-byte aligned
+    input of at least one chunk): segments across share and chunk edges,
+    starts on them, more than 256 starts in one chunk, empty segments at both
+    ends, a tail after the last whole vector, one segment over everything.
+    Integers exact against numpy and against the tile-pipeline variant
+    (variant 1); float and double Sum within the stated tolerances."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    _, lens = case
+    offs = datagen.offsets_from_lengths(np.asarray(lens, dtype=np.int64))
+    n = int(offs[-1])
+    nseg = offs.size - 1
+    do = _dev(torch, offs)
+    xi = datagen.uniform_i32(n, 0, 255, seed=21)
+    xl = datagen.uniform_i64(n, -(1 << 40), 1 << 40, seed=22)
+    for x in (xi, xl):
+        dx = _dev(torch, x)
+        for op in ("sum", "min", "max"):
+            want = _seg_expect(x, offs, op)
+            for variant in (0, 1):
+                o = torch.empty(nseg, dtype=dx.dtype, device="cuda")
+                gbk.segmented_reduce(op, dx, do, o, tune=(256, 7, 0, variant))
+                gbk.stream_check()
+                np.testing.assert_array_equal(o.cpu().numpy(), want, err_msg=f"{x.dtype} {op} variant {variant}")
+    for dt, rel in ((np.float32, 1e-5), (np.float64, 1e-12)):
+        xf = datagen.normal_f64(n, seed=23).astype(dt)
+        o = torch.empty(nseg, dtype=torch.float32 if dt == np.float32 else torch.float64, device="cuda")
+        gbk.segmented_reduce("sum", _dev(torch, xf), do, o)
+        gbk.stream_check()
+        got = o.cpu().numpy()
+        big = [s for s in range(nseg) if offs[s + 1] - offs[s] > 64] + list(range(min(nseg, 50)))
+        for s in big:
+            seg = xf[offs[s]:offs[s + 1]]
+            ok, info = sum_ok(got[s], seg, rel) if seg.size else (got[s] == 0.0, got[s])
+            assert ok, (dt, s, info)
+        # the same call twice gives the same bits (fixed join order)
+        o2 = torch.empty_like(o)
+        gbk.segmented_reduce("sum", _dev(torch, xf), do, o2)
+        gbk.stream_check()
+        assert o2.cpu().numpy().tobytes() == got.tobytes()
