@@ -292,6 +292,34 @@ def other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind, reps=10):
     out["c3_data"] = {"segments": nseg, "elements": ns, "lognormal_sigma": round(float(sigma), 4)}
     del xf, xq, yq, do, segout
 
+    # ---- c3 graph: 8 dependent reduce / scan nodes over 2^24 values, replayed
+    # as one CUDA graph vs issued as 8 stream launches --------------------------
+    n = 1 << 24
+    xg = torch.from_numpy(datagen.uniform_i32(n, 0, 15, seed=1)).to(dev)
+    gb = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(4)]
+    gres = torch.zeros(64, dtype=torch.uint8, device=dev)
+    gbk.check(lib.gbk_workspace_reserve(sp, 64 << 20), "workspace_reserve")
+
+    def chain():
+        gbk.scan(xg, gb[0], inclusive=False, init=0, stream=stream)      # each node reads the previous one
+        gbk.reduce("max", gb[0], out=gres[0:8], stream=stream)
+        gbk.scan(gb[0], gb[1], inclusive=True, stream=stream)
+        gbk.reduce("sum", gb[1], out=gres[8:16], stream=stream)
+        gbk.scan(gb[1], gb[2], inclusive=False, init=3, stream=stream)
+        gbk.reduce("minloc", gb[2], out=gres[16:32], stream=stream)
+        gbk.scan(gb[2], gb[3], inclusive=True, stream=stream)
+        gbk.reduce("maxloc", gb[3], out=gres[32:48], stream=stream)
+
+    graph = gbk.Graph(stream)
+    with graph:
+        chain()
+    ms_stream = timed([chain], reps, batch=True)
+    ms_graph = timed([graph.submit], reps, batch=True)
+    node_bytes = 4 * (n * 12) + 4 * (n * 8)  # scans i32->i64 / i64->i64 read + write, reduces read
+    out["c3_graph_8_nodes_2^24"] = dict(rate(node_bytes, ms_graph), stream_launches_ms=round(ms_stream, 4),
+                                        graph_speedup=round(ms_stream / ms_graph, 3))
+    del graph, xg, gb
+
     # ---- c4 -----------------------------------------------------------------
     n = 1 << 27
     iota = torch.arange(n, dtype=torch.int32, device=dev)

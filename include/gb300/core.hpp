@@ -45,6 +45,37 @@ struct LayoutRight {};
 struct HostSpace {};
 struct GB300Space {};
 
+// Kokkos::InitializationSettings (core/src/impl/Kokkos_InitializationSettings.hpp):
+// the settings a space's impl_initialize receives; this space reads the
+// device id only (the library runs on the current device).
+class InitializationSettings {
+ public:
+  InitializationSettings& set_device_id(int d) {
+    device_id_ = d;
+    return *this;
+  }
+  InitializationSettings& set_num_threads(int t) {
+    num_threads_ = t;
+    return *this;
+  }
+  bool has_device_id() const { return device_id_ >= 0; }
+  int get_device_id() const { return device_id_; }
+  int get_num_threads() const { return num_threads_; }
+
+ private:
+  int device_id_ = -1, num_threads_ = -1;
+};
+// Kokkos::Device<ExecSpace, MemSpace> (core/src/Kokkos_Core_fwd.hpp).
+template <class ExecSpace, class MemSpace>
+struct Device {
+  using execution_space = ExecSpace;
+  using memory_space = MemSpace;
+  using device_type = Device;
+};
+// Team scratch memory space tag (the header path's teams use static shared
+// memory inside the library skeletons).
+struct ScratchMemorySpaceTag {};
+
 namespace Experimental {
 // The execution space (core/src/Cuda/Kokkos_Cuda.hpp:95-260 is the device
 // model): one CUDA stream; fence() = gbk_stream_check, which also reports
@@ -53,8 +84,10 @@ class GB300 {
  public:
   using execution_space = GB300;
   using memory_space = GB300Space;
+  using device_type = Device<GB300, GB300Space>;
   using array_layout = LayoutLeft;
   using size_type = int64_t;
+  using scratch_memory_space = ScratchMemorySpaceTag;
   GB300() = default;
   explicit GB300(cudaStream_t s) : stream_(s) {}
   cudaStream_t stream() const { return stream_; }
@@ -76,6 +109,14 @@ class GB300 {
        << " bytes\n";
   }
   static const char* name() { return "GB300"; }
+  // Space registration hooks (core/src/impl/Kokkos_ExecSpaceManager.hpp:17-108):
+  // select the device, make the library's per-device state; release it.
+  static void impl_initialize(const InitializationSettings& s) {
+    if (s.has_device_id()) check_cuda(cudaSetDevice(s.get_device_id()), "GB300::impl_initialize");
+    int sm = 0;
+    check(gbk_device_info(&sm, nullptr, nullptr, nullptr), "GB300::impl_initialize");
+  }
+  static void impl_finalize() { check_cuda(cudaDeviceSynchronize(), "GB300::impl_finalize"); }
 
  private:
   cudaStream_t stream_ = nullptr;
@@ -86,11 +127,13 @@ using DefaultExecutionSpace = Experimental::GB300;
 
 // initialize(): GBK_TUNING_TABLE=<file> loads a tuning table (as written by
 // the autotuner) and enables it for every call made without a configuration.
-inline void initialize(int = 0, char** = nullptr) {
+inline void initialize(const InitializationSettings& s) {
+  Experimental::GB300::impl_initialize(s);
   if (const char* p = std::getenv("GBK_TUNING_TABLE")) {
     if (gbk_tuner_load(p) == GBK_OK) gbk_tuner_enable(1);
   }
 }
+inline void initialize(int = 0, char** = nullptr) { initialize(InitializationSettings()); }
 inline void finalize() { check_cuda(cudaDeviceSynchronize(), "finalize"); }
 inline void fence(const std::string& = std::string()) { Experimental::GB300::impl_static_fence(); }
 

@@ -15,6 +15,18 @@
 #include <numeric>
 #include <vector>
 
+// The execution-space concept a Kokkos space must model
+// (core/src/impl/Kokkos_ExecSpaceManager.hpp:17-108): typedefs, regular and
+// at most two pointers in size.
+using ESpace = Kokkos::Experimental::GB300;
+static_assert(std::is_same<ESpace::execution_space, ESpace>::value, "execution_space");
+static_assert(std::is_same<ESpace::device_type::execution_space, ESpace>::value, "device_type");
+static_assert(std::is_same<ESpace::device_type::memory_space, ESpace::memory_space>::value, "memory_space");
+static_assert(sizeof(ESpace::size_type) == 8 && sizeof(ESpace::array_layout) >= 1, "size_type / array_layout");
+static_assert(sizeof(ESpace::scratch_memory_space) >= 1, "scratch_memory_space");
+static_assert(std::is_default_constructible<ESpace>::value && std::is_copy_assignable<ESpace>::value, "regular");
+static_assert(sizeof(ESpace) <= 2 * sizeof(void*), "at most two pointers");
+
 static int g_fail = 0;
 static void report(bool ok, const char* name, const char* detail = "") {
   std::printf("%s %s %s\n", ok ? "PASS" : "FAIL", name, detail);
