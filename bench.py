@@ -52,7 +52,8 @@ STEP_BYTES = 3 * RED_BYTES + HIST_BYTES
 # The dominant kernel and its DRAM traffic per launch (dram__bytes_read.sum +
 # dram__bytes_write.sum from one ncu capture of the same launch, as recorded
 # in profiles/).
-ROOF_KERNEL = "k_reduce_tma (MinLoc/MaxLoc/Sum f32, shared-memory ring)"
+ROOF_KERNEL = ("flat reduce of the box, MinLoc/MaxLoc/Sum f32 (with the autotuner table: k_reduce_tma shared-memory "
+               "ring, 2 CTAs/SM, for MinLoc and Sum; k_reduce_flat load-pipelined for MaxLoc)")
 ROOF_TRAFFIC = 272138240  # MinLoc f32 over the box: 268.48 MB read + 3.66 MB written
 WORKLOAD = ("MDRange<Rank<3>> MinLoc+MaxLoc+Sum over LayoutLeft View<float***> 512x512x256 N(0,1) "
             "+ ScatterView histogram 2^26 int32 Zipf(1.1) keys -> 2^16 int64 bins")
@@ -390,12 +391,15 @@ def main():
     ap.add_argument("--no-tuning-table", action="store_true",
                     help="use the library defaults instead of the autotuner's table (kokkos_gb300/tuning_table.txt)")
     ap.add_argument("--only", default=None,
-                    choices=["minloc", "maxloc", "sum", "hist", "sum_f64", "exscan", "sort"],
+                    choices=["minloc", "maxloc", "sum", "hist", "sum_f64", "exscan", "sort", "segsum"],
                     help="run just this operation warmup+steps times (for profiler captures): the bench ops on the "
                          "bench inputs, or sum_f64 / exscan on 2^24 doubles / int32 (the RangePolicy Sum and "
                          "exclusive_scan i32->i64 workload), or sort: sort_by_key of --sort-n uniform uint64 keys "
-                         "with an int32 iota payload (the sort_by_key workload, 2^27 by default)")
+                         "with an int32 iota payload (the sort_by_key workload, 2^27 by default), or segsum: the "
+                         "segmented Sum of --seg-total float elements in lognormal segments")
     ap.add_argument("--sort-n", type=int, default=1 << 27)
+    ap.add_argument("--seg-total", type=int, default=1 << 28,
+                    help="--only segsum: elements of the lognormal segments (10,000 segments per 2^28, median 2,048)")
     ap.add_argument("--sort-keys", default="uniform", choices=["uniform", "lowentropy"],
                     help="--only sort keys: uniform 64-bit, or a seeded base pattern with 8 random bit positions")
     args = ap.parse_args()
@@ -441,6 +445,23 @@ def main():
         gbk.stream_check(stream)
         ms = [a.elapsed_time(b) for a, b in evs[args.warmup:]]
         print(json.dumps({"only": "sort", "keys": args.sort_keys, "n": n, "ms": ms, "Gpairs/s": [round(n / m / 1e6, 3) for m in ms]}))
+        return
+    if args.only == "segsum":
+        total = args.seg_total
+        nseg = max(1, int(round(10000 * total / (1 << 28))))
+        lens, _ = datagen.lognormal_lengths(nseg, median=2048.0, max_len=1 << 21, target_total=total, seed=0)
+        offs = datagen.offsets_from_lengths(lens)
+        ns = int(offs[-1])
+        xf = torch.from_numpy(datagen.normal_f32(ns, seed=0)).to(dev)
+        do = torch.from_numpy(offs).to(dev)
+        so = torch.empty(nseg, dtype=torch.float32, device=dev)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup + args.steps):
+                gbk.check(lib.gbk_segmented_reduce(0, 4, ctypes.c_void_p(xf.data_ptr()), ctypes.c_void_p(do.data_ptr()),
+                                                   nseg, ns, ctypes.c_void_p(so.data_ptr()), sp, None), "segsum")
+        torch.cuda.synchronize()
+        gbk.stream_check(stream)
+        print(json.dumps({"only": "segsum", "elements": ns, "segments": nseg, "launches": args.warmup + args.steps}))
         return
     if args.only in ("sum_f64", "exscan"):
         n = 1 << 24

@@ -485,6 +485,7 @@ struct SegRedCta {
   static constexpr int VEC = 16 / sizeof(T);
   static constexpr int WARPS = SR_BLOCK / 32;
   int64_t* s_win;
+  int64_t* s_wb;
   V* s_red0;
   V* s_red1;
   int64_t* s_cur;
@@ -493,46 +494,58 @@ struct SegRedCta {
   int* s_started;
   SegRec<T>* rec_first;
 
+  // Refill the window of starts: s_win[t] = offsets[base + t].
+  __device__ void load_window(int64_t base, const SegRedArgs& A) const {
+    __syncthreads();  // earlier readers of s_win are done
+    const int tid = threadIdx.x;
+    s_win[tid] = base + tid <= A.nseg ? A.offsets[base + tid] : (int64_t)0x7FFFFFFFFFFFFFFFLL;
+    if (tid == 0) *s_wb = base;
+    __syncthreads();
+  }
+
   // A chunk [c0, c1) that holds at least one segment start; get(i) reads
-  // element i.  `acc` (the per-thread partials of the current segment) is
-  // folded into the carry first and reset.
+  // element i.  The starts come from the window of offsets cached in shared
+  // memory (s_win[t] = offsets[*s_wb + t]), refilled only when more than its
+  // 256 entries are consumed.  `acc` (the per-thread partials of the current
+  // segment) joins the first piece, and is reset.
   template <class Get>
   __device__ void slow(const Get& get, int64_t c0, int64_t c1, V& acc, T* out, const SegRedArgs& A) const {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const V pend = block_reduce<R, SR_BLOCK>(acc, s_red0);
-    if (tid == 0) R::join(*s_carry, pend);
-    acc = R::init();
-    int64_t kb = *s_cur + 1;  // index of the next start not yet consumed
     int64_t seg = *s_cur, prev = c0, first_b = c0, last_b = c0, next_start = 0;
     bool first_window = true;
     while (true) {
-      __syncthreads();  // earlier readers of s_win are done
-      const int64_t wv = kb + tid <= A.nseg ? A.offsets[kb + tid] : (int64_t)0x7FFFFFFFFFFFFFFFLL;
-      s_win[tid] = wv;
-      const int m = __syncthreads_count(wv < c1);  // offsets are sorted: the first m of the window
-      for (int j = warp; j < m; j += WARPS) {
-        if (first_window && j == 0) continue;  // the first piece: folded by the whole CTA below
-        const int64_t lo = j == 0 ? prev : s_win[j - 1], hi = s_win[j];
+      const int64_t j0l = seg + 1 - *s_wb;  // window slot of the next start not yet consumed
+      if (j0l >= SR_BLOCK) {
+        load_window(seg + 1, A);
+        continue;
+      }
+      const int j0 = (int)j0l;
+      const int m = __syncthreads_count(tid >= j0 && s_win[tid] < c1);  // sorted: slots [j0, j0 + m)
+      for (int q = warp; q < m; q += WARPS) {
+        if (first_window && q == 0) continue;  // the first piece: folded by the whole CTA below
+        const int jj = j0 + q;
+        const int64_t lo = q == 0 ? prev : s_win[jj - 1], hi = s_win[jj];
         if (hi <= lo) continue;  // empty segment: identity from the pre-pass
         V v = R::init();
         for (int64_t i = lo + lane; i < hi; i += 32) R::template update<true>(v, get(i), 0);
         v = WarpRed<R>::run(v);
-        if (lane == 0) out[seg + j] = v;  // a whole segment inside this chunk
+        if (lane == 0) out[seg + q] = v;  // a whole segment inside this chunk
       }
       if (m > 0) {
-        if (first_window) first_b = s_win[0];
-        last_b = s_win[m - 1];
+        if (first_window) first_b = s_win[j0];
+        last_b = s_win[j0 + m - 1];
         prev = last_b;
       }
       seg += m;
-      kb += m;
       first_window = false;
-      if (m < SR_BLOCK) {
-        next_start = s_win[m];
+      if (j0 + m < SR_BLOCK) {
+        next_start = s_win[j0 + m];
         break;
       }
+      load_window(seg + 1, A);
     }
-    V fp = R::init(), lp = R::init();
+    V fp = acc, lp = R::init();
+    acc = R::init();
     for (int64_t i = c0 + tid; i < c1; i += SR_BLOCK) {
       if (i < first_b) R::template update<true>(fp, get(i), 0);
       else if (i >= last_b) R::template update<true>(lp, get(i), 0);
@@ -579,7 +592,7 @@ __global__ void __launch_bounds__(SR_BLOCK) k_segred(const T* __restrict__ x, T*
   __shared__ __align__(8) unsigned long long s_bar[SR_STAGES];
   __shared__ int64_t s_win[SR_BLOCK];
   __shared__ V s_red0[WARPS], s_red1[WARPS];
-  __shared__ int64_t s_cur, s_next, s_lo, s_hi;
+  __shared__ int64_t s_cur, s_next, s_lo, s_hi, s_wb;
   __shared__ V s_carry;
   __shared__ int s_started;
   __shared__ unsigned s_ticket;
@@ -629,14 +642,15 @@ __global__ void __launch_bounds__(SR_BLOCK) k_segred(const T* __restrict__ x, T*
     }
     __syncthreads();
   }
+  const SegRedCta<R, T> cta{s_win, &s_wb, s_red0, s_red1, &s_cur, &s_next, &s_carry, &s_started, &recs[2 * b]};
+  cta.load_window(s_lo + 1, A);  // the first 256 starts after element a
   if (tid == 0) {
     s_cur = s_lo;
-    s_next = A.offsets[s_lo + 1];
+    s_next = s_win[0];
     s_started = A.offsets[s_lo] == a;
     s_carry = R::init();
   }
   __syncthreads();
-  const SegRedCta<R, T> cta{s_win, s_red0, s_red1, &s_cur, &s_next, &s_carry, &s_started, &recs[2 * b]};
   V acc = R::init();
   bool bad = false;
   for (int64_t c = 0; c < nchunks; ++c) {

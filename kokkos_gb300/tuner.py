@@ -29,7 +29,9 @@ KIND_REDUCE, KIND_SCAN, KIND_HIST, KIND_SEG = 0, 1, 2, 3
 REDUCE_CFGS = [(b, u, c) for (b, u) in [(256, 2), (256, 4), (256, 8), (512, 2), (512, 4), (128, 8), (1024, 2)]
                for c in (1, 2, 4, 8)]
 SCAN_CFGS = [(9, 0), (7, 0), (3, 0), (9, 1)]  # (vectors per thread, CTAs per SM; 0 = all resident)
-SEG_CFGS = [(7, 0), (3, 0), (7, 1)]  # (vectors per thread, CTAs per SM; 0 = all resident)
+# segmented reduce (variant, vectors per thread, CTAs per SM; 0 = all resident): variant 0 is the
+# contiguous-share kernel (its shape is fixed), variant 1 the tile pipeline
+SEG_CFGS = [(0, 7, 0), (1, 7, 0), (1, 3, 0), (1, 7, 1)]
 # histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit, no privatisation
 HIST_CFGS_SMALL = [(0x01, 1), (0x01, 2), (0x11, 2), (0x20, 1), (0x30, 1), (0x40, 1)]
 HIST_CFGS_2E16 = [(0x02, 1), (0x12, 1), (0x04, 1), (0x20, 1), (0x30, 1), (0x40, 1)]
@@ -47,7 +49,7 @@ def candidates(w):
     if k == KIND_SCAN:
         return [{"block": 256, "ipt": u, "cps": c, "variant": 0} for (u, c) in SCAN_CFGS]
     if k == KIND_SEG:
-        return [{"block": 256, "ipt": u, "cps": c, "variant": 0} for (u, c) in SEG_CFGS]
+        return [{"block": 256, "ipt": u, "cps": c, "variant": v} for (v, u, c) in SEG_CFGS]
     cf = HIST_CFGS_2E16 if w["nbins"] > 24576 else HIST_CFGS_SMALL
     return [{"block": 0, "ipt": 0, "cps": c, "variant": v} for (v, c) in cf]
 
@@ -69,7 +71,10 @@ def features(w, c):
     f[19] = (math.log2(max(c["cps"], 1)) - 2.0) / 2.0
     v = c["variant"]
     # histogram: cluster-split bins; reduce: the ring kernel (variant 2)
-    f[20] = float((v & 0xF) > 1) if v and not (v & 0x60) else 0.0
+    if w["kind"] == KIND_SEG:
+        f[20] = float(v == 1)                            # segmented: the tile pipeline
+    else:
+        f[20] = float((v & 0xF) > 1) if v and not (v & 0x60) else 0.0
     f[21] = float((v & 0x10) != 0)                       # warp aggregation
     f[22] = float((v & 0x20) != 0)                       # 16-bit bins
     f[23] = float((v & 0x40) != 0)                       # no privatisation
@@ -129,8 +134,11 @@ class Bench:
         self.bins = torch.zeros(65536, dtype=torch.int64, device="cuda")
         self._ent = {}
         self.seg_cache = {}
-        # Written before every timed call: inputs start cold in L2, as in the bench.
-        self.flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        # Read before every timed call: inputs start cold in L2, as in the bench, and the lines
+        # that evict them are clean (a written flush buffer would be written back to HBM during
+        # the timed call, which the bench step never does).
+        self.flush = torch.ones(256 << 20, dtype=torch.uint8, device="cuda")
+        self.flush_sink = torch.zeros(1, dtype=torch.int64, device="cuda")
 
     def entropy(self, pool, nbins):
         key = (pool, nbins)
@@ -187,7 +195,7 @@ class Bench:
             return float("inf")
         for r in range(reps):
             with torch.cuda.stream(self.s):
-                self.flush.fill_(r & 255)
+                self.flush_sink.copy_(self.flush.sum(dtype=torch.int64))
             e[2 * r].record(self.s)
             self.call(w, c)
             e[2 * r + 1].record(self.s)
