@@ -12,14 +12,15 @@ ScatterView workload:
 268 MB, larger than the 129 MB L2, so no flush is needed).  `e2e` times the
 same step through the C ABI from pinned HOST buffers: deep_copy of the view
 and the keys to the device, the four operations, and the results copied
-back, every step.  `roofline` is the dominant kernel (the flat ring reduce
-the contiguous MDRange box collapses to).  `cpu_baseline` is the
-oracle (CPU restatement of the reference OpenMP algorithms) on this host.
+back, every step.  `roofline` is the dominant kernel (the flat reduce the
+contiguous MDRange box collapses to).  `cpu_baseline` is the oracle (CPU
+restatement of the reference OpenMP algorithms) on this host.
 `other_configs` (N = 1 only) times the other headline workloads after the
 step, outside the timed region: the RangePolicy Sum and exclusive_scan of
 2^24 values, the batched segmented Sum / inclusive_scan over 10,000
-lognormal segments against the one-launch-per-segment loop, and
-sort_by_key of 2^27 uint64 keys with an int32 payload.
+lognormal segments against the one-launch-per-segment loop, a Graph of 8
+dependent reduce / scan nodes, sort_by_key, sort and BinSort of 2^27 uint64
+keys, and deep_copy / fill / permute.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbk|reference]
 
@@ -341,6 +342,32 @@ def other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind, reps=10):
             rate(pass_bytes, ms), digit_passes=passes, Gpairs_per_s=round(n / (ms / 1e3) / 1e9, 3),
             min_bytes_GBps=round(n * 24 / (ms / 1e3) / 1e9, 1))
         del k0
+    # Kokkos::sort of the uniform keys alone, and BinSort with BinOp1D(n / 2 bins, min, max) (the bins the
+    # reference's host sort path uses): the bin permutation (stable within a bin), then applying it to the keys
+    kh = datagen.bits_u64(n, seed=0)
+    k0 = torch.from_numpy(kh.view(np.int64)).to(dev)
+
+    def refill_keys(_c):
+        dk.copy_(k0)
+
+    ms = timed([lambda: gbk.check(lib.gbk_sort(3, P(dk.data_ptr()), n, sp), "sort")], 3, prep=refill_keys)
+    passes = 8
+    out["c4_sort_u64_2^27_uniform"] = dict(rate(n * 8 + (passes - 1) * n * 8 + passes * n * 16, ms),
+                                           Gkeys_per_s=round(n / (ms / 1e3) / 1e9, 3))
+    kmin, kmax = float(kh.min()), float(kh.max())
+    nb_req = n // 2
+    mul = float(nb_req) / (kmax - kmin)
+    nbb = nb_req + 1
+    bcnt = torch.empty(nbb, dtype=torch.int32, device=dev)
+    boff = torch.empty(nbb, dtype=torch.int64, device=dev)
+    bperm = torch.empty(n, dtype=torch.int64, device=dev)
+    ms_bin = timed([lambda: gbk.check(lib.gbk_binsort_u64(P(k0.data_ptr()), n, nbb, kmin, mul, 0, P(bcnt.data_ptr()),
+                                                          P(boff.data_ptr()), P(bperm.data_ptr()), sp), "binsort")], 3)
+    ms_perm = timed([lambda: gbk.check(lib.gbk_permute(8, P(k0.data_ptr()), P(bperm.data_ptr()), n, P(dk.data_ptr()), sp),
+                                       "permute")], 3)
+    out["c4_binsort_u64_2^27_uniform"] = {"binsort_ms": round(ms_bin, 3), "permute_ms": round(ms_perm, 3),
+                                          "bins": nbb, "Gkeys_per_s": round(n / ((ms_bin + ms_perm) / 1e3) / 1e9, 3)}
+    del k0, bcnt, boff, bperm
     del iota, dk, dv
 
     # ---- data movement either side of the path --------------------------------
