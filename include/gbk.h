@@ -246,16 +246,18 @@ int gbk_scatter(gbk_reducer_t op, gbk_dtype_t dtype, const int32_t* idx, const v
 /* ---- batched segmented work ------------------------------------------------ */
 /* Segments s = [offsets[s], offsets[s+1]) of x[0..n), offsets non-decreasing
  * with offsets[0] = 0 and offsets[nseg] = n (device memory, int64).  All
- * segments are processed in ONE launch, load-balanced over fixed tiles of the
- * concatenated array whatever the segment lengths.  Stands in for the
+ * segments are processed in ONE launch, load-balanced over equal shares (or
+ * tiles) of the concatenated array whatever the segment lengths.  Stands in for the
  * TeamPolicy league pattern, one team per segment with a TeamThreadRange
  * reduce / scan inside (core/src/Kokkos_ExecPolicy.hpp:366-700,
  * core/src/Cuda/Kokkos_Cuda_Parallel_Team.hpp:589-980,
  * core/src/OpenMP/Kokkos_OpenMP_Parallel_Reduce.hpp:332-530), and for a loop
  * of one parallel_reduce / inclusive_scan per segment.
  * reduce: out[s] = op over segment s (Sum, Min, Max; identity for an empty
- * segment), all six dtypes.  tune->items_per_thread (2, 4, 8) sets the tile;
- * NULL = tuning table or default. */
+ * segment), all six dtypes.  Variant 0 (default): contiguous per-CTA shares
+ * for 16-byte aligned x of at least one 16 KiB chunk; variant 1 (and any
+ * other x): the tile pipeline, tune->items_per_thread (3 or 7) sets its
+ * tile.  NULL = tuning table or default.  Results are deterministic. */
 int gbk_segmented_reduce(gbk_reducer_t op, gbk_dtype_t dtype, const void* x, const int64_t* offsets, int64_t nseg,
                          int64_t n, void* out, gbk_stream_t stream, const gbk_tuning_t* tune);
 /* scan: per-segment inclusive / exclusive (from 0) prefix sums, (in, out) in
