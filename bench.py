@@ -418,12 +418,12 @@ def main():
     ap.add_argument("--no-tuning-table", action="store_true",
                     help="use the library defaults instead of the autotuner's table (kokkos_gb300/tuning_table.txt)")
     ap.add_argument("--only", default=None,
-                    choices=["minloc", "maxloc", "sum", "hist", "sum_f64", "exscan", "sort", "segsum"],
+                    choices=["minloc", "maxloc", "sum", "hist", "sum_f64", "exscan", "sort", "segsum", "segscan"],
                     help="run just this operation warmup+steps times (for profiler captures): the bench ops on the "
                          "bench inputs, or sum_f64 / exscan on 2^24 doubles / int32 (the RangePolicy Sum and "
                          "exclusive_scan i32->i64 workload), or sort: sort_by_key of --sort-n uniform uint64 keys "
-                         "with an int32 iota payload (the sort_by_key workload, 2^27 by default), or segsum: the "
-                         "segmented Sum of --seg-total float elements in lognormal segments")
+                         "with an int32 iota payload (the sort_by_key workload, 2^27 by default), or segsum / segscan: the "
+                         "segmented Sum (f32) / inclusive_scan (i32) of --seg-total elements in lognormal segments")
     ap.add_argument("--sort-n", type=int, default=1 << 27)
     ap.add_argument("--seg-total", type=int, default=1 << 28,
                     help="--only segsum: elements of the lognormal segments (10,000 segments per 2^28, median 2,048)")
@@ -473,22 +473,31 @@ def main():
         ms = [a.elapsed_time(b) for a, b in evs[args.warmup:]]
         print(json.dumps({"only": "sort", "keys": args.sort_keys, "n": n, "ms": ms, "Gpairs/s": [round(n / m / 1e6, 3) for m in ms]}))
         return
-    if args.only == "segsum":
+    if args.only in ("segsum", "segscan"):
         total = args.seg_total
         nseg = max(1, int(round(10000 * total / (1 << 28))))
         lens, _ = datagen.lognormal_lengths(nseg, median=2048.0, max_len=1 << 21, target_total=total, seed=0)
         offs = datagen.offsets_from_lengths(lens)
         ns = int(offs[-1])
-        xf = torch.from_numpy(datagen.normal_f32(ns, seed=0)).to(dev)
         do = torch.from_numpy(offs).to(dev)
-        so = torch.empty(nseg, dtype=torch.float32, device=dev)
+        if args.only == "segsum":
+            xf = torch.from_numpy(datagen.normal_f32(ns, seed=0)).to(dev)
+            so = torch.empty(nseg, dtype=torch.float32, device=dev)
+            call = lambda: gbk.check(lib.gbk_segmented_reduce(  # noqa: E731
+                0, 4, ctypes.c_void_p(xf.data_ptr()), ctypes.c_void_p(do.data_ptr()), nseg, ns,
+                ctypes.c_void_p(so.data_ptr()), sp, None), "segsum")
+        else:
+            xq = torch.from_numpy(datagen.uniform_i32(ns, 0, 255, seed=0)).to(dev)
+            yq = torch.empty(ns, dtype=torch.int32, device=dev)
+            call = lambda: gbk.check(lib.gbk_segmented_scan(  # noqa: E731
+                1, 0, 0, ctypes.c_void_p(xq.data_ptr()), ctypes.c_void_p(do.data_ptr()), nseg, ns,
+                ctypes.c_void_p(yq.data_ptr()), sp, None), "segscan")
         with torch.cuda.stream(stream):
             for _ in range(args.warmup + args.steps):
-                gbk.check(lib.gbk_segmented_reduce(0, 4, ctypes.c_void_p(xf.data_ptr()), ctypes.c_void_p(do.data_ptr()),
-                                                   nseg, ns, ctypes.c_void_p(so.data_ptr()), sp, None), "segsum")
+                call()
         torch.cuda.synchronize()
         gbk.stream_check(stream)
-        print(json.dumps({"only": "segsum", "elements": ns, "segments": nseg, "launches": args.warmup + args.steps}))
+        print(json.dumps({"only": args.only, "elements": ns, "segments": nseg, "launches": args.warmup + args.steps}))
         return
     if args.only in ("sum_f64", "exscan"):
         n = 1 << 24
