@@ -220,6 +220,12 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
         for (int q = 0; q < VEC; ++q) v[q] = e0 + q < n ? x[e0 + q] : TI(0);
       }
     };
+    // Elements of this thread's C that exist in a tile starting at tbase
+    // (C for every tile but the last): one small-integer compare per element.
+    auto thread_valid = [&](int64_t tbase) -> int {
+      const int64_t rem = n - (tbase + r0);
+      return rem <= 0 ? 0 : (rem >= C ? C : (int)rem);
+    };
     // Head bits of this thread's elements (bit k: element r0 + k) and the next.
     auto head_bits = [&](int s) -> unsigned long long {
       const unsigned* bm = reinterpret_cast<const unsigned*>(dsm + (size_t)s * STAGE_BYTES + IN_BYTES);
@@ -234,6 +240,7 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
       if (!mbar_wait(&s_bar[s], (unsigned)(j / STG) & 1u, S.wait_limit)) bad = true;
       const unsigned long long hb = head_bits(s);
       const int64_t tbase = tile * TILE;
+      const int valid = thread_valid(tbase);
       TO a = O::id();
       unsigned h = 0;
 #pragma unroll
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
             a = O::id();
             h = 1;
           }
-          if (tbase + r0 + kk < n) a = O::f(a, (TO)v[q]);
+          if (kk < valid) a = O::f(a, (TO)v[q]);
         }
       }
       TO iv = a;
@@ -332,6 +339,7 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
       const TO v1 = q_wh ? q_wv : O::f(excl, q_wv);  // carry into this warp
       TO run = q_eh ? q_ev : O::f(v1, q_ev);         // carry into this thread
       const bool out_full = OUT_TILE && tbase + TILE <= nout;
+      const int valid = thread_valid(tbase);
       // Reduce: nothing to write from a tile in which no segment ends.
       const int passes = (MODE != M_REDUCE || (s_info_h[i % SEG_NLB] & 4u)) ? IPT : 0;
 #pragma unroll
@@ -346,7 +354,7 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
           const int64_t e = tbase + r0 + kk;
           if ((hb >> kk) & 1u) run = O::id();
           if (MODE == M_EXCL) o[q] = run;
-          if (e < n) run = O::f(run, (TO)v[q]);
+          if (kk < valid) run = O::f(run, (TO)v[q]);
           if (MODE == M_INCL) o[q] = run;
           if (MODE == M_REDUCE && e < n && (((hb >> (kk + 1)) & 1u) || e == n - 1)) {
             // Last element of its segment: the segment is the last s with
