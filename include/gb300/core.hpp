@@ -20,6 +20,7 @@
 
 #include "../gbk.h"
 #include "../gbk_tools.h"
+#include "tools.hpp"
 
 #ifndef KOKKOS_LAMBDA
 #define KOKKOS_LAMBDA [=] __host__ __device__
@@ -129,12 +130,16 @@ using DefaultExecutionSpace = Experimental::GB300;
 // the autotuner) and enables it for every call made without a configuration.
 inline void initialize(const InitializationSettings& s) {
   Experimental::GB300::impl_initialize(s);
+  Tools::Impl::load_tool();  // KOKKOS_TOOLS_LIBS
   if (const char* p = std::getenv("GBK_TUNING_TABLE")) {
     if (gbk_tuner_load(p) == GBK_OK) gbk_tuner_enable(1);
   }
 }
 inline void initialize(int = 0, char** = nullptr) { initialize(InitializationSettings()); }
-inline void finalize() { check_cuda(cudaDeviceSynchronize(), "finalize"); }
+inline void finalize() {
+  check_cuda(cudaDeviceSynchronize(), "finalize");
+  Tools::Impl::unload_tool();
+}
 inline void fence(const std::string& = std::string()) { Experimental::GB300::impl_static_fence(); }
 
 // ---------------------------------------------------------------------------

@@ -200,6 +200,7 @@ struct AsReducer {
 // ---- parallel_for ------------------------------------------------------------
 template <class E, class... R, class F>
 void parallel_for(const RangePolicy<E, R...>& p, const F& f) {
+  Tools::Impl::Region<F> tool_region(Tools::Impl::kFor, p.space().stream());
   const int64_t n = p.end() - p.begin();
   if (n <= 0) return;
   const int64_t g = Impl::grid_for(n);
@@ -212,6 +213,7 @@ void parallel_for(int64_t n, const F& f) {
 }
 template <class RankT, class E, class F>
 void parallel_for(const MDRangePolicy<RankT, E>& p, const F& f) {
+  Tools::Impl::Region<F> tool_region(Tools::Impl::kFor, p.space().stream());
   constexpr int R = RankT::rank;
   Impl::MDArgs m{};
   int64_t n = 1;
@@ -227,6 +229,7 @@ void parallel_for(const MDRangePolicy<RankT, E>& p, const F& f) {
 }
 template <class E, class... R, class F>
 void parallel_for(const TeamPolicy<E, R...>& p, const F& f) {
+  Tools::Impl::Region<F> tool_region(Tools::Impl::kFor, p.space().stream());
   if (p.league_size() <= 0) return;
   int64_t g = p.league_size();
   const int64_t cap = (int64_t)Impl::num_sms() * (2048 / p.team_size());
@@ -235,7 +238,8 @@ void parallel_for(const TeamPolicy<E, R...>& p, const F& f) {
   Impl::launched(cudaGetLastError(), "parallel_for(TeamPolicy)");
 }
 template <class P, class F>
-void parallel_for(const std::string&, const P& p, const F& f) {
+void parallel_for(const std::string& label, const P& p, const F& f) {
+  Tools::Impl::LabelScope ls(label);
   parallel_for(p, f);
 }
 
@@ -243,6 +247,7 @@ void parallel_for(const std::string&, const P& p, const F& f) {
 template <class E, class... R, class F, class Red,
           std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
 void parallel_reduce(const RangePolicy<E, R...>& p, const F& f, const Red& red) {
+  Tools::Impl::Region<F> tool_region(Tools::Impl::kReduce, p.space().stream());
   using V = typename Red::value_type;
   const int64_t n = p.end() - p.begin();
   const int64_t g = Impl::grid_for(n);
@@ -255,6 +260,7 @@ void parallel_reduce(const RangePolicy<E, R...>& p, const F& f, const Red& red) 
 }
 template <class RankT, class E, class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
 void parallel_reduce(const MDRangePolicy<RankT, E>& p, const F& f, const Red& red) {
+  Tools::Impl::Region<F> tool_region(Tools::Impl::kReduce, p.space().stream());
   using V = typename Red::value_type;
   constexpr int R = RankT::rank;
   Impl::MDArgs m{};
@@ -274,6 +280,7 @@ void parallel_reduce(const MDRangePolicy<RankT, E>& p, const F& f, const Red& re
 }
 template <class E, class... R, class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
 void parallel_reduce(const TeamPolicy<E, R...>& p, const F& f, const Red& red) {
+  Tools::Impl::Region<F> tool_region(Tools::Impl::kReduce, p.space().stream());
   using V = typename Red::value_type;
   int64_t g = p.league_size();
   const int64_t cap = (int64_t)Impl::num_sms() * (2048 / p.team_size());
@@ -309,7 +316,8 @@ void parallel_reduce(int64_t n, const F& f, const Red& red) {
   parallel_reduce(RangePolicy<>(0, n), f, red);
 }
 template <class P, class F, class T>
-void parallel_reduce(const std::string&, const P& p, const F& f, T&& result) {
+void parallel_reduce(const std::string& label, const P& p, const F& f, T&& result) {
+  Tools::Impl::LabelScope ls(label);
   parallel_reduce(p, f, std::forward<T>(result));
 }
 

@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(kBlock) k_range_scan(F f, J j, int64_t b, int6
 
 template <class V, class P, class F, class J = Impl::PlusJ<V>>
 void parallel_scan_impl(const P& p, const F& f, V* host_total, J j = J()) {
+  Tools::Impl::Region<F> tool_region(Tools::Impl::kScan, p.space().stream());
   static_assert(sizeof(V) % 4 == 0, "scan value size must be a multiple of 4 bytes");
   constexpr int ITEMS = 8;
   constexpr int64_t TILE = Impl::kBlock * ITEMS;
@@ -254,11 +255,13 @@ void parallel_scan(int64_t n, const F& f) {
   parallel_scan(RangePolicy<>(0, n), f);
 }
 template <class P, class F>
-void parallel_scan(const std::string&, const P& p, const F& f) {
+void parallel_scan(const std::string& label, const P& p, const F& f) {
+  Tools::Impl::LabelScope ls(label);
   parallel_scan(p, f);
 }
 template <class P, class F, class V>
-void parallel_scan(const std::string&, const P& p, const F& f, V& total) {
+void parallel_scan(const std::string& label, const P& p, const F& f, V& total) {
+  Tools::Impl::LabelScope ls(label);
   parallel_scan(p, f, total);
 }
 
