@@ -35,6 +35,7 @@ SEG_CFGS = [(0, 7, 0), (1, 7, 0), (1, 3, 0), (1, 7, 1)]
 # histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit, no privatisation
 HIST_CFGS_SMALL = [(0x01, 1), (0x01, 2), (0x11, 2), (0x20, 1), (0x30, 1), (0x40, 1)]
 HIST_CFGS_2E16 = [(0x02, 1), (0x12, 1), (0x04, 1), (0x20, 1), (0x30, 1), (0x40, 1)]
+SPLIT_CFGS = [(3, 0), (4, 0), (5, 0), (6, 0), (5, 2)]  # double Sum, variant 3: (vectors per thread, CTAs per SM)
 REDUCE_OPS = [("sum", 5), ("sum", 4), ("minloc", 4), ("maxloc", 4), ("sum", 0), ("sum", 1)]  # (op, dtype code)
 OPC = {"sum": 0, "minloc": 8, "maxloc": 9}
 NFEAT = 24
@@ -43,9 +44,13 @@ NFEAT = 24
 def candidates(w):
     k = w["kind"]
     if k == KIND_REDUCE:
-        # variant 1: load-pipelined kernel; variant 2: shared-memory ring kernel
-        return [{"block": b, "ipt": u, "cps": c, "variant": 1} for (b, u, c) in REDUCE_CFGS] + \
-               [{"block": 256, "ipt": 4, "cps": c, "variant": 2} for c in (0, 2)]
+        # variant 1: load-pipelined kernel; variant 2: shared-memory ring kernel; variant 3 (double
+        # Sum only): adds split between the FP64 pipe and an integer fixed-point accumulator
+        cs = [{"block": b, "ipt": u, "cps": c, "variant": 1} for (b, u, c) in REDUCE_CFGS] + \
+             [{"block": 256, "ipt": 4, "cps": c, "variant": 2} for c in (0, 2)]
+        if w.get("op", 0) == 0 and w["dtype"] == 5:
+            cs += [{"block": 256, "ipt": u, "cps": c, "variant": 3} for (u, c) in SPLIT_CFGS]
+        return cs
     if k == KIND_SCAN:
         return [{"block": 256, "ipt": u, "cps": c, "variant": 0} for (u, c) in SCAN_CFGS]
     if k == KIND_SEG:
@@ -73,9 +78,12 @@ def features(w, c):
     # histogram: cluster-split bins; reduce: the ring kernel (variant 2)
     if w["kind"] == KIND_SEG:
         f[20] = float(v == 1)                            # segmented: the tile pipeline
+    elif w["kind"] == KIND_REDUCE:
+        f[20] = float(v == 2)
     else:
         f[20] = float((v & 0xF) > 1) if v and not (v & 0x60) else 0.0
-    f[21] = float((v & 0x10) != 0)                       # warp aggregation
+    # histogram: warp aggregation; reduce: the FP64 / integer split kernel (variant 3)
+    f[21] = float(v == 3) if w["kind"] == KIND_REDUCE else float((v & 0x10) != 0)
     f[22] = float((v & 0x20) != 0)                       # 16-bit bins
     f[23] = float((v & 0x40) != 0)                       # no privatisation
     return f
@@ -305,6 +313,10 @@ def default_cfg_index(w, cs):
     for i, c in enumerate(cs):
         if k == KIND_REDUCE:
             size = {5: 8, 1: 8, 3: 8}.get(w["dtype"], 4) * w["n"]
+            if w.get("op", 0) == 0 and w["dtype"] == 5 and w["n"] >= (1 << 23):
+                if c["variant"] == 3 and (c["ipt"], c["cps"]) == (5, 0):
+                    return i
+                continue
             if (size >= (4 << 20) and c["variant"] == 2 and c["cps"] == 0) or \
                     (size < (4 << 20) and c["variant"] == 1 and (c["block"], c["ipt"], c["cps"]) == (256, 4, 8)):
                 return i

@@ -247,3 +247,79 @@ def test_loc_ties_nan_signed_zero(env, n, dtype):
             got = gbk.reduce_value(op, d)
             want = oracle.reduce(op, a, 1)
             compare(op, got, want, a)
+
+
+SPLIT_TUNES = [(256, 4, 0, 3), (256, 3, 0, 3), (256, 5, 0, 3), (256, 6, 2, 3), (256, 4, 1, 4)]
+
+
+@pytest.mark.parametrize("tune", SPLIT_TUNES)
+def test_sum_f64_split_pipes(env, tune):
+    """Sum<double> with the adds split between the FP64 pipe and the exact
+    fixed-point accumulator on the integer pipes (every launch shape):
+    uniform, mixed-sign, exponent ranges far wider than 53 bits, subnormals,
+    unaligned heads and odd tails, within 1e-12 of the compensated sum."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    rng = np.random.default_rng(7)
+    n = (1 << 20) + 3
+    cases = {
+        "uniform": datagen.uniform_f64(n, seed=3),
+        "normal": datagen.normal_f64(n, seed=4),
+        "wide": datagen.normal_f64(n, seed=5) * 10.0 ** rng.integers(-250, 250, n),
+        "cancel": np.concatenate([datagen.normal_f64(n // 2, seed=6) * 1e30, -datagen.normal_f64(n // 2, seed=6) * 1e30,
+                                  datagen.uniform_f64(3, seed=8)]),
+        "subnormal": datagen.uniform_f64(n, seed=9) * 1e-310,
+        "ints": rng.integers(-1 << 20, 1 << 20, n).astype(np.float64),
+    }
+    for name, x in cases.items():
+        for off in (0, 1):
+            sub = x[off:]
+            got = gbk.reduce_value("sum", _dev(torch, sub), tune=tune)
+            ok, info = sum_ok(got, sub, 1e-12)
+            assert ok, (name, off, info)
+            if name == "ints":  # every partial is an integer below 2^53: exact
+                assert float(got) == float(np.sum(sub.astype(np.int64))), (name, off)
+    gbk.stream_check()
+
+
+def test_sum_f64_split_nonfinite(env):
+    """Infinities and NaNs keep their FP64 meaning on the split kernel."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    n = 1 << 20
+    x = datagen.uniform_f64(n, seed=1)
+    for tune in ((256, 4, 0, 3), (256, 4, 0, 4)):
+        y = x.copy()
+        y[12345] = np.inf
+        assert float(gbk.reduce_value("sum", _dev(torch, y), tune=tune)) == np.inf
+        y[777777] = -np.inf
+        assert np.isnan(float(gbk.reduce_value("sum", _dev(torch, y), tune=tune)))
+        y = x.copy()
+        y[n - 1] = np.nan
+        assert np.isnan(float(gbk.reduce_value("sum", _dev(torch, y), tune=tune)))
+        y = np.full(n, 1.5e308)
+        assert float(gbk.reduce_value("sum", _dev(torch, y), tune=tune)) == np.inf
+        y[1::2] = -1.5e308  # exact cancellation of huge values
+        assert float(gbk.reduce_value("sum", _dev(torch, y), tune=tune)) == 0.0
+    gbk.stream_check()
+
+
+def test_sum_f64_split_fold_interval(env):
+    """2^30 doubles on one CTA per SM: each thread folds its fixed-point
+    accumulator into FP64 mid-way (more than 2^14 elements per thread).  The
+    values are multiples of 2^-20 below 2^31 in every partial, so the sum is
+    exact and compared bit for bit."""
+    gbk, torch = env
+    n = 1 << 30
+    i = torch.arange(n, dtype=torch.int64, device="cuda")
+    x = (1.0 + (i % 7).to(torch.float64) * 2.0 ** -20) * torch.where(i % 3 == 0, -1.0, 1.0).to(torch.float64)
+    del i
+    k = np.arange(21)
+    pat = (1.0 + (k % 7) * 2.0 ** -20) * np.where(k % 3 == 0, -1.0, 1.0)
+    want = (n // 21) * int(np.sum(pat * 2 ** 20)) + int(np.sum(pat[: n % 21] * 2 ** 20))
+    for tune in ((256, 4, 1, 3), (256, 4, 1, 4)):
+        got = float(gbk.reduce_value("sum", x, tune=tune))
+        assert got * 2 ** 20 == want, (tune, got, want / 2 ** 20)
+    del x
+    torch.cuda.empty_cache()
+    gbk.stream_check()
