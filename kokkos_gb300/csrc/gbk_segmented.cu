@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
   constexpr int OVN = (int)(VEC * sizeof(TO) / 16);
   constexpr int OV = 16 / sizeof(TO);
   constexpr int64_t TILE = (int64_t)SEG_COMPUTE * C;
+  constexpr unsigned long long CMASK = (1ull << C) - 1ull;  // head bits of this thread's C elements
   constexpr unsigned IN_BYTES = (unsigned)SEG_COMPUTE * IPT * 16;
   constexpr unsigned BM_BYTES = (unsigned)(TILE / 8) + 16;  // the tile's row and the next row's first word
   constexpr unsigned STAGE_BYTES = (IN_BYTES + BM_BYTES + 127) / 128 * 128;
@@ -243,18 +244,28 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
       const int valid = thread_valid(tbase);
       TO a = O::id();
       unsigned h = 0;
+      if (valid == C && (hb & CMASK) == 0) {  // no head among this thread's elements: plain fold
 #pragma unroll
-      for (int jj = 0; jj < IPT; ++jj) {
-        TI v[VEC];
-        load_vec(s, tbase, jj, v);
+        for (int jj = 0; jj < IPT; ++jj) {
+          TI v[VEC];
+          load_vec(s, tbase, jj, v);
 #pragma unroll
-        for (int q = 0; q < VEC; ++q) {
-          const int kk = jj * VEC + q;
-          if ((hb >> kk) & 1u) {
-            a = O::id();
-            h = 1;
+          for (int q = 0; q < VEC; ++q) a = O::f(a, (TO)v[q]);
+        }
+      } else {
+#pragma unroll
+        for (int jj = 0; jj < IPT; ++jj) {
+          TI v[VEC];
+          load_vec(s, tbase, jj, v);
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) {
+            const int kk = jj * VEC + q;
+            if ((hb >> kk) & 1u) {
+              a = O::id();
+              h = 1;
+            }
+            if (kk < valid) a = O::f(a, (TO)v[q]);
           }
-          if (kk < valid) a = O::f(a, (TO)v[q]);
         }
       }
       TO iv = a;
@@ -342,31 +353,43 @@ __global__ void __launch_bounds__(SEG_BLOCK, 2)
       const int valid = thread_valid(tbase);
       // Reduce: nothing to write from a tile in which no segment ends.
       const int passes = (MODE != M_REDUCE || (s_info_h[i % SEG_NLB] & 4u)) ? IPT : 0;
+      // Scans: no head among this thread's elements (segments are usually
+      // far longer than C): one operator application per element.
+      const bool plain = MODE != M_REDUCE && valid == C && (hb & CMASK) == 0;
 #pragma unroll
       for (int jj = 0; jj < IPT; ++jj) {
         if (jj >= passes) break;
         TI v[VEC];
         load_vec(s, tbase, jj, v);
         TO o[VEC];
+        if (plain) {
 #pragma unroll
-        for (int q = 0; q < VEC; ++q) {
-          const int kk = jj * VEC + q;
-          const int64_t e = tbase + r0 + kk;
-          if ((hb >> kk) & 1u) run = O::id();
-          if (MODE == M_EXCL) o[q] = run;
-          if (kk < valid) run = O::f(run, (TO)v[q]);
-          if (MODE == M_INCL) o[q] = run;
-          if (MODE == M_REDUCE && e < n && (((hb >> (kk + 1)) & 1u) || e == n - 1)) {
-            // Last element of its segment: the segment is the last s with
-            // offsets[s] <= e, among those that can touch this tile.
-            int64_t lo = __ldcg(A.tile_lo + tile) - 1, hi = __ldcg(A.tile_lo + tile + 1);
-            if (lo < 0) lo = 0;
-            if (hi > A.nseg) hi = A.nseg;
-            while (hi - lo > 1) {  // offsets[lo] <= e < offsets[hi] (or hi = nseg)
-              const int64_t mid = lo + (hi - lo) / 2;
-              if (__ldg(A.offsets + mid) <= e) lo = mid; else hi = mid;
+          for (int q = 0; q < VEC; ++q) {
+            if (MODE == M_EXCL) o[q] = run;
+            run = O::f(run, (TO)v[q]);
+            if (MODE == M_INCL) o[q] = run;
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) {
+            const int kk = jj * VEC + q;
+            const int64_t e = tbase + r0 + kk;
+            if ((hb >> kk) & 1u) run = O::id();
+            if (MODE == M_EXCL) o[q] = run;
+            if (kk < valid) run = O::f(run, (TO)v[q]);
+            if (MODE == M_INCL) o[q] = run;
+            if (MODE == M_REDUCE && e < n && (((hb >> (kk + 1)) & 1u) || e == n - 1)) {
+              // Last element of its segment: the segment is the last s with
+              // offsets[s] <= e, among those that can touch this tile.
+              int64_t lo = __ldcg(A.tile_lo + tile) - 1, hi = __ldcg(A.tile_lo + tile + 1);
+              if (lo < 0) lo = 0;
+              if (hi > A.nseg) hi = A.nseg;
+              while (hi - lo > 1) {  // offsets[lo] <= e < offsets[hi] (or hi = nseg)
+                const int64_t mid = lo + (hi - lo) / 2;
+                if (__ldg(A.offsets + mid) <= e) lo = mid; else hi = mid;
+              }
+              y[lo] = run;
             }
-            y[lo] = run;
           }
         }
         if (MODE != M_REDUCE) {
