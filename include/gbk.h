@@ -57,7 +57,12 @@ typedef enum { GBK_I32 = 0, GBK_I64 = 1, GBK_U32 = 2, GBK_U64 = 3, GBK_F32 = 4, 
 
 typedef enum {
   GBK_SUM = 0, GBK_PROD = 1, GBK_MIN = 2, GBK_MAX = 3, GBK_LAND = 4, GBK_LOR = 5,
-  GBK_BAND = 6, GBK_BOR = 7, GBK_MINLOC = 8, GBK_MAXLOC = 9, GBK_MINMAX = 10, GBK_MINMAXLOC = 11
+  GBK_BAND = 6, GBK_BOR = 7, GBK_MINLOC = 8, GBK_MAXLOC = 9, GBK_MINMAX = 10, GBK_MINMAXLOC = 11,
+  /* MinMaxLoc and Sum in one pass: the parallel_reduce with several reducers
+   * (core/src/impl/Kokkos_Combined_Reducer.hpp:533-580) for
+   * parallel_reduce(policy, f, MinMaxLoc<T,int64_t>(r1), Sum<T>(r2)).  Result:
+   * the MinMaxLoc record, then the sum (gbk_reduce and gbk_mdrange_reduce only). */
+  GBK_MINMAXLOC_SUM = 12
 } gbk_reducer_t;
 
 /* A cudaStream_t; NULL is the legacy default stream. */

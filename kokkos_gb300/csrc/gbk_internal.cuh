@@ -90,6 +90,7 @@ constexpr int64_t LOC_ID = 9223372036854775807LL;
 template <class T> struct ValLoc { T val; int64_t loc; };
 template <class T> struct MinMaxV { T min_val, max_val; };
 template <class T> struct MinMaxLocV { T min_val, max_val; int64_t min_loc, max_loc; };
+template <class T> struct MinMaxLocSumV { T min_val, max_val; int64_t min_loc, max_loc; T sum; };
 
 // ---------------------------------------------------------------------------
 // warp shuffles of the value types
@@ -103,6 +104,10 @@ template <class T> __device__ __forceinline__ MinMaxV<T> shx(MinMaxV<T> v, int m
 template <class T> __device__ __forceinline__ MinMaxLocV<T> shx(MinMaxLocV<T> v, int m) {
   v.min_val = shx(v.min_val, m); v.max_val = shx(v.max_val, m);
   v.min_loc = shx(v.min_loc, m); v.max_loc = shx(v.max_loc, m); return v;
+}
+template <class T> __device__ __forceinline__ MinMaxLocSumV<T> shx(MinMaxLocSumV<T> v, int m) {
+  v.min_val = shx(v.min_val, m); v.max_val = shx(v.max_val, m);
+  v.min_loc = shx(v.min_loc, m); v.max_loc = shx(v.max_loc, m); v.sum = shx(v.sum, m); return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -216,6 +221,24 @@ template <class T> struct RMinMaxLoc {
     if (b.max_val > a.max_val || (b.max_val == a.max_val && b.max_loc < a.max_loc)) { a.max_val = b.max_val; a.max_loc = b.max_loc; }
   }
 };
+// MinMaxLoc and Sum of the same elements in one pass (two reducers of one
+// parallel_reduce); each half behaves exactly as its own reducer.
+template <class T> struct RMinMaxLocSum {
+  using V = MinMaxLocSumV<T>;
+  __device__ static V init() { return V{lim<T>::hi(), lim<T>::lo(), LOC_ID, LOC_ID, T(0)}; }
+  template <bool ORD> __device__ static void update(V& v, T x, int64_t l) {
+    MinMaxLocV<T> m{v.min_val, v.max_val, v.min_loc, v.max_loc};
+    RMinMaxLoc<T>::template update<ORD>(m, x, l);
+    v.min_val = m.min_val; v.max_val = m.max_val; v.min_loc = m.min_loc; v.max_loc = m.max_loc;
+    v.sum += x;
+  }
+  __device__ static void join(V& a, const V& b) {
+    MinMaxLocV<T> m{a.min_val, a.max_val, a.min_loc, a.max_loc};
+    RMinMaxLoc<T>::join(m, MinMaxLocV<T>{b.min_val, b.max_val, b.min_loc, b.max_loc});
+    a.min_val = m.min_val; a.max_val = m.max_val; a.min_loc = m.min_loc; a.max_loc = m.max_loc;
+    a.sum += b.sum;
+  }
+};
 
 // Ordered update by one 16-byte vector of consecutive elements at locs l0,
 // l0 + 1, ...: the same result as update<true> element by element.  The
@@ -291,6 +314,16 @@ template <class T, int VEC> struct VecUpd<RMinMaxLoc<T>, T, VEC> {
       vec_first_equal<T, VEC>(v, hi, acc.max_val, q);
       acc.max_loc = l0 + q;
     }
+  }
+};
+
+template <class T, int VEC> struct VecUpd<RMinMaxLocSum<T>, T, VEC> {
+  __device__ static void run(MinMaxLocSumV<T>& acc, const T* v, int64_t l0) {
+    MinMaxLocV<T> m{acc.min_val, acc.max_val, acc.min_loc, acc.max_loc};
+    VecUpd<RMinMaxLoc<T>, T, VEC>::run(m, v, l0);
+    acc.min_val = m.min_val; acc.max_val = m.max_val; acc.min_loc = m.min_loc; acc.max_loc = m.max_loc;
+#pragma unroll
+    for (int q = 0; q < VEC; ++q) acc.sum += v[q];
   }
 };
 

@@ -14,12 +14,13 @@ size_t result_size(int op, int dt) {
     case GBK_MAXLOC: return 16;
     case GBK_MINMAX: return 2 * e;
     case GBK_MINMAXLOC: return (2 * e + 7) / 8 * 8 + 16;
+    case GBK_MINMAXLOC_SUM: return (2 * e + 7) / 8 * 8 + 16 + (e + 7) / 8 * 8;
     default: return e;
   }
 }
 
 bool valid_op(int op, int dt) {
-  if (op < GBK_SUM || op > GBK_MINMAXLOC) return false;
+  if (op < GBK_SUM || op > GBK_MINMAXLOC_SUM) return false;
   if (dt < GBK_I32 || dt > GBK_F64) return false;
   if ((dt == GBK_F32 || dt == GBK_F64) && op >= GBK_LAND && op <= GBK_BOR) return false;
   return true;

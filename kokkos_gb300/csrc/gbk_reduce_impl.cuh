@@ -379,6 +379,7 @@ int reduce_typed(int op, const T* x, int64_t n, int64_t loc0, void* out, Workspa
     case GBK_MAXLOC: return launch_flat_cfg<RMaxLoc<T>, T>(x, n, loc0, out, w, t);
     case GBK_MINMAX: return launch_flat_cfg<RMinMax<T>, T>(x, n, loc0, out, w, t);
     case GBK_MINMAXLOC: return launch_flat_cfg<RMinMaxLoc<T>, T>(x, n, loc0, out, w, t);
+    case GBK_MINMAXLOC_SUM: return launch_flat_cfg<RMinMaxLocSum<T>, T>(x, n, loc0, out, w, t);
     default: break;
   }
   if constexpr (INT) {
@@ -405,6 +406,7 @@ int mdreduce_typed(int op, const T* base, const MDBox& b, void* out, Workspace* 
     case GBK_MAXLOC: return launch_md<RMaxLoc<T>, T>(base, b, out, w, t);
     case GBK_MINMAX: return launch_md<RMinMax<T>, T>(base, b, out, w, t);
     case GBK_MINMAXLOC: return launch_md<RMinMaxLoc<T>, T>(base, b, out, w, t);
+    case GBK_MINMAXLOC_SUM: return launch_md<RMinMaxLocSum<T>, T>(base, b, out, w, t);
     default: break;
   }
   if constexpr (INT) {

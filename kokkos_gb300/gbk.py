@@ -25,7 +25,7 @@ lib = ctypes.CDLL(LIB_PATH)
 DT = {"i32": 0, "i64": 1, "u32": 2, "u64": 3, "f32": 4, "f64": 5}
 NP = {0: np.int32, 1: np.int64, 2: np.uint32, 3: np.uint64, 4: np.float32, 5: np.float64}
 OPS = {"sum": 0, "prod": 1, "min": 2, "max": 3, "land": 4, "lor": 5, "band": 6, "bor": 7,
-       "minloc": 8, "maxloc": 9, "minmax": 10, "minmaxloc": 11}
+       "minloc": 8, "maxloc": 9, "minmax": 10, "minmaxloc": 11, "minmaxloc_sum": 12}
 STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "device timeout",
           5: "out of workspace", 6: "key out of range", 7: "no device"}
 
@@ -156,6 +156,8 @@ def result_nbytes(op, dt):
         return 2 * e
     if op == 11:
         return (2 * e + 7) // 8 * 8 + 16
+    if op == 12:
+        return (2 * e + 7) // 8 * 8 + 24
     return e
 
 
@@ -170,6 +172,11 @@ def result_dtype(op, dt):
         return np.dtype({"names": ["min_val", "max_val", "min_loc", "max_loc"],
                          "formats": [t, t, np.int64, np.int64],
                          "offsets": [0, t.itemsize, lo, lo + 8], "itemsize": lo + 16})
+    if op == 12:
+        lo = (2 * t.itemsize + 7) // 8 * 8
+        return np.dtype({"names": ["min_val", "max_val", "min_loc", "max_loc", "sum"],
+                         "formats": [t, t, np.int64, np.int64, t],
+                         "offsets": [0, t.itemsize, lo, lo + 8, lo + 16], "itemsize": lo + 24})
     return t
 
 

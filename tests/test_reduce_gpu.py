@@ -323,3 +323,62 @@ def test_sum_f64_split_fold_interval(env):
     del x
     torch.cuda.empty_cache()
     gbk.stream_check()
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int64, np.uint32, np.float32, np.float64])
+@pytest.mark.parametrize("n", [0, 1, 33, 4097, (1 << 20) + 5])
+def test_minmaxloc_sum_one_pass(env, dtype, n):
+    """MinMaxLoc and Sum as two reducers of one parallel_reduce (one pass):
+    the MinMaxLoc half equals the MinMaxLoc reducer's result exactly (ties:
+    first index), the Sum half matches the oracle (exact for integers,
+    within the Sum tolerances for floats); head/tail offsets included."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    t = np.dtype(dtype)
+    if t.kind == "f":
+        x = datagen.normal_f64(n + 3, seed=n + 11).astype(t)
+    elif t.kind == "i":
+        x = datagen.uniform_i64(n + 3, -1000, 1000, seed=n + 11).astype(t)
+    else:
+        x = datagen.uniform_i64(n + 3, 0, 100000, seed=n + 11).astype(t)
+    for off in (0, 1, 3):
+        xx = x[off:off + n]
+        got = gbk.reduce_value("minmaxloc_sum", _dev(torch, xx))
+        want = oracle.reduce("minmaxloc", xx, 4)
+        for nm in ("min_val", "max_val", "min_loc", "max_loc"):
+            assert np.asarray(got[nm]).tobytes() == np.asarray(want[nm]).tobytes(), (nm, off, got, want)
+        if t.kind == "f":
+            ok, info = sum_ok(got["sum"], xx, sum_tol(t))
+            assert ok, (off, info)
+        else:
+            assert np.asarray(got["sum"]).tobytes() == np.asarray(oracle.reduce("sum", xx, 4)).tobytes(), off
+    gbk.stream_check()
+
+
+def test_c2_minmaxloc_sum_one_pass_full_size(env):
+    """The C2 box (LayoutLeft View<float***> 512x512x256 of N(0,1)) reduced
+    once for MinLoc, MaxLoc and Sum together, and a strided sub-box through
+    the generic row kernel."""
+    gbk, torch = env
+    import oracle
+    from kokkos_gb300 import datagen
+    n0, n1, n2 = 512, 512, 256
+    x = datagen.normal_f32(n0 * n1 * n2, seed=0)
+    d = _dev(torch, x)
+    st = [1, n0, n0 * n1]
+    imin, imax = int(np.argmin(x)), int(np.argmax(x))
+    r = gbk.decode_result(gbk.mdrange_reduce("minmaxloc_sum", d, [0, 0, 0], [n0, n1, n2], st).cpu().numpy(), 12, 4)
+    assert r["min_val"] == x[imin] and r["min_loc"] == imin
+    assert r["max_val"] == x[imax] and r["max_loc"] == imax
+    ok, info = sum_ok(r["sum"], x, 1e-5)
+    assert ok, info
+    lo, up = [3, 5, 7], [500, 300, 200]
+    r = gbk.decode_result(gbk.mdrange_reduce("minmaxloc_sum", d, lo, up, st).cpu().numpy(), 12, 4)
+    want = oracle.mdrange_reduce("minmaxloc", x, lo, up, st, 4)
+    for nm in ("min_val", "max_val", "min_loc", "max_loc"):
+        assert np.asarray(r[nm]).tobytes() == np.asarray(want[nm]).tobytes(), nm
+    sub = x.reshape(n2, n1, n0)[7:200, 5:300, 3:500]
+    ok, info = sum_ok(r["sum"], np.ascontiguousarray(sub).ravel(), 1e-5)
+    assert ok, info
+    gbk.stream_check()
