@@ -18,6 +18,7 @@
 #pragma once
 
 #include <string>
+#include <utility>
 
 #include "reducers.hpp"
 
@@ -319,6 +320,115 @@ template <class P, class F, class T>
 void parallel_reduce(const std::string& label, const P& p, const F& f, T&& result) {
   Tools::Impl::LabelScope ls(label);
   parallel_reduce(p, f, std::forward<T>(result));
+}
+
+// ---- several reducers in one pass ----------------------------------------------
+// parallel_reduce(policy, f, r0, r1, ...) (core/src/impl/Kokkos_Combined_Reducer.hpp:
+// 533-620): the functor takes one value per reducer, f(i..., v0, v1, ...), and
+// every result is delivered to its own reducer's target; a plain arithmetic
+// result stands for a Sum into it.  The values travel through the kernels as
+// one packed value, joined component-wise.
+namespace Impl {
+template <class... V> struct VPack;
+template <class V0> struct VPack<V0> { V0 head; };
+template <class V0, class V1, class... Vs> struct VPack<V0, V1, Vs...> {
+  V0 head;
+  VPack<V1, Vs...> tail;
+};
+template <size_t K> struct PackGet {
+  template <class P> __host__ __device__ static auto& get(P& p) { return PackGet<K - 1>::get(p.tail); }
+};
+template <> struct PackGet<0> {
+  template <class P> __host__ __device__ static auto& get(P& p) { return p.head; }
+};
+
+template <class... R> struct RPack;
+template <class R0> struct RPack<R0> {
+  R0 head;
+  using value_type = VPack<typename R0::value_type>;
+  __device__ void init(value_type& v) const { head.init(v.head); }
+  __device__ void join(value_type& a, const value_type& b) const { head.join(a.head, b.head); }
+};
+template <class R0, class R1, class... Rs> struct RPack<R0, R1, Rs...> {
+  R0 head;
+  RPack<R1, Rs...> tail;
+  using value_type = VPack<typename R0::value_type, typename R1::value_type, typename Rs::value_type...>;
+  __device__ void init(value_type& v) const {
+    head.init(v.head);
+    tail.init(v.tail);
+  }
+  __device__ void join(value_type& a, const value_type& b) const {
+    head.join(a.head, b.head);
+    tail.join(a.tail, b.tail);
+  }
+};
+template <class R0> RPack<R0> make_rpack(const R0& r0) { return RPack<R0>{r0}; }
+template <class R0, class R1, class... Rs>
+RPack<R0, R1, Rs...> make_rpack(const R0& r0, const R1& r1, const Rs&... rs) {
+  return RPack<R0, R1, Rs...>{r0, make_rpack(r1, rs...)};
+}
+
+template <class... Rs>
+struct CombinedReducer {
+  using reducer = CombinedReducer;
+  using value_type = VPack<typename Rs::value_type...>;
+  RPack<Rs...> reds;
+  ResultRef<value_type> res;
+  __device__ void init(value_type& v) const { reds.init(v); }
+  __device__ void join(value_type& a, const value_type& b) const { reds.join(a, b); }
+};
+
+// The user functor seen through the packed value: one overload per policy kind.
+template <class F, class VP, size_t... Is>
+struct CombinedFunctor {
+  F f;
+  __device__ void operator()(int64_t i, VP& v) const { f(i, PackGet<Is>::get(v)...); }
+  __device__ void operator()(int64_t i, int64_t j, VP& v) const { f(i, j, PackGet<Is>::get(v)...); }
+  __device__ void operator()(int64_t i, int64_t j, int64_t k, VP& v) const { f(i, j, k, PackGet<Is>::get(v)...); }
+  __device__ void operator()(int64_t i, int64_t j, int64_t k, int64_t l, VP& v) const {
+    f(i, j, k, l, PackGet<Is>::get(v)...);
+  }
+  __device__ void operator()(const TeamMember& m, VP& v) const { f(m, PackGet<Is>::get(v)...); }
+};
+
+template <class A, std::enable_if_t<is_reducer<std::decay_t<A>>::value, bool> = true>
+std::decay_t<A> as_reducer(A&& a) {
+  return a;
+}
+template <class T, std::enable_if_t<std::is_arithmetic<T>::value, bool> = true>
+Sum<T> as_reducer(T& a) {
+  return Sum<T>(a);
+}
+
+template <class R>
+void deliver(const R& r, const typename R::value_type& v, cudaStream_t s) {
+  if (r.res.device) {
+    check_cuda(cudaMemcpyAsync(r.res.ptr, &v, sizeof(v), cudaMemcpyHostToDevice, s), "parallel_reduce");
+    check_cuda(cudaStreamSynchronize(s), "parallel_reduce");
+  } else {
+    *r.res.ptr = v;
+  }
+}
+
+template <class P, class F, size_t... Is, class... Rs>
+void combined_reduce(const P& p, const F& f, std::index_sequence<Is...>, const Rs&... rs) {
+  using VP = VPack<typename Rs::value_type...>;
+  VP host_val{};
+  CombinedReducer<Rs...> cr{make_rpack(rs...), ResultRef<VP>{&host_val, false}};
+  parallel_reduce(p, CombinedFunctor<F, VP, Is...>{f}, cr);
+  (deliver(rs, PackGet<Is>::get(host_val), p.space().stream()), ...);
+}
+}  // namespace Impl
+
+template <class P, class F, class A0, class A1, class... As, std::enable_if_t<Impl::is_policy<P>::value, bool> = true>
+void parallel_reduce(const P& p, const F& f, A0&& a0, A1&& a1, As&&... as) {
+  Impl::combined_reduce(p, f, std::make_index_sequence<2 + sizeof...(As)>{}, Impl::as_reducer(a0),
+                        Impl::as_reducer(a1), Impl::as_reducer(as)...);
+}
+template <class P, class F, class A0, class A1, class... As, std::enable_if_t<Impl::is_policy<P>::value, bool> = true>
+void parallel_reduce(const std::string& label, const P& p, const F& f, A0&& a0, A1&& a1, As&&... as) {
+  Tools::Impl::LabelScope ls(label);
+  parallel_reduce(p, f, std::forward<A0>(a0), std::forward<A1>(a1), std::forward<As>(as)...);
 }
 
 // ---- nested patterns inside a TeamPolicy functor ---------------------------------

@@ -110,6 +110,34 @@ static void test_range_reducers() {
     if (di(i) > u.val) { u.val = di(i); u.loc = i; }
   }, Kokkos::MaxLoc<int32_t, int64_t>(mx));
   report(mx.val == 7000 && mx.loc == n / 5, "range_maxloc_i32");
+  {  // several reducers in one pass (Kokkos_Combined_Reducer.hpp): MinLoc, MaxLoc, a Sum and a plain count
+    VL cmn, cmx;
+    double cs2 = 0;
+    int64_t pos = 0;
+    Kokkos::parallel_reduce("combined", Kokkos::RangePolicy<>(0, n),
+                            KOKKOS_LAMBDA(int64_t i, VL& a, VL& b, double& su, int64_t& c) {
+                              if (di(i) < a.val) { a.val = di(i); a.loc = i; }
+                              if (di(i) > b.val) { b.val = di(i); b.loc = i; }
+                              su += dx(i);
+                              if (di(i) > 0) c += 1;
+                            },
+                            Kokkos::MinLoc<int32_t, int64_t>(cmn), Kokkos::MaxLoc<int32_t, int64_t>(cmx),
+                            Kokkos::Sum<double>(cs2), pos);
+    int64_t hpos = 0;
+    for (int64_t i = 0; i < n; ++i) hpos += hi[i] > 0;
+    report(cmn.val == -5000 && cmn.loc == n / 3 && cmx.val == 7000 && cmx.loc == n / 5 &&
+               std::fabs(cs2 - cs) <= 1e-12 * a && pos == hpos,
+           "range_combined_minloc_maxloc_sum_count");
+    Kokkos::View<double*> dsum("dsum", 1);
+    int64_t pos2 = 0;
+    Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, n), KOKKOS_LAMBDA(int64_t i, double& su, int64_t& c) {
+      su += dx(i);
+      c += di(i) > 0;
+    }, Kokkos::Sum<double>(dsum), pos2);
+    double hsum = 0;
+    Kokkos::check_cuda(cudaMemcpy(&hsum, dsum.data(), sizeof(double), cudaMemcpyDeviceToHost), "copy");
+    report(std::fabs(hsum - cs) <= 1e-12 * a && pos2 == hpos, "range_combined_view_result");
+  }
   Kokkos::MinMaxScalar<int32_t> mm;
   Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, n), KOKKOS_LAMBDA(int64_t i, Kokkos::MinMaxScalar<int32_t>& u) {
     if (di(i) < u.min_val) u.min_val = di(i);
@@ -163,6 +191,24 @@ static void test_mdrange() {
                           Kokkos::MaxLoc<float, int64_t>(mx));
   report(mn.val == -3.f && mn.loc == imin, "mdrange_minloc_f32");
   report(mx.val == 3.f && mx.loc == imax, "mdrange_maxloc_f32");
+  {
+    V cmn, cmx;
+    double cs3 = 0;
+    Kokkos::parallel_reduce(Kokkos::MDRangePolicy<Kokkos::Rank<3>>({0, 0, 0}, {n0, n1, n2}),
+                            KOKKOS_LAMBDA(int64_t i, int64_t j, int64_t k, V& a, V& b, double& su) {
+                              const float v = x(i, j, k);
+                              const int64_t l = i + n0 * (j + n1 * k);
+                              if (v < a.val) { a.val = v; a.loc = l; }
+                              if (v > b.val) { b.val = v; b.loc = l; }
+                              su += v;
+                            },
+                            Kokkos::MinLoc<float, int64_t>(cmn), Kokkos::MaxLoc<float, int64_t>(cmx), cs3);
+    double hs3 = 0;
+    for (float v : h) hs3 += v;
+    report(cmn.val == -3.f && cmn.loc == imin && cmx.val == 3.f && cmx.loc == imax &&
+               std::fabs(cs3 - hs3) <= 1e-9 * std::fabs(hs3) + 1e-9,
+           "mdrange_combined_minloc_maxloc_sum");
+  }
   // LOr over a sub-box, rank 2 (TestMDRangeReduce: bounds {0,1,7,32,65,7000})
   for (int64_t e : {0L, 1L, 7L, 32L, 65L, 7000L}) {
     int32_t lor = 0;
@@ -219,6 +265,18 @@ static void test_team() {
     if (t.team_rank() == 0) u += ts;
   }, lsum);
   report(lsum == tot, "team_league_reduce");
+  int64_t lsum2 = 0, lcnt = 0;
+  Kokkos::parallel_reduce(TP(league, 128), KOKKOS_LAMBDA(const TP::member_type& t, int64_t& u, int64_t& c) {
+    const int64_t s = t.league_rank();
+    int64_t ts = 0;
+    Kokkos::parallel_reduce(Kokkos::TeamThreadRange(t, doff(s), doff(s + 1)),
+                            [&](int64_t i, int64_t& w) { w += dv(i); }, ts);
+    if (t.team_rank() == 0) {
+      u += ts;
+      c += 1;
+    }
+  }, lsum2, lcnt);
+  report(lsum2 == tot && lcnt == league, "team_combined_reduce");
   // team scan: per-segment exclusive prefix inside each team
   Kokkos::View<int64_t*> pre("pre", (int64_t)v.size());
   Kokkos::parallel_for(TP(league, 64), KOKKOS_LAMBDA(const TP::member_type& t) {
