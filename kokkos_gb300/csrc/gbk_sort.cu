@@ -31,6 +31,8 @@
 //    counts) instead of an inter-tile look-back, whose walk grows with the
 //    number of tiles in flight.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "gbk_internal.cuh"
@@ -103,6 +105,33 @@ __device__ __forceinline__ unsigned rank_row(unsigned short* cnt, unsigned d, bo
   b = __shfl_sync(0xffffffffu, b, leader < 0 ? lane : leader);
   __syncwarp();
   return b + (unsigned)__popc(m & ((1u << lane) - 1u));
+}
+
+// The same rank from a per-warp array of 256 lane masks in shared memory
+// (zero between rows): every lane ORs its bit into its digit's mask, reads
+// the mask back as its peer set, and the group's lowest lane advances the
+// count and clears the mask.  About a third of the instructions of the
+// eight ballots; lanes sharing a digit serialise on its word, so the host
+// picks it only for passes where no digit value holds a large share of the
+// keys.
+template <bool ALL>
+__device__ __forceinline__ unsigned rank_row_or(unsigned short* cnt, unsigned* masks, unsigned d, bool ok,
+                                                int lane) {
+  const unsigned bit = 1u << lane;
+  if (ALL || ok) atomicOr(&masks[d], bit);
+  __syncwarp();
+  const unsigned m = (ALL || ok) ? masks[d] : 0u;
+  __syncwarp();  // every lane has read its mask before the leader clears it
+  const int leader = __ffs(m) - 1;
+  unsigned b = 0;
+  if ((ALL || ok) && lane == leader) {
+    b = cnt[d];
+    cnt[d] = (unsigned short)(b + (unsigned)__popc(m));
+    masks[d] = 0u;
+  }
+  b = __shfl_sync(0xffffffffu, b, leader < 0 ? lane : leader);
+  __syncwarp();
+  return b + (unsigned)__popc(m & (bit - 1u));
 }
 
 // After a wait that gave up: wait (bounded) for the bulk copies still in
@@ -255,7 +284,7 @@ template <> struct ScVar<0> { static constexpr int BLOCK = 256, KPT = 16, MINB =
 template <int KB, int VB, int VAR> struct ScShape {
   static constexpr int BLOCK = ScVar<VAR>::BLOCK, MINB = ScVar<VAR>::MINB;
   static constexpr int WARPS = BLOCK / 32;
-  static constexpr int STATIC_BYTES = WARPS * 256 * 4 + 256 * 8 + 256;  // counters, offsets, bases, misc
+  static constexpr int STATIC_BYTES = WARPS * 256 * 6 + 256 * 8 + 256;  // counters, masks/offsets, bases, misc
   static constexpr int BUDGET = 233472 / MINB - 1024 - STATIC_BYTES;  // per CTA, 1 KiB reserved per CTA
   // keys per thread: doubled for 4-byte keys alone, halved when two stages
   // of the widest elements would not fit
@@ -276,6 +305,7 @@ struct ScatterArgs {
   int64_t tiles_per_chunk;
   int64_t wait_limit;
   int shift;
+  int rank_or;  // rank with the shared lane masks (rank_row_or) instead of ballots
 };
 
 // Grid = nchunks, MINB CTAs per SM.  TMA: kin/vin 16-byte aligned, tiles
@@ -293,7 +323,11 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
   extern __shared__ __align__(128) unsigned char ring[];
   __shared__ __align__(8) unsigned long long s_bar[STAGES];
   __shared__ unsigned short s_cnt[WARPS][256];  // per-warp digit counts of the tile (rank_row)
-  __shared__ unsigned short s_off[WARPS][256];  // tile-local slot of each warp's first key of each digit
+  // per-warp lane masks of rank_row_or while a tile is ranked; afterwards the
+  // first half holds s_off: the tile-local slot of each warp's first key of
+  // each digit
+  __shared__ __align__(16) unsigned s_rk[WARPS * 256];
+  unsigned short(*s_off)[256] = reinterpret_cast<unsigned short(*)[256]>(s_rk);
   __shared__ long long s_gb[256];               // global position of tile slot 0 of each digit
   __shared__ unsigned s_wsum[8];
   __shared__ int s_oob;  // a digit range of the current tile falls outside [0, n)
@@ -338,7 +372,10 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
     for (; q < nc; ++q) r += cp[q * 256];
     run = r;
   }
-  for (int i = threadIdx.x; i < WARPS * 256; i += BLOCK) (&s_cnt[0][0])[i] = 0;
+  for (int i = threadIdx.x; i < WARPS * 256; i += BLOCK) {
+    (&s_cnt[0][0])[i] = 0;
+    s_rk[i] = 0u;
+  }
   if (threadIdx.x == 0) s_oob = 0;
   __syncthreads();
   const int wb = warp * 32 * KPT;  // the warp's first slot in the tile
@@ -367,8 +404,13 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
         if (VB) val[k] = s_vals[slot];
         dig[k] = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
       }
+      if (A.rank_or) {
 #pragma unroll
-      for (int k = 0; k < KPT; ++k) rk[k] = rank_row<true>(s_cnt[warp], dig[k], true, lane);
+        for (int k = 0; k < KPT; ++k) rk[k] = rank_row_or<true>(s_cnt[warp], s_rk + warp * 256, dig[k], true, lane);
+      } else {
+#pragma unroll
+        for (int k = 0; k < KPT; ++k) rk[k] = rank_row<true>(s_cnt[warp], dig[k], true, lane);
+      }
     } else {
 #pragma unroll
       for (int k = 0; k < KPT; ++k) {
@@ -378,8 +420,14 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
         if (VB) val[k] = slot < cv ? s_vals[slot] : (ok ? vin[base + slot] : V(0));
         dig[k] = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
       }
+      if (A.rank_or) {
 #pragma unroll
-      for (int k = 0; k < KPT; ++k) rk[k] = rank_row<false>(s_cnt[warp], dig[k], wb + k * 32 + lane < cnt, lane);
+        for (int k = 0; k < KPT; ++k)
+          rk[k] = rank_row_or<false>(s_cnt[warp], s_rk + warp * 256, dig[k], wb + k * 32 + lane < cnt, lane);
+      } else {
+#pragma unroll
+        for (int k = 0; k < KPT; ++k) rk[k] = rank_row<false>(s_cnt[warp], dig[k], wb + k * 32 + lane < cnt, lane);
+      }
     }
     if (__syncthreads_or(bad)) {  // counts complete and every key read, or a copy never arrived
       failed = j;
@@ -438,6 +486,10 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
       }
     }
     __syncthreads();
+    if (A.rank_or) {  // s_off is dead: clear the lane masks for the next tile (visible after the loop's barrier)
+      uint4* z = reinterpret_cast<uint4*>(s_rk);
+      for (int i = threadIdx.x; i < WARPS * 256 / 4; i += BLOCK) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
     // ---- write the runs of equal digits ---------------------------------------
     auto emit = [&](int i) {
       const K kk = s_keys[i];
@@ -503,6 +555,18 @@ int launch_pass(const void* kin, void* kout, const void* vin, void* vout, int64_
   return cuda_status(cudaGetLastError());
 }
 
+// Ranking of the scatter passes: GBK_SORT_RANK=masks or =ballot in the
+// environment forces one method for every pass; otherwise it is chosen per
+// pass from the digit histogram.
+int sort_rank_mode() {
+  static int mode = -1;
+  if (mode < 0) {
+    const char* e = getenv("GBK_SORT_RANK");
+    mode = (e && !strcmp(e, "masks")) ? 1 : (e && !strcmp(e, "ballot")) ? 2 : 0;
+  }
+  return mode;
+}
+
 template <int DT, int VB, int VAR>
 int sort_var(void* keys, void* vals, int64_t n, Workspace* w) {
   using K = typename Radix<DT>::K;
@@ -566,6 +630,7 @@ int sort_var(void* keys, void* vals, int64_t n, Workspace* w) {
   K* kout = ktmp;
   V* vin = (V*)vals;
   V* vout = vtmp;
+  const int rank_mode = sort_rank_mode();
   for (size_t i = 0; i < passes.size(); ++i) {
     const int p = passes[i];
     ScatterArgs A;
@@ -575,6 +640,10 @@ int sort_var(void* keys, void* vals, int64_t n, Workspace* w) {
     A.tiles_per_chunk = tpc;
     A.wait_limit = wait_limit();
     A.shift = 8 * p;
+    // Lane-mask ranking unless one digit value holds more than 1/32 of the keys.
+    unsigned long long hmax = 0;
+    for (int d = 0; d < 256; ++d) hmax = std::max(hmax, h[p * 256 + d]);
+    A.rank_or = (rank_mode == 1 || (rank_mode == 0 && (int64_t)hmax * 32 <= n)) ? 1 : 0;
     // the first pass uses the per-chunk counts of the all-digit histogram
     unsigned* counts = i == 0 ? d_cc + (size_t)p * nchunks * 256 : d_c1;
     const bool tma = kin != (K*)keys || user_aligned;
