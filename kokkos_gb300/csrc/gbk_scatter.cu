@@ -153,17 +153,30 @@ __global__ void __launch_bounds__(BLOCK, 1)
       atomicAdd(sh + (hi ? k - nwords : k), add << (hi ? 16 : 0));
     }
   };
+  auto drain_word = [&](int i, unsigned w) {
+    const unsigned hi = w & 0x80008000u;
+    if (hi) {
+      sh[i] = w - hi;
+      if (hi & 0x8000u) red_add_u64(bins + i, 0x8000ull);
+      if (hi & 0x80000000u) red_add_u64(bins + nwords + i, 0x8000ull);
+    }
+  };
+  // Every word is scanned once per drain (as many word reads as keys
+  // between drains): 16-byte reads and one test per four words.
   auto drain = [&]() {
     __syncthreads();
-    for (int i = threadIdx.x; i < nwords; i += BLOCK) {
-      const unsigned w = sh[i];
-      const unsigned hi = w & 0x80008000u;
-      if (hi) {
-        sh[i] = w - hi;
-        if (hi & 0x8000u) red_add_u64(bins + i, 0x8000ull);
-        if (hi & 0x80000000u) red_add_u64(bins + nwords + i, 0x8000ull);
+    const int nq = nwords >> 2;
+    const uint4* sq = reinterpret_cast<const uint4*>(sh);
+    for (int i = threadIdx.x; i < nq; i += BLOCK) {
+      const uint4 w = sq[i];
+      if ((w.x | w.y | w.z | w.w) & 0x80008000u) {
+        drain_word(4 * i, w.x);
+        drain_word(4 * i + 1, w.y);
+        drain_word(4 * i + 2, w.z);
+        drain_word(4 * i + 3, w.w);
       }
     }
+    for (int i = 4 * nq + threadIdx.x; i < nwords; i += BLOCK) drain_word(i, sh[i]);
     __syncthreads();
   };
   int64_t v = v0;

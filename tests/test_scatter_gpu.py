@@ -71,6 +71,20 @@ def test_hist16_saturating_bins(env, variant):
         np.testing.assert_array_equal(bins.cpu().numpy(), want)
 
 
+@pytest.mark.parametrize("variant", [0x20, 0x30])
+def test_hist16_saturating_ragged_words(env, variant):
+    """16-bit counters when the word count is not a multiple of four (4,099
+    bins: 2,050 words): the hot bins sit in the last words, which the drain
+    scans one by one, and share a word (bins 2,048 and 4,098)."""
+    gbk, torch = env
+    nb = 4099
+    keys = np.tile(np.array([2048, 4098, 2048, 2049, 4098, 0], dtype=np.int32), 700001)
+    bins = torch.zeros(nb, dtype=torch.int64, device="cuda")
+    gbk.histogram(_dev(torch, keys), bins, tune=(0, 0, 0, variant))
+    gbk.stream_check()
+    np.testing.assert_array_equal(bins.cpu().numpy(), np.bincount(keys, minlength=nb))
+
+
 def test_c2_histogram_full_size(env):
     """ScatterView histogram of 2^26 int32 Zipf(1.1) keys over 2^16 bins into
     int64 counts: bit-exact."""
