@@ -130,27 +130,35 @@ __global__ void __launch_bounds__(BLOCK, 1)
   constexpr int DRAIN = 32768 / (ROUND * 4);   // rounds between drains
   static_assert(DRAIN >= 1, "round too large for 16-bit counters");
   const int nwords = (int)((nbins + 1) >> 1);
-  for (int i = threadIdx.x; i < nwords; i += BLOCK) sh[i] = 0u;
+  for (int i = threadIdx.x; i <= nwords; i += BLOCK) sh[i] = 0u;  // the counters and the spare word
   __syncthreads();
   bool bad = false;
   // Contiguous, balanced share of the vectors for this CTA.
   const int64_t per = nvec / gridDim.x, rem = nvec % gridDim.x;
   const int64_t v0 = blockIdx.x * per + (blockIdx.x < rem ? blockIdx.x : rem);
   const int64_t v1 = v0 + per + (blockIdx.x < rem ? 1 : 0);
+  const unsigned nb32 = (unsigned)nbins, nw32 = (unsigned)nwords;  // nbins fits the 200 KiB of counters
   auto count = [&](int32_t k) {
-    const bool ok = (uint32_t)k < (uint64_t)nbins;
-    if (!ok) bad = true;
-    unsigned add = 1;
-    bool leader = ok;
     if (AGG) {
+      const bool ok = (uint32_t)k < (uint64_t)nbins;
+      if (!ok) bad = true;
       const unsigned act = __activemask();
       const unsigned peers = __match_any_sync(act, ok ? k : -1);
-      leader = ok && ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1));
-      add = __popc(peers);
-    }
-    if (leader) {
-      const bool hi = k >= nwords;
-      atomicAdd(sh + (hi ? k - nwords : k), add << (hi ? 16 : 0));
+      const bool leader = ok && ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1));
+      const unsigned add = __popc(peers);
+      if (leader) {
+        const bool hi = k >= nwords;
+        atomicAdd(sh + (hi ? k - nwords : k), add << (hi ? 16 : 0));
+      }
+    } else {
+      // Branch-free: a key outside the bins counts into the spare word
+      // sh[nwords] (never drained nor flushed) and raises the error flag.
+      const unsigned uk = (unsigned)k;
+      const bool ok = uk < nb32;
+      bad = bad || !ok;
+      const unsigned hi = uk >= nw32 ? 1u : 0u;
+      const unsigned word = ok ? uk - (hi ? nw32 : 0u) : nw32;
+      atomicAdd(sh + word, 1u << (hi << 4));
     }
   };
   auto drain_word = [&](int i, unsigned w) {
@@ -235,7 +243,7 @@ __global__ void k_hist_edges(const int32_t* __restrict__ keys, int64_t head, int
 template <bool AGG>
 int launch_hist16(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, Workspace* w) {
   constexpr int BLOCK = 1024;
-  const size_t smem = (size_t)((nbins + 1) >> 1) * 4;
+  const size_t smem = (size_t)((nbins + 1) >> 1) * 4 + 16;  // counters, then the spare word for keys outside the bins
   auto kfn = k_hist16<BLOCK, AGG>;
   GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uintptr_t a = (uintptr_t)keys;

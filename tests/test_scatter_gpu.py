@@ -113,6 +113,25 @@ def test_out_of_range_keys_flagged(env):
     gbk.stream_check()  # the flag was cleared
 
 
+@pytest.mark.parametrize("variant", [0x20, 0x30])
+def test_hist16_out_of_range_keys(env, variant):
+    """16-bit counters: keys below 0 or at and above nbins (odd nbins, so
+    the last word's high half is not a bin) are left out of every bin and
+    raise the key-range status; the valid keys count exactly."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    nb = 40001
+    keys = datagen.uniform_i64(2000003, -50, nb + 50, seed=3).astype(np.int32)
+    bins = torch.zeros(nb, dtype=torch.int64, device="cuda")
+    gbk.histogram(_dev(torch, keys), bins, tune=(0, 0, 0, variant))
+    with pytest.raises(gbk.GbkError) as e:
+        gbk.stream_check()
+    assert e.value.status == 6
+    ok = keys[(keys >= 0) & (keys < nb)]
+    np.testing.assert_array_equal(bins.cpu().numpy(), np.bincount(ok, minlength=nb))
+    gbk.stream_check()
+
+
 @pytest.mark.parametrize("op", ["sum", "min", "max", "prod"])
 @pytest.mark.parametrize("dt", ["i32", "i64", "u64", "f32", "f64"])
 def test_scatter_ops(env, op, dt):
