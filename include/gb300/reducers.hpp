@@ -232,6 +232,46 @@ using MaxFirstLoc = MaxFirstLocCustomComparator<T, I, Impl::Less, Space>;
 template <class T, class I = int64_t, class Space = GB300Space>
 using MinMaxFirstLastLoc = MinMaxFirstLastLocCustomComparator<T, I, Impl::Less, Space>;
 
+// FirstLoc / LastLoc (Kokkos_Parallel_Reduce.hpp:1103-1220): the smallest /
+// largest index at which the functor found its predicate true; the
+// identities are the index type's largest / smallest value.
+template <class I>
+struct FirstLocScalar {
+  I min_loc_true;
+};
+template <class I>
+struct LastLocScalar {
+  I max_loc_true;
+};
+template <class I, class Space = GB300Space>
+struct FirstLoc : Impl::ReducerBase<FirstLoc<I, Space>, FirstLocScalar<I>> {
+  static_assert(std::is_integral<I>::value, "FirstLoc takes an integral index type");
+  using V = FirstLocScalar<I>;
+  using reducer = FirstLoc;
+  using value_type = V;
+  __host__ __device__ FirstLoc(V& r) : Impl::ReducerBase<FirstLoc, V>(r) {}
+  template <class D, class... P>
+  FirstLoc(const View<D, P...>& v) : Impl::ReducerBase<FirstLoc, V>(v) {}
+  __device__ void init(V& v) const { v.min_loc_true = gbk::lim<I>::hi(); }
+  __device__ void join(V& a, const V& b) const {
+    if (b.min_loc_true < a.min_loc_true) a.min_loc_true = b.min_loc_true;
+  }
+};
+template <class I, class Space = GB300Space>
+struct LastLoc : Impl::ReducerBase<LastLoc<I, Space>, LastLocScalar<I>> {
+  static_assert(std::is_integral<I>::value, "LastLoc takes an integral index type");
+  using V = LastLocScalar<I>;
+  using reducer = LastLoc;
+  using value_type = V;
+  __host__ __device__ LastLoc(V& r) : Impl::ReducerBase<LastLoc, V>(r) {}
+  template <class D, class... P>
+  LastLoc(const View<D, P...>& v) : Impl::ReducerBase<LastLoc, V>(v) {}
+  __device__ void init(V& v) const { v.max_loc_true = gbk::lim<I>::lo(); }
+  __device__ void join(V& a, const V& b) const {
+    if (b.max_loc_true > a.max_loc_true) a.max_loc_true = b.max_loc_true;
+  }
+};
+
 namespace Impl {
 // A custom joiner with no neutral element (std transform_reduce / reduce with
 // a user joiner): the value carries a "has a value" flag, the identity is an

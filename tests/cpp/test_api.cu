@@ -138,6 +138,37 @@ static void test_range_reducers() {
     Kokkos::check_cuda(cudaMemcpy(&hsum, dsum.data(), sizeof(double), cudaMemcpyDeviceToHost), "copy");
     report(std::fabs(hsum - cs) <= 1e-12 * a && pos2 == hpos, "range_combined_view_result");
   }
+  {  // FirstLoc / LastLoc of a predicate, alone and as two reducers of one pass
+    using FL = Kokkos::FirstLoc<int64_t>;
+    using LL = Kokkos::LastLoc<int64_t>;
+    FL::value_type f1;
+    Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, n), KOKKOS_LAMBDA(int64_t i, FL::value_type& u) {
+      if (di(i) > 900 && i < u.min_loc_true) u.min_loc_true = i;
+    }, FL(f1));
+    FL::value_type f2;
+    LL::value_type l2;
+    Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, n),
+                            KOKKOS_LAMBDA(int64_t i, FL::value_type& u, LL::value_type& w) {
+                              if (di(i) > 900) {
+                                if (i < u.min_loc_true) u.min_loc_true = i;
+                                if (i > w.max_loc_true) w.max_loc_true = i;
+                              }
+                            },
+                            FL(f2), LL(l2));
+    int64_t hf = -1, hl = -1;
+    for (int64_t i = 0; i < n; ++i)
+      if (hi[i] > 900) {
+        if (hf < 0) hf = i;
+        hl = i;
+      }
+    FL::value_type none;
+    Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, n), KOKKOS_LAMBDA(int64_t i, FL::value_type& u) {
+      if (di(i) > 100000 && i < u.min_loc_true) u.min_loc_true = i;
+    }, FL(none));
+    report(f1.min_loc_true == hf && f2.min_loc_true == hf && l2.max_loc_true == hl &&
+               none.min_loc_true == std::numeric_limits<int64_t>::max(),
+           "range_firstloc_lastloc");
+  }
   Kokkos::MinMaxScalar<int32_t> mm;
   Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, n), KOKKOS_LAMBDA(int64_t i, Kokkos::MinMaxScalar<int32_t>& u) {
     if (di(i) < u.min_val) u.min_val = di(i);
