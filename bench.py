@@ -425,6 +425,7 @@ def main():
                          "with an int32 iota payload (the sort_by_key workload, 2^27 by default), or segsum / segscan: the "
                          "segmented Sum (f32) / inclusive_scan (i32) of --seg-total elements in lognormal segments")
     ap.add_argument("--sort-n", type=int, default=1 << 27)
+    ap.add_argument("--sum-n", type=int, default=1 << 24, help="elements for --only sum_f64 / exscan")
     ap.add_argument("--seg-total", type=int, default=1 << 28,
                     help="--only segsum: elements of the lognormal segments (10,000 segments per 2^28, median 2,048)")
     ap.add_argument("--sort-keys", default="uniform", choices=["uniform", "lowentropy"],
@@ -500,7 +501,7 @@ def main():
         print(json.dumps({"only": args.only, "elements": ns, "segments": nseg, "launches": args.warmup + args.steps}))
         return
     if args.only in ("sum_f64", "exscan"):
-        n = 1 << 24
+        n = args.sum_n
         res = torch.zeros(64, dtype=torch.uint8, device=dev)
         if args.only == "sum_f64":
             x = torch.from_numpy(datagen.uniform_f64(n, seed=0)).to(dev)
