@@ -430,6 +430,16 @@ void parallel_reduce(const std::string& label, const P& p, const F& f, A0&& a0, 
   Tools::Impl::LabelScope ls(label);
   parallel_reduce(p, f, std::forward<A0>(a0), std::forward<A1>(a1), std::forward<As>(as)...);
 }
+// ... and over [0, n) (Kokkos_Combined_Reducer.hpp:597-620)
+template <class N, class F, class A0, class A1, class... As, std::enable_if_t<std::is_integral<N>::value, bool> = true>
+void parallel_reduce(N n, const F& f, A0&& a0, A1&& a1, As&&... as) {
+  parallel_reduce(RangePolicy<>(0, (int64_t)n), f, std::forward<A0>(a0), std::forward<A1>(a1), std::forward<As>(as)...);
+}
+template <class N, class F, class A0, class A1, class... As, std::enable_if_t<std::is_integral<N>::value, bool> = true>
+void parallel_reduce(const std::string& label, N n, const F& f, A0&& a0, A1&& a1, As&&... as) {
+  Tools::Impl::LabelScope ls(label);
+  parallel_reduce(RangePolicy<>(0, (int64_t)n), f, std::forward<A0>(a0), std::forward<A1>(a1), std::forward<As>(as)...);
+}
 
 // ---- nested patterns inside a TeamPolicy functor ---------------------------------
 // (host-device because they are called from KOKKOS_LAMBDA bodies; they only

@@ -137,6 +137,14 @@ static void test_range_reducers() {
     double hsum = 0;
     Kokkos::check_cuda(cudaMemcpy(&hsum, dsum.data(), sizeof(double), cudaMemcpyDeviceToHost), "copy");
     report(std::fabs(hsum - cs) <= 1e-12 * a && pos2 == hpos, "range_combined_view_result");
+    int64_t pos3 = 0, neg3 = 0;
+    Kokkos::parallel_reduce("count", n, KOKKOS_LAMBDA(int64_t i, int64_t& p, int64_t& q) {
+      p += di(i) > 0;
+      q += di(i) < 0;
+    }, pos3, neg3);
+    int64_t hneg = 0;
+    for (int64_t i = 0; i < n; ++i) hneg += hi[i] < 0;
+    report(pos3 == hpos && neg3 == hneg, "range_combined_count_form");
   }
   {  // FirstLoc / LastLoc of a predicate, alone and as two reducers of one pass
     using FL = Kokkos::FirstLoc<int64_t>;
