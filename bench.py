@@ -53,9 +53,9 @@ STEP_BYTES = 3 * RED_BYTES + HIST_BYTES
 # The dominant kernel and its DRAM traffic per launch (dram__bytes_read.sum +
 # dram__bytes_write.sum from one ncu capture of the same launch, as recorded
 # in profiles/).
-ROOF_KERNEL = ("flat reduce of the box, MinLoc/MaxLoc/Sum f32 (with the autotuner table: k_reduce_tma shared-memory "
-               "ring, 2 CTAs/SM, for MinLoc and Sum; k_reduce_flat load-pipelined for MaxLoc)")
-ROOF_TRAFFIC = 272138240  # MinLoc f32 over the box: 268.48 MB read + 3.66 MB written
+ROOF_KERNEL = ("flat reduce of the box, MinLoc/MaxLoc/Sum f32 (with the autotuner table: k_reduce_flat load-pipelined "
+               "512 x 4, 2 CTAs/SM, for MinLoc and MaxLoc; k_reduce_tma shared-memory ring, 2 CTAs/SM, for Sum)")
+ROOF_TRAFFIC = 271620000  # MinLoc f32 over the box, load-pipelined kernel: 268.69 MB read + 2.93 MB written (ncu, MB precision)
 WORKLOAD = ("MDRange<Rank<3>> MinLoc+MaxLoc+Sum over LayoutLeft View<float***> 512x512x256 N(0,1) "
             "+ ScatterView histogram 2^26 int32 Zipf(1.1) keys -> 2^16 int64 bins")
 

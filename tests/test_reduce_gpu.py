@@ -203,15 +203,20 @@ def test_tuning_configs_agree(env):
     d, df = _dev(torch, x), _dev(torch, xf)
     w = oracle.reduce("sum", x, 1)
     wl = oracle.reduce("minloc", xf, 1)
+    wm = oracle.reduce("maxloc", xf, 1)
     for blk, un, cps in [(256, 2, 8), (256, 4, 8), (512, 2, 4), (512, 4, 2), (128, 8, 16), (256, 8, 4), (1024, 2, 2),
                          (256, 4, 1)]:
-        got = gbk.decode_result(gbk.reduce("sum", d, tune=(blk, un, cps, 0)).cpu().numpy(), 0, 0)
-        assert got == w, (blk, un, cps)
-        gl = gbk.decode_result(gbk.reduce("minloc", df, tune=(blk, un, cps, 0)).cpu().numpy(), 8, 4)
-        assert gl["val"] == wl["val"] and gl["loc"] == wl["loc"]
-        gs = gbk.decode_result(gbk.reduce("sum", df, tune=(blk, un, cps, 0)).cpu().numpy(), 0, 4)
-        ok, info = sum_ok(gs, xf, 1e-5)
-        assert ok, info
+        for var in (0, 1):  # 0: the ring kernel at this size; 1: the load-pipelined kernel with this shape
+            tune = (blk, un, cps, var)
+            got = gbk.decode_result(gbk.reduce("sum", d, tune=tune).cpu().numpy(), 0, 0)
+            assert got == w, tune
+            gl = gbk.decode_result(gbk.reduce("minloc", df, tune=tune).cpu().numpy(), 8, 4)
+            assert gl["val"] == wl["val"] and gl["loc"] == wl["loc"], tune
+            gm = gbk.decode_result(gbk.reduce("maxloc", df, tune=tune).cpu().numpy(), 9, 4)
+            assert gm["val"] == wm["val"] and gm["loc"] == wm["loc"], tune
+            gs = gbk.decode_result(gbk.reduce("sum", df, tune=tune).cpu().numpy(), 0, 4)
+            ok, info = sum_ok(gs, xf, 1e-5)
+            assert ok, (tune, info)
 
 
 @pytest.mark.parametrize("n", [4099, (1 << 21) + 7, (1 << 22) + 3])
