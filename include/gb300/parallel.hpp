@@ -399,6 +399,10 @@ template <class T, std::enable_if_t<std::is_arithmetic<T>::value, bool> = true>
 Sum<T> as_reducer(T& a) {
   return Sum<T>(a);
 }
+template <class D, class... P>
+Sum<typename View<D, P...>::non_const_value_type> as_reducer(const View<D, P...>& v) {  // a View result: its first element
+  return Sum<typename View<D, P...>::non_const_value_type>(v);
+}
 
 template <class R>
 void deliver(const R& r, const typename R::value_type& v, cudaStream_t s) {

@@ -137,6 +137,14 @@ static void test_range_reducers() {
     double hsum = 0;
     Kokkos::check_cuda(cudaMemcpy(&hsum, dsum.data(), sizeof(double), cudaMemcpyDeviceToHost), "copy");
     report(std::fabs(hsum - cs) <= 1e-12 * a && pos2 == hpos, "range_combined_view_result");
+    Kokkos::View<int64_t*> dcount("dcount", 1);
+    int64_t neg4 = 0;
+    Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, n), KOKKOS_LAMBDA(int64_t i, int64_t& p, int64_t& q) {
+      p += di(i) > 0;
+      q += di(i) < 0;
+    }, dcount, neg4);  // a View result stands for a Sum into it, as a scalar does
+    int64_t hcount = -1;
+    Kokkos::check_cuda(cudaMemcpy(&hcount, dcount.data(), sizeof(int64_t), cudaMemcpyDeviceToHost), "copy");
     int64_t pos3 = 0, neg3 = 0;
     Kokkos::parallel_reduce("count", n, KOKKOS_LAMBDA(int64_t i, int64_t& p, int64_t& q) {
       p += di(i) > 0;
@@ -145,6 +153,7 @@ static void test_range_reducers() {
     int64_t hneg = 0;
     for (int64_t i = 0; i < n; ++i) hneg += hi[i] < 0;
     report(pos3 == hpos && neg3 == hneg, "range_combined_count_form");
+    report(hcount == hpos && neg4 == hneg, "range_combined_view_as_sum");
   }
   {  // FirstLoc / LastLoc of a predicate, alone and as two reducers of one pass
     using FL = Kokkos::FirstLoc<int64_t>;
