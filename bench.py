@@ -36,6 +36,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -56,6 +57,7 @@ STEP_BYTES = 3 * RED_BYTES + HIST_BYTES
 ROOF_KERNEL = ("flat reduce of the box, MinLoc/MaxLoc/Sum f32 (with the autotuner table: k_reduce_flat load-pipelined "
                "512 x 4, 2 CTAs/SM, for MinLoc and MaxLoc; k_reduce_tma shared-memory ring, 2 CTAs/SM, for Sum)")
 ROOF_TRAFFIC = 271620000  # MinLoc f32 over the box, load-pipelined kernel: 268.69 MB read + 2.93 MB written (ncu, MB precision)
+METRIC = "HBM GB/s (algorithmic bytes / step time) of MDRange reduce + ScatterView histogram"
 WORKLOAD = ("MDRange<Rank<3>> MinLoc+MaxLoc+Sum over LayoutLeft View<float***> 512x512x256 N(0,1) "
             "+ ScatterView histogram 2^26 int32 Zipf(1.1) keys -> 2^16 int64 bins")
 
@@ -114,9 +116,8 @@ class Clocks:
 
     def __init__(self, gpu_index):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"gbk_clocks_{os.getpid()}.csv")
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
@@ -160,29 +161,42 @@ class Clocks:
 
 
 def cpu_baseline(budget_s=12.0):
-    """Oracle (CPU restatement of the reference OpenMP reduce and ScatterView
-    algorithms) over the same workload on this host's cores: full-size
-    inputs, as many whole steps as fit in the time budget (at least one)."""
+    """Oracle (CPU restatement of the reference OpenMP MDRange reduce and
+    Duplicated ScatterView algorithms) over the same workload on this host's
+    cores: full-size inputs, as many whole steps as fit in the time budget
+    (at least one).  The reduces walk the box as the reference's host
+    backend does for MDRangePolicy<Rank<3>> (Iterate::Right outer and inner,
+    default tiles {2, 2, 256}) over the LayoutLeft view, i.e. the stride-
+    n0*n1 dimension innermost; the same three reduces with
+    Rank<3, Iterate::Left, Iterate::Left> (unit stride innermost) are timed
+    once beside it as `iterate_left_step_s`."""
     import oracle
     from kokkos_gb300 import datagen
     P = oracle.max_threads()
     x = datagen.normal_f32(NX, seed=0)
     keys = datagen.zipf_i32(NKEYS, NBINS, 1.1, seed=0)
+    box = ([0, 0, 0], [N0, N1, N2], [1, N0, N0 * N1])
     steps, t0 = 0, time.perf_counter()
     while True:
-        # The full box of a LayoutLeft view is one contiguous range with
-        # loc = flat index, so the range reduce is the MDRange reduce.
-        oracle.reduce("minloc", x, P)
-        oracle.reduce("maxloc", x, P)
-        oracle.reduce("sum", x, P)
+        oracle.mdrange_reduce("minloc", x, *box, P)
+        oracle.mdrange_reduce("maxloc", x, *box, P)
+        oracle.mdrange_reduce("sum", x, *box, P)
         oracle.histogram(keys, NBINS, P)
         steps += 1
         el = time.perf_counter() - t0
         if el >= budget_s:
             break
     gbs = steps * STEP_BYTES / el / 1e9
+    t1 = time.perf_counter()
+    for op in ("minloc", "maxloc", "sum"):
+        oracle.mdrange_reduce(op, x, *box, P, outer="left", inner="left")
+    oracle.histogram(keys, NBINS, P)
+    left_s = time.perf_counter() - t1
     return {"value": round(gbs, 3), "unit": "GB/s", "cores": P, "kind": "port",
-            "sample": f"{steps} full-size steps ({el:.1f} s) of the same workload, OpenMP threads={P}"}
+            "sample": (f"{steps} full-size steps ({el:.1f} s) of the same workload, OpenMP threads={P}; "
+                       "MDRangePolicy<Rank<3>> host defaults (Iterate::Right) over the LayoutLeft view"),
+            "iterate_left_step_s": round(left_s, 4),
+            "iterate_left_GBps": round(STEP_BYTES / left_s / 1e9, 3)}
 
 
 def other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind, reps=10):
@@ -397,7 +411,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     cb = cpu_baseline(budget_s=max(5.0, 2.0 * (args.steps + args.warmup)))
-    line = {"metric": "HBM GB/s (algorithmic bytes / step time)", "value": cb["value"], "unit": "GB/s",
+    line = {"metric": METRIC, "value": cb["value"], "unit": "GB/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(STEP_BYTES / (cb["value"] * 1e9) * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, seed 0)",
@@ -614,6 +628,33 @@ def main():
     red_ms = np.mean([per_op[n]["ms"] for n in ("mdrange_minloc_f32", "mdrange_maxloc_f32", "mdrange_sum_f32")])
     red_gbs = RED_BYTES / (red_ms / 1e3) / 1e9
 
+    # Each operation again with L2 emptied of its input first: a read of a
+    # 256 MiB buffer (clean lines, so no write-back is charged to the timed
+    # call) between calls; median of 10 calls per operation.  In the step,
+    # MaxLoc and Sum follow MinLoc over the same view, so part of their input
+    # can still be in L2; these numbers have none of that.
+    flush = torch.empty(1 << 26, dtype=torch.float32, device=dev).fill_(1.0)
+    FL = ctypes.c_void_p(flush.data_ptr())
+    fres = torch.zeros(64, dtype=torch.uint8, device=dev)
+    FR = ctypes.c_void_p(fres.data_ptr())
+    cold = {}
+    with torch.cuda.stream(stream):
+        for name, f, nbytes in ops:
+            ce = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+            for a_, b_ in ce:
+                gbk.check(lib.gbk_reduce(3, 4, FL, 1 << 26, FR, sp, None), "flush")  # Max: a plain read
+                a_.record(stream)
+                f()
+                b_.record(stream)
+            torch.cuda.synchronize()
+            gbk.stream_check(stream)
+            c_ms = float(np.median([a_.elapsed_time(b_) for a_, b_ in ce]))
+            gbs = nbytes / (c_ms / 1e3) / 1e9
+            cold[name] = {"ms": round(c_ms, 5), "GB/s": round(gbs, 1), "frac_of_" + peak_kind + "_hbm": round(gbs / hbm, 4)}
+    del flush
+    red_cold_ms = np.mean([cold[n]["ms"] for n in ("mdrange_minloc_f32", "mdrange_maxloc_f32", "mdrange_sum_f32")])
+    red_cold_gbs = RED_BYTES / (red_cold_ms / 1e3) / 1e9
+
     # The same three results from one pass: MinMaxLoc and Sum as two reducers
     # of one parallel_reduce over the box (reported beside the step, not in it).
     R3 = ctypes.c_void_p(dres.data_ptr() + 192)
@@ -680,18 +721,21 @@ def main():
     ok = bool(mn["val"] == hx_np.min() and int(hbins.numpy().sum()) == NKEYS)
 
     line = {
-        "metric": "HBM GB/s (algorithmic bytes / step time) of MDRange reduce + ScatterView histogram",
+        "metric": METRIC,
         "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded xoshiro256**, seed 0; N(0,1) floats, Zipf(1.1) keys)",
-        "config": {"workload": WORKLOAD, "step_bytes": STEP_BYTES, "l2": "inputs 268 MB each > 129 MB L2; no flush",
+        "config": {"workload": WORKLOAD, "step_bytes": STEP_BYTES, "l2": ("inputs 268 MB each > 129 MB L2, no flush in the step; MaxLoc and Sum re-read the view MinLoc "
+                          "just read, so part of it can still be in L2 (ops_cold_l2: each op after a 256 MiB read)"),
                    "parallelism": f"replicas x{world}",
                    "launch_config": "autotuner table" if tuned else "library defaults"},
         "roofline": {"bound": "hbm", "kernel": ROOF_KERNEL,
                      "achieved": round(red_gbs, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(red_gbs / hbm, 4), "peak_kind": peak_kind + " hbm_gbs (burst copy)",
-                     "traffic": ROOF_TRAFFIC},
+                     "traffic": ROOF_TRAFFIC,
+                     "achieved_cold_l2": round(red_cold_gbs, 1), "frac_cold_l2": round(red_cold_gbs / hbm, 4)},
         "ops": per_op,
+        "ops_cold_l2": cold,
         "e2e": {"value": round(e2e_val, 1), "unit": "GB/s", "ms_per_step": round(e_ms, 3),
                 "h2d_bytes_per_step": NX * 4 + NKEYS * 4, "d2h_bytes_per_step": 192 + NBINS * 8},
         "gpu_launches": int(launches),

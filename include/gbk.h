@@ -172,18 +172,25 @@ GBK_FOR_EACH_INT_DTYPE(GBK_DECLARE_TYPED_REDUCE, bor)
  * device-memory budget owned by someone else (a framework's caching
  * allocator, an application that forbids allocations after start-up) and
  * latency-critical loops that must not hit the device-wide synchronisation
- * cudaMalloc/cudaFree can cause.  Same reducers, dtypes, layouts and result
- * as gbk_reduce (its default launch shape: grid = SMs * ctas_per_sm CTAs of
- * 256 threads, ctas_per_sm 0 = 8), but the per-CTA partial values and the
- * ticket live in one fixed device array inside the library: 128 KiB + 256 B
- * per GPU that loads the library, held until the process exits, room for at
- * most 4096 CTAs.  A call that would need more CTAs returns
- * GBK_ERR_SCRATCH_LIMIT.  The caller still provides x and result (device
- * memory).  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress) and should come before any stream capture.
- * All calls on a device share the array: calls whose kernels may overlap on
- * the GPU (different streams not ordered by events) race and must not be
- * issued. */
+ * cudaMalloc/cudaFree can cause.  Reducers GBK_SUM .. GBK_MINMAXLOC over the
+ * six dtypes, with gbk_reduce's result layout; GBK_MINMAXLOC_SUM returns
+ * GBK_ERR_UNSUPPORTED.  It always runs the load-pipelined flat kernel with
+ * gbk_reduce's default launch shape (grid = SMs * ctas_per_sm CTAs of 256
+ * threads, ctas_per_sm 0 = 8), whereas gbk_reduce may pick another kernel
+ * for large inputs (the bulk-copy ring kernel, the split fixed-point double
+ * Sum): integer results, Min/Max and the *Loc results are identical, but
+ * float and double Sums can differ from gbk_reduce's in the last bits.
+ * The per-CTA partial values and the ticket live in one fixed device array
+ * inside the library: 128 KiB + 256 B per GPU that loads the library, held
+ * until the process exits, room for at most 4096 CTAs.  A call that would
+ * need more CTAs returns GBK_ERR_SCRATCH_LIMIT.  The caller still provides
+ * x and result (device memory).  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) and clears its ticket on the
+ * call's stream; that first call should come before any stream capture, and
+ * the address is kept until exit, so a process that resets the device
+ * (cudaDeviceReset) must not call this entry point afterwards.  All calls on
+ * a device share the array: calls whose kernels may overlap on the GPU
+ * (different streams not ordered by events) race and must not be issued. */
 int gbk_reduce_noalloc(gbk_reducer_t op, gbk_dtype_t dtype, const void* x, int64_t n, void* result,
                        gbk_stream_t stream, int32_t ctas_per_sm);
 

@@ -13,16 +13,20 @@
 // library holds it until the process exits.
 //
 // The array is shared by every call on a device and keeps the last call's
-// contents.  The ticket that must start at zero is cleared on the stream
-// before each launch (cudaMemsetAsync, not an allocation); the partials are
-// written before they are read.  Calls whose kernels overlap on the GPU (the
-// same device, different streams, not ordered by events) race on the array
-// and must not be issued.
+// contents.  The ticket must start at zero: the first call on a device
+// clears it (cudaMemsetAsync on that call's stream, not an allocation), and
+// every launch leaves it at zero again (the last CTA resets it when it
+// finishes the reduction).  The partials are written before they are read.
+// Calls whose kernels overlap on the GPU (the same device, different streams
+// not ordered by events) race on the array and must not be issued.
 //
 // Host code cannot use the array's name as a device address (in host code it
 // names a host-side stand-in).  The first call on each device, with that
 // device current, looks the address up with cudaGetSymbolAddress and keeps
-// it; that first call should come before any stream capture.
+// it; that first call should come before any stream capture.  The address is
+// kept for the life of the process: a caller that resets the device
+// (cudaDeviceReset) must not call this entry point afterwards, since the
+// module and its array are loaded again at a new address.
 #include <mutex>
 
 #include "gbk_reduce_impl.cuh"
@@ -40,7 +44,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 std::mutex g_na_mu;
 char* g_na_base[64] = {};
 
-int noalloc_base(char** out) {
+// Set-up, once per device with that device current: the array's device
+// address, and the ticket line cleared on the first caller's stream.
+int noalloc_base(char** out, cudaStream_t s) {
   int dev = 0;
   GBK_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return GBK_ERR_INVALID_ARGUMENT;
@@ -49,6 +55,7 @@ int noalloc_base(char** out) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) return e != cudaSuccess ? cuda_status(e) : GBK_ERR_CUDA;
+    GBK_CUDA_TRY(cudaMemsetAsync(p, 0, NOALLOC_HEADER, s));
     g_na_base[dev] = (char*)p;
   }
   *out = g_na_base[dev];
@@ -80,11 +87,10 @@ int noalloc_flat(const T* x, int64_t n, void* out, cudaStream_t s, int ctas_per_
   while (grid * BLOCK < head || grid * BLOCK < tail) ++grid;
   if (grid > NOALLOC_MAX_CTAS) return GBK_ERR_SCRATCH_LIMIT;
   char* base = nullptr;
-  const int st = noalloc_base(&base);
+  const int st = noalloc_base(&base, s);
   if (st) return st;
-  unsigned* ticket = (unsigned*)base;
+  unsigned* ticket = (unsigned*)base;  // zero here: cleared at set-up, reset by every launch's last CTA
   V* partials = (V*)(base + NOALLOC_HEADER);
-  GBK_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));
   k_reduce_flat<R, T, BLOCK, UNROLL><<<(unsigned)grid, BLOCK, 0, s>>>(x, n, head, 0, partials, ticket, (V*)out);
   note_launch();
   return cuda_status(cudaGetLastError());

@@ -436,7 +436,7 @@ def main():
     ap.add_argument("--train-workloads", type=int, default=1350)  # about 20,000 timings
     ap.add_argument("--eval-workloads", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=300)
-    ap.add_argument("--out", default="gpurun_out/tuner")
+    ap.add_argument("--out", default="tuner_out")
     ap.add_argument("--max-n", type=int, default=1 << 28)
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)

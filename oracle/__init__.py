@@ -39,6 +39,7 @@ def lib():
         L.orc_reduce.argtypes = [ci, ci, vp, i64, ci, vp]
         L.orc_sum_compensated.argtypes = [ci, vp, i64, vp]
         L.orc_mdrange_reduce.argtypes = [ci, ci, vp, ci, vp, vp, vp, ci, vp]
+        L.orc_mdrange_reduce_ex.argtypes = [ci, ci, vp, ci, vp, vp, vp, vp, ci, ci, ci, vp]
         L.orc_scan.argtypes = [ci, ci, ci, vp, i64, vp, vp, ci]
         L.orc_histogram_i32_i64.argtypes = [vp, i64, vp, i64, ci, vp]
         L.orc_sort_u64.argtypes = [vp, i64]
@@ -92,14 +93,18 @@ def sum_compensated(x):
     return float(out[0]), float(out[1]), float(out[2])
 
 
-def mdrange_reduce(op, base, lower, upper, strides, nthreads):
-    """base: flat numpy array; lower/upper/strides in elements; loc = element offset."""
+def mdrange_reduce(op, base, lower, upper, strides, nthreads, tile=None, outer="right", inner="right"):
+    """base: flat numpy array; lower/upper/strides in elements; loc = element offset.
+    The reference's host tile walk: MDRangePolicy<Rank<N, outer, inner>>(lower, upper, tile),
+    default tiles where tile is None or an entry is <= 0."""
     rank = len(lower)
     lo = np.asarray(lower, dtype=np.int64)
     up = np.asarray(upper, dtype=np.int64)
     st = np.asarray(strides, dtype=np.int64)
+    tl = np.asarray(tile if tile is not None else [0] * rank, dtype=np.int64)
     out = np.zeros(1, dtype=result_dtype(op, base.dtype))
-    rc = lib().orc_mdrange_reduce(OPS[op], DT[base.dtype], _p(base), rank, _p(lo), _p(up), _p(st), nthreads, _p(out))
+    rc = lib().orc_mdrange_reduce_ex(OPS[op], DT[base.dtype], _p(base), rank, _p(lo), _p(up), _p(st), _p(tl),
+                                     int(outer == "left"), int(inner == "left"), nthreads, _p(out))
     if rc:
         raise ValueError("oracle mdrange_reduce failed")
     return out[0]

@@ -298,50 +298,151 @@ int orc_sum_compensated(int dtype, const void* x, int64_t n, double* out3) {
   return 0;
 }
 
+}  // extern "C"
+
 // MDRange reduce over an iteration box [lower, upper) of a strided view
 // (strides in elements).  Element "loc" is the element's offset from base:
-// sum_d i_d * stride_d.  The extremum result (value and loc) is independent
-// of iteration order whenever the extremum is unique; Sum/Prod over floating
-// point are compared against the compensated sum instead.  Restates the
-// per-element semantics of OpenMP ParallelReduce<MDRangePolicy>
-// (core/src/OpenMP/Kokkos_OpenMP_Parallel_Reduce.hpp:187-326) with a
-// Right-major (last index fastest) walk per thread over slabs of dim 0.
+// sum_d i_d * stride_d.  Restates OpenMP ParallelReduce<MDRangePolicy>
+// (core/src/OpenMP/Kokkos_OpenMP_Parallel_Reduce.hpp:187-326) with the
+// host tile rules of MDRangePolicy::init_helper
+// (core/src/KokkosExp_MDRangePolicy.hpp:388-425; host TileSizeProperties
+// :145-152: default tile 2, the innermost dimension's tile = its whole
+// length), the tile partition set_work_partition(num_tiles, 1) over the
+// thread pool, and HostIterateTile's walk
+// (core/src/impl/KokkosExp_Host_IterateTile.hpp:2040-2110: tile offsets in
+// outer-direction order, partial tiles by check_iteration_bounds, elements in
+// inner-direction order), then the thread-order join.  So the result equals
+// the reference's bit for bit, floating-point Sums included.
+// iter_outer / iter_inner: 0 = Right (last index fastest, the host default),
+// 1 = Left.  tile: rank entries, <= 0 = the default for that dimension.
+template <class R, class T>
+static typename R::V mdrange_tiles(const T* base, int rank, const int64_t* lower, const int64_t* upper,
+                                   const int64_t* strides, const int64_t* tile_in, int outer_left,
+                                   int inner_left, int P) {
+  using V = typename R::V;
+  int64_t tile[6], tend[6], num_tiles = 1, prod = 1;
+  const int64_t int_max = std::numeric_limits<int>::max();
+  const int first = inner_left ? 0 : rank - 1, last = inner_left ? rank : -1, inc = inner_left ? 1 : -1;
+  for (int i = first; i != last; i += inc) {
+    const int64_t len = upper[i] - lower[i];
+    tile[i] = tile_in ? tile_in[i] : 0;
+    if (tile[i] <= 0) {
+      const bool innermost = inner_left ? (i == 0) : (i == rank - 1);
+      if (!innermost) tile[i] = (prod * 2 < int_max) ? 2 : 1;
+      else tile[i] = std::max<int64_t>(len, 1);
+    }
+    tend[i] = (len + tile[i] - 1) / tile[i];
+    num_tiles *= tend[i];
+    prod *= tile[i];
+  }
+  if (P < 1) P = 1;
+  std::vector<V> part(P, R::init());
+  auto run_tiles = [&](int64_t tb, int64_t te, V& v) {
+    int64_t off[6], dims[6];
+    for (int64_t t = tb; t < te; ++t) {
+      int64_t ti = t;
+      if (outer_left) {
+        for (int i = 0; i < rank; ++i) { off[i] = (ti % tend[i]) * tile[i] + lower[i]; ti /= tend[i]; }
+      } else {
+        for (int i = rank - 1; i >= 0; --i) { off[i] = (ti % tend[i]) * tile[i] + lower[i]; ti /= tend[i]; }
+      }
+      for (int i = 0; i < rank; ++i) {
+        if (off[i] + tile[i] <= upper[i]) dims[i] = tile[i];
+        else dims[i] = (upper[i] - 1 - off[i]) == 0 ? 1
+                       : (upper[i] - tile[i]) > 0 ? (upper[i] - off[i]) : (upper[i] - lower[i]);
+      }
+      // Elements of the tile: the innermost loop runs over dimension
+      // rank-1 (Right) or 0 (Left); the counter idx walks the others as an
+      // odometer in the same nesting order.
+      const int in_d = inner_left ? 0 : rank - 1;
+      int64_t idx[6] = {0, 0, 0, 0, 0, 0};
+      int64_t outer_cnt = 1;
+      for (int i = 0; i < rank; ++i) if (i != in_d) outer_cnt *= dims[i];
+      for (int64_t c = 0; c < outer_cnt; ++c) {
+        int64_t o = 0;
+        for (int i = 0; i < rank; ++i) if (i != in_d) o += (off[i] + idx[i]) * strides[i];
+        const int64_t s = strides[in_d];
+        int64_t e = o + off[in_d] * s;
+        for (int64_t k = 0; k < dims[in_d]; ++k, e += s) R::update(v, base[e], e);
+        // advance the odometer: innermost of the remaining dimensions first
+        if (inner_left) {
+          for (int i = 1; i < rank; ++i) { if (++idx[i] < dims[i]) break; idx[i] = 0; }
+        } else {
+          for (int i = rank - 2; i >= 0; --i) { if (++idx[i] < dims[i]) break; idx[i] = 0; }
+        }
+      }
+    }
+  };
+#pragma omp parallel num_threads(P)
+  {
+    const int r = omp_get_thread_num();
+    const int np = omp_get_num_threads();
+    for (int q = r; q < P; q += np) {
+      auto rg = work_partition(num_tiles, 1, q, P);
+      V v = R::init();
+      run_tiles(rg.first, rg.second, v);
+      part[q] = v;
+    }
+  }
+  V acc = part[0];
+  for (int i = 1; i < P; ++i) R::join(acc, part[i]);
+  return acc;
+}
+
+template <class T>
+static int mdrange_dispatch_T(int op, const T* b, int rank, const int64_t* lo, const int64_t* up,
+                              const int64_t* st, const int64_t* tile, int ol, int il, int P, void* out) {
+  switch (op) {
+    case 0: *(T*)out = mdrange_tiles<RSum<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0;
+    case 1: *(T*)out = mdrange_tiles<RProd<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0;
+    case 2: *(T*)out = mdrange_tiles<RMin<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0;
+    case 3: *(T*)out = mdrange_tiles<RMax<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0;
+    case 4:
+      if constexpr (std::is_integral_v<T>) { *(T*)out = mdrange_tiles<RLAnd<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0; }
+      return 1;
+    case 5:
+      if constexpr (std::is_integral_v<T>) { *(T*)out = mdrange_tiles<RLOr<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0; }
+      return 1;
+    case 6:
+      if constexpr (std::is_integral_v<T>) { *(T*)out = mdrange_tiles<RBAnd<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0; }
+      return 1;
+    case 7:
+      if constexpr (std::is_integral_v<T>) { *(T*)out = mdrange_tiles<RBOr<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0; }
+      return 1;
+    case 8: *(ValLoc<T>*)out = mdrange_tiles<RMinLoc<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0;
+    case 9: *(ValLoc<T>*)out = mdrange_tiles<RMaxLoc<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0;
+    case 10: *(MinMaxV<T>*)out = mdrange_tiles<RMinMax<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0;
+    case 11: *(MinMaxLocV<T>*)out = mdrange_tiles<RMinMaxLoc<T>>(b, rank, lo, up, st, tile, ol, il, P); return 0;
+  }
+  return 1;
+}
+
+extern "C" {
+
+// The tile walk above with explicit tiles and iteration directions
+// (MDRangePolicy<Rank<N, outer, inner>>(lower, upper, tile)).
+int orc_mdrange_reduce_ex(int op, int dtype, const void* base, int rank, const int64_t* lower,
+                          const int64_t* upper, const int64_t* strides, const int64_t* tile, int outer_left,
+                          int inner_left, int nthreads, void* out) {
+  if (rank < 1 || rank > 6) return 1;
+  for (int d = 0; d < rank; ++d)
+    if (upper[d] < lower[d]) return 1;  // the reference aborts (KokkosExp_MDRangePolicy.hpp:399-411)
+  switch (dtype) {
+    case 0: return mdrange_dispatch_T<int32_t>(op, (const int32_t*)base, rank, lower, upper, strides, tile, outer_left, inner_left, nthreads, out);
+    case 1: return mdrange_dispatch_T<int64_t>(op, (const int64_t*)base, rank, lower, upper, strides, tile, outer_left, inner_left, nthreads, out);
+    case 2: return mdrange_dispatch_T<uint32_t>(op, (const uint32_t*)base, rank, lower, upper, strides, tile, outer_left, inner_left, nthreads, out);
+    case 3: return mdrange_dispatch_T<uint64_t>(op, (const uint64_t*)base, rank, lower, upper, strides, tile, outer_left, inner_left, nthreads, out);
+    case 4: return mdrange_dispatch_T<float>(op, (const float*)base, rank, lower, upper, strides, tile, outer_left, inner_left, nthreads, out);
+    case 5: return mdrange_dispatch_T<double>(op, (const double*)base, rank, lower, upper, strides, tile, outer_left, inner_left, nthreads, out);
+  }
+  return 1;
+}
+
+// MDRangePolicy<Rank<N>>(lower, upper) on the host defaults: Iterate::Right
+// outer and inner (KokkosExp_MDRangePolicy.hpp:48-58), default tiles.
 int orc_mdrange_reduce(int op, int dtype, const void* base, int rank, const int64_t* lower,
                        const int64_t* upper, const int64_t* strides, int nthreads, void* out) {
-  if (rank < 1 || rank > 6) return 1;
-  // Gather the box into a flat array in Left order (dim 0 fastest) with its
-  // locs, then reduce it with the range algorithm.  Value and loc of a
-  // unique extremum do not depend on this order.
-  int64_t ext[6], cnt = 1;
-  for (int d = 0; d < rank; ++d) {
-    ext[d] = upper[d] > lower[d] ? upper[d] - lower[d] : 0;
-    cnt *= ext[d];
-  }
-  const size_t esz = (dtype == 0 || dtype == 2 || dtype == 4) ? 4 : 8;
-  std::vector<unsigned char> buf((size_t)cnt * esz);
-  std::vector<int64_t> locs((size_t)cnt);
-  for (int64_t f = 0; f < cnt; ++f) {
-    int64_t rem = f, off = 0;
-    for (int d = 0; d < rank; ++d) {
-      const int64_t i = lower[d] + rem % ext[d];
-      rem /= ext[d];
-      off += i * strides[d];
-    }
-    std::memcpy(&buf[(size_t)f * esz], (const unsigned char*)base + off * (int64_t)esz, esz);
-    locs[f] = off;
-  }
-  int rc = orc_reduce(op, dtype, buf.data(), cnt, nthreads, out);
-  if (rc) return rc;
-  // Map flat positions back to element offsets for the *Loc reducers.
-  auto fix = [&](int64_t* loc) { if (*loc != LOC_IDENT) *loc = locs[*loc]; };
-  unsigned char* o = (unsigned char*)out;
-  if (op == 8 || op == 9) fix((int64_t*)(o + esz * (esz == 4 ? 2 : 1)));
-  if (op == 11) {
-    const size_t lo = (2 * esz + 7) / 8 * 8;
-    fix((int64_t*)(o + lo));
-    fix((int64_t*)(o + lo + 8));
-  }
-  return 0;
+  return orc_mdrange_reduce_ex(op, dtype, base, rank, lower, upper, strides, nullptr, 0, 0, nthreads, out);
 }
 
 // OpenMP ParallelScan: core/src/OpenMP/Kokkos_OpenMP_Parallel_Scan.hpp:69-140

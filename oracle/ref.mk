@@ -8,7 +8,7 @@
 # The config headers CMake would generate are replaced by the hand-written
 # feature-macro headers in oracle/refcfg/.
 
-REF    ?= /root/reference
+REF    ?= $(abspath $(dir $(lastword $(MAKEFILE_LIST)))/../../reference)
 OUT    ?= oracle/_ref
 CXX    ?= g++
 CXXFLAGS ?= -O3 -std=c++17 -fopenmp -fPIC

@@ -83,7 +83,7 @@ def reduce_input(op, dt, n, seed):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("KOKKOS_REF_SRC", os.path.join(ROOT, os.pardir, "reference")))
     args = ap.parse_args()
     if not os.path.isdir(args.ref):
         sys.exit(f"reference sources not found at {args.ref}")
