@@ -1,0 +1,152 @@
+// The GB300 space's hooks in Kokkos' containers and algorithms, declared
+// ahead of the headers that use them (Kokkos_Core.hpp includes this through
+// the backend declarations, before Kokkos_ScatterView.hpp and Kokkos_Sort.hpp
+// are read):
+//
+//   * ScatterView defaults (containers/src/Kokkos_ScatterView.hpp:59-198):
+//     NonDuplicated + Atomic, as for the CUDA space; and the atomic Sum
+//     contribution on this space is warp-aggregated: the lanes of a warp that
+//     add to the same element combine their values first and one lane issues
+//     the atomic (hot keys of a skewed histogram serialise 32x less);
+//   * sort_device_view_without_comparator / sort_by_key_device_view_without_
+//     comparator overloads (algorithms/src/sorting/impl/Kokkos_SortImpl.hpp:
+//     347-396, impl/Kokkos_SortByKeyImpl.hpp:356-409): Kokkos::sort and
+//     Experimental::sort_by_key on a contiguous GB300 View of 4- or 8-byte
+//     keys run the library's stable radix sort (gbk_sort / gbk_sort_by_key)
+//     where the CUDA space calls thrust.
+#ifndef KOKKOS_GB300_HOOKS_HPP_
+#define KOKKOS_GB300_HOOKS_HPP_
+
+#include <Kokkos_Macros.hpp>
+#if defined(KOKKOS_ENABLE_GB300)
+
+#include <algorithm>
+#include <cstdint>
+#include <type_traits>
+#include <vector>
+
+#include <Kokkos_Atomic.hpp>
+
+#include <GB300/Kokkos_GB300.hpp>
+
+// ---- ScatterView ----------------------------------------------------------------
+namespace Kokkos {
+namespace Experimental {
+struct ScatterSum;
+struct ScatterNonDuplicated;
+struct ScatterDuplicated;
+struct ScatterAtomic;
+}  // namespace Experimental
+namespace Impl {
+namespace Experimental {
+template <typename ExecSpace>
+struct DefaultDuplication;
+template <typename ExecSpace, typename Duplication>
+struct DefaultContribution;
+template <typename ValueType, typename Op, typename DeviceType, typename Contribution>
+struct ScatterValue;
+
+template <>
+struct DefaultDuplication<Kokkos::Experimental::GB300> {
+  using type = Kokkos::Experimental::ScatterNonDuplicated;
+};
+template <>
+struct DefaultContribution<Kokkos::Experimental::GB300, Kokkos::Experimental::ScatterNonDuplicated> {
+  using type = Kokkos::Experimental::ScatterAtomic;
+};
+template <>
+struct DefaultContribution<Kokkos::Experimental::GB300, Kokkos::Experimental::ScatterDuplicated> {
+  using type = Kokkos::Experimental::ScatterAtomic;
+};
+
+// Warp-aggregated atomic add: lanes adding to the same address sum their
+// values over shuffles (every lane of a group walks the group's lanes in the
+// same order) and the group's lowest lane adds the sum.
+template <class T>
+__device__ __forceinline__ void gb300_aggregated_add(T* dest, T v) {
+  if constexpr (std::is_arithmetic_v<T> && (sizeof(T) == 4 || sizeof(T) == 8)) {
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, (unsigned long long)(uintptr_t)dest);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    T sum = T(0);
+    for (unsigned m = peers; m; m &= m - 1) sum += __shfl_sync(peers, v, __ffs(m) - 1);
+    if (lane == leader) Kokkos::atomic_add(dest, sum);
+  } else {
+    Kokkos::atomic_add(dest, v);
+  }
+}
+
+template <typename ValueType>
+struct ScatterValue<ValueType, Kokkos::Experimental::ScatterSum,
+                    Kokkos::Device<Kokkos::Experimental::GB300, Kokkos::Experimental::GB300Space>,
+                    Kokkos::Experimental::ScatterAtomic> {
+  ValueType& value;
+
+ public:
+  KOKKOS_FORCEINLINE_FUNCTION ScatterValue(ValueType& value_in) : value(value_in) {}
+  KOKKOS_FORCEINLINE_FUNCTION void operator+=(ValueType const& rhs) { this->join(value, rhs); }
+  KOKKOS_FORCEINLINE_FUNCTION void operator++() { this->join(value, ValueType(1)); }
+  KOKKOS_FORCEINLINE_FUNCTION void operator++(int) { this->join(value, ValueType(1)); }
+  KOKKOS_FORCEINLINE_FUNCTION void operator-=(ValueType const& rhs) { this->join(value, ValueType(-rhs)); }
+  KOKKOS_FORCEINLINE_FUNCTION void operator--() { this->join(value, ValueType(-1)); }
+  KOKKOS_FORCEINLINE_FUNCTION void operator--(int) { this->join(value, ValueType(-1)); }
+  KOKKOS_INLINE_FUNCTION void join(ValueType& dest, const ValueType& src) const {
+    KOKKOS_IF_ON_DEVICE((gb300_aggregated_add(&dest, src);))
+    KOKKOS_IF_ON_HOST((Kokkos::atomic_add(&dest, src);))
+  }
+  KOKKOS_FORCEINLINE_FUNCTION void update(ValueType const& rhs) { this->join(value, rhs); }
+  KOKKOS_FORCEINLINE_FUNCTION void reset() { value = ValueType(); }
+};
+
+}  // namespace Experimental
+
+// ---- sort ----------------------------------------------------------------------------
+template <class T>
+constexpr int gb300_sort_dtype() {
+  if constexpr (std::is_same_v<T, int32_t>) return GBK_I32;
+  else if constexpr (std::is_same_v<T, int64_t>) return GBK_I64;
+  else if constexpr (std::is_same_v<T, uint32_t>) return GBK_U32;
+  else if constexpr (std::is_same_v<T, uint64_t>) return GBK_U64;
+  else if constexpr (std::is_same_v<T, float>) return GBK_F32;
+  else if constexpr (std::is_same_v<T, double>) return GBK_F64;
+  else if constexpr (std::is_integral_v<T> && sizeof(T) == 8)
+    return std::is_signed_v<T> ? GBK_I64 : GBK_U64;  // long long / unsigned long long
+  else return -1;
+}
+
+template <class DataType, class... Properties>
+void sort_device_view_without_comparator(const Kokkos::Experimental::GB300& exec,
+                                         const Kokkos::View<DataType, Properties...>& view) {
+  using ViewType = Kokkos::View<DataType, Properties...>;
+  using T = typename ViewType::non_const_value_type;
+  static_assert(ViewType::rank == 1, "Kokkos::sort: currently only supports rank-1 Views.");
+  constexpr int dt = gb300_sort_dtype<T>();
+  static_assert(dt >= 0, "Kokkos::sort on GB300: keys must be 4- or 8-byte integers or floating point");
+  if (view.extent(0) <= 1) return;
+  if (!view.span_is_contiguous()) Kokkos::abort("Kokkos::sort on GB300: the View must be contiguous");
+  gb300_check(gbk_sort((gbk_dtype_t)dt, (void*)view.data(), (int64_t)view.extent(0), (gbk_stream_t)exec.stream()),
+              "sort");
+}
+
+template <class KeysDataType, class... KeysProperties, class ValuesDataType, class... ValuesProperties>
+void sort_by_key_device_view_without_comparator(const Kokkos::Experimental::GB300& exec,
+                                                const Kokkos::View<KeysDataType, KeysProperties...>& keys,
+                                                const Kokkos::View<ValuesDataType, ValuesProperties...>& values) {
+  using K = typename Kokkos::View<KeysDataType, KeysProperties...>::non_const_value_type;
+  using V = typename Kokkos::View<ValuesDataType, ValuesProperties...>::non_const_value_type;
+  constexpr int dt = gb300_sort_dtype<K>();
+  static_assert(dt >= 0, "Kokkos::sort_by_key on GB300: keys must be 4- or 8-byte integers or floating point");
+  static_assert(sizeof(V) == 4 || sizeof(V) == 8, "Kokkos::sort_by_key on GB300: values of 4 or 8 bytes");
+  if (!keys.span_is_contiguous() || !values.span_is_contiguous())
+    Kokkos::abort("Kokkos::sort_by_key on GB300: the Views must be contiguous");
+  gb300_check(gbk_sort_by_key((gbk_dtype_t)dt, (void*)keys.data(), (int)sizeof(V), (void*)values.data(),
+                              (int64_t)keys.extent(0), (gbk_stream_t)exec.stream()),
+              "sort_by_key");
+}
+
+}  // namespace Impl
+}  // namespace Kokkos
+
+#endif  // KOKKOS_ENABLE_GB300
+#endif  // KOKKOS_GB300_HOOKS_HPP_

@@ -52,6 +52,7 @@ extern "C" {
 #define GBK_ERR_KEY_OUT_OF_RANGE 6
 #define GBK_ERR_NO_DEVICE 7
 #define GBK_ERR_SCRATCH_LIMIT 8 /* request exceeds the fixed scratch of gbk_reduce_noalloc */
+#define GBK_ERR_DEVICE_ABORT 9  /* a kernel of the header paths called Kokkos::abort in device code */
 
 typedef enum { GBK_I32 = 0, GBK_I64 = 1, GBK_U32 = 2, GBK_U64 = 3, GBK_F32 = 4, GBK_F64 = 5 } gbk_dtype_t;
 
@@ -110,6 +111,8 @@ int gbk_note_launches(int64_t count);
 /* Bound, in polls, of every device-side wait (lookback, barriers).  The
  * default bounds a wait at roughly a second. */
 int gbk_set_wait_limit(int64_t polls);
+/* The current bound (for kernels instantiated outside the library). */
+int64_t gbk_wait_limit(void);
 /* Number of this library's kernels launched so far (all streams). */
 int64_t gbk_launch_count(void);
 /* deep_copy between any two buffers the runtime can address (host<->device

@@ -22,6 +22,7 @@
 #define GBK_EBIT_TIMEOUT 1
 #define GBK_EBIT_KEY_RANGE 2
 #define GBK_EBIT_BAD_STATE 4
+#define GBK_EBIT_ABORT 8  /* a kernel instantiated outside the library ran a device-side abort */
 
 namespace gbk {
 

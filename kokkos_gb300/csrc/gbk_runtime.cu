@@ -172,6 +172,7 @@ const char* gbk_status_string(int s) {
     case GBK_ERR_OUT_OF_WORKSPACE: return "workspace too small (reserve it before stream capture)";
     case GBK_ERR_KEY_OUT_OF_RANGE: return "key outside the bin range (skipped)";
     case GBK_ERR_NO_DEVICE: return "no CUDA device";
+    case GBK_ERR_DEVICE_ABORT: return "a kernel called abort in device code";
     case GBK_ERR_SCRATCH_LIMIT: return "request needs more CTAs than the fixed scratch of gbk_reduce_noalloc holds (4096)";
   }
   return "unknown status";
@@ -208,6 +209,7 @@ int gbk_stream_check(gbk_stream_t stream) {
   if (bits & GBK_EBIT_TIMEOUT) return GBK_ERR_DEVICE_TIMEOUT;
   if (bits & GBK_EBIT_BAD_STATE) return GBK_ERR_CUDA;
   if (bits & GBK_EBIT_KEY_RANGE) return GBK_ERR_KEY_OUT_OF_RANGE;
+  if (bits & GBK_EBIT_ABORT) return GBK_ERR_DEVICE_ABORT;
   return GBK_OK;
 }
 
@@ -270,6 +272,8 @@ int gbk_set_wait_limit(int64_t polls) {
   g_wait_limit = polls;
   return GBK_OK;
 }
+
+int64_t gbk_wait_limit(void) { return g_wait_limit.load(); }
 
 int64_t gbk_launch_count(void) { return g_launches.load(); }
 
