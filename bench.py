@@ -337,6 +337,12 @@ def other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind, reps=10):
     del graph, xg, gb
 
     # ---- c4 -----------------------------------------------------------------
+    thr = None
+    thr_path = os.path.join(ROOT, "kokkos_gb300", "comparators", "libgbk_thrust.so")
+    if os.path.exists(thr_path):
+        thr = ctypes.CDLL(thr_path)
+        thr.gbk_cmp_thrust_sort_by_key_u64_i32.argtypes = [P, P, ctypes.c_int64, P]
+        thr.gbk_cmp_thrust_sort_u64.argtypes = [P, ctypes.c_int64, P]
     n = 1 << 27
     iota = torch.arange(n, dtype=torch.int32, device=dev)
     dk, dv = torch.empty(n, dtype=torch.int64, device=dev), torch.empty_like(iota)
@@ -355,6 +361,12 @@ def other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind, reps=10):
         out["c4_sort_by_key_u64_i32_2^27_" + name] = dict(
             rate(pass_bytes, ms), digit_passes=passes, Gpairs_per_s=round(n / (ms / 1e3) / 1e9, 3),
             min_bytes_GBps=round(n * 24 / (ms / 1e3) / 1e9, 1))
+        if thr is not None:
+            # the reference's CUDA path: thrust::sort_by_key on the same keys and stream
+            ms_t = timed([lambda: thr.gbk_cmp_thrust_sort_by_key_u64_i32(P(dk.data_ptr()), P(dv.data_ptr()), n, sp)],
+                         3, prep=refill)
+            out["c4_sort_by_key_u64_i32_2^27_" + name].update(
+                thrust_sort_by_key_ms=round(ms_t, 4), speedup_vs_thrust=round(ms_t / ms, 3))
         del k0
     # Kokkos::sort of the uniform keys alone, and BinSort with BinOp1D(n / 2 bins, min, max) (the bins the
     # reference's host sort path uses): the bin permutation (stable within a bin), then applying it to the keys
@@ -368,6 +380,9 @@ def other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind, reps=10):
     passes = 8
     out["c4_sort_u64_2^27_uniform"] = dict(rate(n * 8 + (passes - 1) * n * 8 + passes * n * 16, ms),
                                            Gkeys_per_s=round(n / (ms / 1e3) / 1e9, 3))
+    if thr is not None:
+        ms_t = timed([lambda: thr.gbk_cmp_thrust_sort_u64(P(dk.data_ptr()), n, sp)], 3, prep=refill_keys)
+        out["c4_sort_u64_2^27_uniform"].update(thrust_sort_ms=round(ms_t, 4), speedup_vs_thrust=round(ms_t / ms, 3))
     kmin, kmax = float(kh.min()), float(kh.max())
     nb_req = n // 2
     mul = float(nb_req) / (kmax - kmin)

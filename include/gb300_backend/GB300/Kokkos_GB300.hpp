@@ -48,6 +48,7 @@
 #include <impl/Kokkos_Profiling_Interface.hpp>
 #include <impl/Kokkos_SharedAlloc.hpp>
 #include <impl/Kokkos_Tools.hpp>
+#include <impl/Kokkos_ZeroMemset_fwd.hpp>
 
 #include <gbk.h>
 
@@ -237,8 +238,69 @@ struct DeepCopy<HostSpace, Kokkos::Experimental::GB300Space, ExecutionSpace,
   }
 };
 
-// ---- MDRange defaults: index 0 fastest on the device (as for the CUDA space,
-// core/src/Cuda/Kokkos_Cuda_MDRangePolicy.hpp:24-49) --------------------------
+// ---- View access checks --------------------------------------------------
+// Kokkos checks a View access in device code against DefaultExecutionSpace
+// and in host code against DefaultHostExecutionSpace
+// (core/src/Kokkos_Core_fwd.hpp:230-256, View/Kokkos_ViewAccessPreconditionsCheck.hpp:
+// 70-77, View/Kokkos_ViewMapping.hpp:3480-3490).  Kokkos' list of default
+// spaces (Kokkos_Core_fwd.hpp:96-121) has no entry for a space added beside
+// the built-in ones, so in this build both are Serial, and the stock checks
+// would reject every device access to GB300 memory.  These specialisations
+// state the real rule: GB300Space is accessible from device code and not
+// from host code; HostSpace is accessible from host code and not from
+// device code.
+template <class MemorySpace, class AccessSpace, bool>
+struct RuntimeCheckBasicViewMemoryAccessViolation;
+template <class MemorySpace, class AccessSpace, bool>
+struct RuntimeCheckViewMemoryAccessViolation;
+
+template <>
+struct RuntimeCheckMemoryAccessViolation<Kokkos::Experimental::GB300Space, Kokkos::DefaultExecutionSpace, false> {
+  KOKKOS_FUNCTION RuntimeCheckMemoryAccessViolation(char const* const msg) {
+    (void)msg;
+    KOKKOS_IF_ON_HOST((Kokkos::abort(msg);))
+  }
+};
+template <>
+struct RuntimeCheckMemoryAccessViolation<Kokkos::HostSpace, Kokkos::DefaultExecutionSpace, true> {
+  KOKKOS_FUNCTION RuntimeCheckMemoryAccessViolation(char const* const msg) {
+    (void)msg;
+    KOKKOS_IF_ON_DEVICE((Kokkos::abort(msg);))
+  }
+};
+template <>
+struct RuntimeCheckBasicViewMemoryAccessViolation<Kokkos::Experimental::GB300Space, Kokkos::DefaultExecutionSpace,
+                                                  false> {
+  KOKKOS_FUNCTION RuntimeCheckBasicViewMemoryAccessViolation(SharedAllocationTracker const&) {
+    KOKKOS_IF_ON_HOST(
+        (Kokkos::abort("Kokkos::View ERROR: attempt to access inaccessible memory space (GB300Space from host code)");))
+  }
+};
+template <>
+struct RuntimeCheckBasicViewMemoryAccessViolation<Kokkos::HostSpace, Kokkos::DefaultExecutionSpace, true> {
+  KOKKOS_FUNCTION RuntimeCheckBasicViewMemoryAccessViolation(SharedAllocationTracker const&) {
+    KOKKOS_IF_ON_DEVICE(
+        (Kokkos::abort("Kokkos::View ERROR: attempt to access inaccessible memory space (HostSpace from device code)");))
+  }
+};
+template <>
+struct RuntimeCheckViewMemoryAccessViolation<Kokkos::Experimental::GB300Space, Kokkos::DefaultExecutionSpace, false> {
+  template <class Track, class Map>
+  KOKKOS_FUNCTION RuntimeCheckViewMemoryAccessViolation(char const* const msg, Track const&, Map const&) {
+    (void)msg;
+    KOKKOS_IF_ON_HOST((Kokkos::abort(msg);))
+  }
+};
+template <>
+struct RuntimeCheckViewMemoryAccessViolation<Kokkos::HostSpace, Kokkos::DefaultExecutionSpace, true> {
+  template <class Track, class Map>
+  KOKKOS_FUNCTION RuntimeCheckViewMemoryAccessViolation(char const* const msg, Track const&, Map const&) {
+    (void)msg;
+    KOKKOS_IF_ON_DEVICE((Kokkos::abort(msg);))
+  }
+};
+
+// ---- deep_copy(view, 0) on the space's stream --------------------------------
 template <>
 struct ZeroMemset<Kokkos::Experimental::GB300> {
   ZeroMemset(const Kokkos::Experimental::GB300& exec, void* dst, size_t cnt) {

@@ -60,16 +60,18 @@ constexpr int kSlotScan = 41;
 // that a kernel sets when code it ran asked for an abort.
 constexpr int kErrBitAbort = 8;
 
-// Device-side abort request (Kokkos::abort called in device code): the
-// message is printed and a flag of this translation unit is set, which every
-// skeleton kernel of the unit folds into its stream's error word when it
-// finishes, so the next fence raises it.  The calling thread continues (no
-// trap: the context stays usable); the flag stays set for the rest of the
-// process, as a device-side assertion would leave a CUDA context unusable.
+// Device-side abort request (Kokkos::abort called in device code): the first
+// request of this translation unit prints its message, a flag of the unit is
+// set, which every skeleton kernel of the unit folds into its stream's error
+// word when it finishes (so the next fence raises it), and the calling thread
+// ends (PTX exit: no trap, the context stays usable).  The flag stays set for
+// the rest of the process, as a device-side assertion would leave a CUDA
+// context unusable.  Correct programs never reach this path.
 static __device__ int g_abort_requested = 0;
 __device__ inline void request_abort(const char* msg) {
-  printf("Kokkos::abort on the GB300 device: %s\n", msg);
-  atomicExch(&g_abort_requested, 1);
+  if (atomicExch(&g_abort_requested, 1) == 0) printf("Kokkos::abort on the GB300 device: %s\n", msg);
+  __threadfence();
+  asm volatile("exit;");
 }
 __device__ __forceinline__ void report_abort(int* err) {
   if (threadIdx.x == 0 && err && *(volatile int*)&g_abort_requested) atomicOr(err, kErrBitAbort);

@@ -24,6 +24,9 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
 
 LIB = os.path.join(HERE, "libgbk.so")
 HOSTLIB = os.path.join(HERE, "libgbk_host.so")
+# thrust comparator for the sort benchmarks (not part of libgbk.so)
+CMP_SRC = os.path.join(HERE, "comparators", "thrust_sort.cu")
+CMP_LIB = os.path.join(HERE, "comparators", "libgbk_thrust.so")
 
 
 def nvcc():
@@ -61,9 +64,12 @@ def build(verbose=False, jobs=None):
         objs.append(o)
         if _stale(o, [u] + hdrs):
             todo.append((u, o))
-    jobs = jobs or max(1, min(len(todo), os.cpu_count() or 4))
+    jobs = jobs or max(1, min(len(todo) + 1, os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         futs = [ex.submit(_run, [nvcc()] + ARCH + NVFLAGS + ["-c", u, "-o", o]) for u, o in todo]
+        if _stale(CMP_LIB, [CMP_SRC]):
+            futs.append(ex.submit(_run, [nvcc()] + ARCH + ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+                                                           CMP_SRC, "-o", CMP_LIB]))
         for f in futs:
             out = f.result()
             if verbose and out.strip():
