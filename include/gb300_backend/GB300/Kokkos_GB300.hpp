@@ -254,8 +254,17 @@ struct RuntimeCheckBasicViewMemoryAccessViolation;
 template <class MemorySpace, class AccessSpace, bool>
 struct RuntimeCheckViewMemoryAccessViolation;
 
+// (the same for the space's team scratch, ScratchMemorySpace<GB300>)
 template <>
 struct RuntimeCheckMemoryAccessViolation<Kokkos::Experimental::GB300Space, Kokkos::DefaultExecutionSpace, false> {
+  KOKKOS_FUNCTION RuntimeCheckMemoryAccessViolation(char const* const msg) {
+    (void)msg;
+    KOKKOS_IF_ON_HOST((Kokkos::abort(msg);))
+  }
+};
+template <>
+struct RuntimeCheckMemoryAccessViolation<Kokkos::ScratchMemorySpace<Kokkos::Experimental::GB300>,
+                                         Kokkos::DefaultExecutionSpace, false> {
   KOKKOS_FUNCTION RuntimeCheckMemoryAccessViolation(char const* const msg) {
     (void)msg;
     KOKKOS_IF_ON_HOST((Kokkos::abort(msg);))
@@ -277,6 +286,14 @@ struct RuntimeCheckBasicViewMemoryAccessViolation<Kokkos::Experimental::GB300Spa
   }
 };
 template <>
+struct RuntimeCheckBasicViewMemoryAccessViolation<Kokkos::ScratchMemorySpace<Kokkos::Experimental::GB300>,
+                                                  Kokkos::DefaultExecutionSpace, false> {
+  KOKKOS_FUNCTION RuntimeCheckBasicViewMemoryAccessViolation(SharedAllocationTracker const&) {
+    KOKKOS_IF_ON_HOST((Kokkos::abort(
+        "Kokkos::View ERROR: attempt to access inaccessible memory space (GB300 team scratch from host code)");))
+  }
+};
+template <>
 struct RuntimeCheckBasicViewMemoryAccessViolation<Kokkos::HostSpace, Kokkos::DefaultExecutionSpace, true> {
   KOKKOS_FUNCTION RuntimeCheckBasicViewMemoryAccessViolation(SharedAllocationTracker const&) {
     KOKKOS_IF_ON_DEVICE(
@@ -285,6 +302,15 @@ struct RuntimeCheckBasicViewMemoryAccessViolation<Kokkos::HostSpace, Kokkos::Def
 };
 template <>
 struct RuntimeCheckViewMemoryAccessViolation<Kokkos::Experimental::GB300Space, Kokkos::DefaultExecutionSpace, false> {
+  template <class Track, class Map>
+  KOKKOS_FUNCTION RuntimeCheckViewMemoryAccessViolation(char const* const msg, Track const&, Map const&) {
+    (void)msg;
+    KOKKOS_IF_ON_HOST((Kokkos::abort(msg);))
+  }
+};
+template <>
+struct RuntimeCheckViewMemoryAccessViolation<Kokkos::ScratchMemorySpace<Kokkos::Experimental::GB300>,
+                                             Kokkos::DefaultExecutionSpace, false> {
   template <class Track, class Map>
   KOKKOS_FUNCTION RuntimeCheckViewMemoryAccessViolation(char const* const msg, Track const&, Map const&) {
     (void)msg;

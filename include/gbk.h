@@ -287,10 +287,11 @@ int gbk_segmented_scan(int inclusive, gbk_dtype_t in_dtype, gbk_dtype_t out_dtyp
  * GraphImpl core/src/Cuda/Kokkos_Cuda_Graph_Impl.hpp:59-215): every gbk_*
  * call issued on `stream` between begin and end becomes a node of a CUDA
  * graph, in issue order (each node depends on the previous one, as a chain
- * of then_parallel_* nodes).  Calls that synchronise the host (gbk_sort*,
- * gbk_binsort_u64, *_host, gbk_stream_check) cannot be captured.  Before
- * capturing, size the stream's workspace with gbk_workspace_reserve and run
- * each call once uncaptured.  submit() = gbk_graph_launch. */
+ * of then_parallel_* nodes).  Calls that synchronise the host (*_host,
+ * gbk_stream_check) and gbk_binsort_u64 (its staging buffer) cannot be
+ * captured; sorts can.  Before capturing, size the stream's workspace with
+ * gbk_workspace_reserve and run each call once uncaptured.
+ * submit() = gbk_graph_launch. */
 typedef struct gbk_graph_s* gbk_graph_t;
 int gbk_graph_begin(gbk_stream_t stream);
 int gbk_graph_end(gbk_stream_t stream, gbk_graph_t* graph);
@@ -303,8 +304,10 @@ int gbk_graph_destroy(gbk_graph_t graph);
  * the reference's CUDA path is thrust::sort, impl/Kokkos_SortImpl.hpp:204-219).
  * Floating point: -0.0 sorts before +0.0, NaNs after +inf (sign-bit clear)
  * or before -inf (sign-bit set).  Stable LSD radix sort; digit passes whose
- * 8-bit digit is the same for every key are skipped.  n < 2^30.  The call
- * synchronises the stream once (to read the digit histograms back). */
+ * 8-bit digit is the same for every key are skipped, decided on the device
+ * from the digit histogram, so the call never waits for the GPU and can be
+ * captured into a graph (its workspace, about n x (key + value) bytes, must
+ * exist first: gbk_workspace_reserve or one uncaptured call).  n < 2^30. */
 int gbk_sort(gbk_dtype_t key_dtype, void* keys, int64_t n, gbk_stream_t stream);
 /* Experimental::sort_by_key(exec, keys, values) (Kokkos_SortByKeyPublicAPI.hpp:30-114,
  * CUDA path thrust::sort_by_key, impl/Kokkos_SortByKeyImpl.hpp:125-138):

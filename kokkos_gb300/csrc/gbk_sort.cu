@@ -14,9 +14,14 @@
 // The array is cut into G chunks of whole tiles (G <= 2 x the SM count, two
 // scatter CTAs per SM); chunk c belongs to CTA c of every scatter launch.
 // 1. k_digit_hist: one read of the keys counts every 8-bit digit position,
-//    for the whole array and per chunk.  The host reads the whole-array
-//    counts back (one 16 KiB copy and a stream sync per sort) and skips each
-//    pass whose digit is the same for all keys.
+//    for the whole array and per chunk.  k_sort_plan (one CTA) turns the
+//    whole-array counts into each pass's digit starts and a plan on the
+//    device: which passes have a digit that is not the same for every key,
+//    which buffer each of them reads, and how each ranks.  Every pass kernel
+//    reads the plan and returns at once for a constant digit, and a final
+//    copy runs only when the data ended in the temporary buffers, so a sort
+//    is a fixed sequence of launches with no host round trip (it can be
+//    captured into a CUDA graph).
 // 2. Per remaining 8-bit pass:
 //    k_chunk_count (all passes but the first, whose counts come from step 1):
 //      per-chunk counts of the pass's digit; keys stream through a
@@ -141,6 +146,16 @@ __device__ __forceinline__ void drain_stages(unsigned long long* bars, int stage
   for (int64_t j = from; j < to; ++j) mbar_wait(&bars[j % stages], (unsigned)(j / stages) & 1u, limit);
 }
 
+// The sort's plan, built on the device from the digit histogram.
+struct SortPlan {
+  int active[8];   // the pass's digit differs between keys
+  int src[8];      // 0: the pass reads the caller's buffers, 1: the temporaries
+  int first[8];    // the first active pass (its per-chunk counts come from k_digit_hist)
+  int rank_or[8];  // rank with the shared lane masks: no digit value holds over 1/32 of the keys
+  int final_tmp;   // after the last active pass the data is in the temporaries
+  int pad[3];
+};
+
 // ---- 1. all digit positions, whole array and per chunk ----------------------
 // hist[p*256 + d] (u64) and ccounts[(p*nchunks + c)*256 + d] (u32), both
 // zeroed by the caller.  Grid = nchunks * sub.
@@ -193,11 +208,16 @@ constexpr int CNT_SUB = 3;  // CTAs per chunk
 
 // counts[c*256 + d] (u32, zeroed by the caller).  Grid = nchunks * CNT_SUB.
 // TMA: keys 16-byte aligned, streamed through the ring; otherwise plain loads.
+// The plan picks the buffer the pass reads (the caller's or the temporary);
+// the first active pass and passes with a constant digit count nothing.
 template <int DT, bool TMA>
 __global__ void __launch_bounds__(CNT_BLOCK)
-    k_chunk_count(const typename Radix<DT>::K* __restrict__ keys, int64_t n, int64_t chunk_keys, int shift,
+    k_chunk_count(const typename Radix<DT>::K* __restrict__ keys_user, const typename Radix<DT>::K* __restrict__ keys_tmp,
+                  const SortPlan* __restrict__ plan, int pass, int64_t n, int64_t chunk_keys, int shift,
                   unsigned* __restrict__ counts, int* err, int64_t wait_limit) {
   using K = typename Radix<DT>::K;
+  if (!plan->active[pass] || plan->first[pass]) return;
+  const K* __restrict__ keys = plan->src[pass] ? keys_tmp : keys_user;
   constexpr int E = CNT_STAGE_BYTES / (int)sizeof(K);  // keys per stage
   constexpr int WARPS = CNT_BLOCK / 32;
   extern __shared__ __align__(128) unsigned char ring[];
@@ -298,26 +318,93 @@ template <int KB, int VB, int VAR> struct ScShape {
   static_assert(KPT * 32 <= 65535 && TILE <= 65535, "16-bit tile offsets");
 };
 
+// One CTA of 256 threads (one per digit): digit starts of every pass and the
+// plan.  A histogram whose counts do not add up to n (keys changed under the
+// sort) marks every pass inactive and raises the bad-state status.
+template <int KB>
+__global__ void __launch_bounds__(256)
+    k_sort_plan(const unsigned long long* __restrict__ hist, int64_t n, int64_t* __restrict__ off, SortPlan* plan,
+                int* err) {
+  __shared__ unsigned long long s_w[8];
+  __shared__ int s_const[KB], s_hot[KB];
+  __shared__ unsigned long long s_tot[KB];
+  const int d = threadIdx.x, lane = d & 31, warp = d >> 5;
+  for (int p = 0; p < KB; ++p) {
+    const unsigned long long v = hist[p * 256 + d];
+    unsigned long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    unsigned long long pre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      if (w < warp) pre += s_w[w];
+      tot += s_w[w];
+    }
+    off[p * 256 + d] = (int64_t)(pre + inc - v);
+    const int c = __syncthreads_or((int64_t)v == n);
+    const int hot = __syncthreads_or((int64_t)v * 32 > n);
+    if (d == 0) {
+      s_const[p] = c;
+      s_hot[p] = hot;
+      s_tot[p] = tot;
+    }
+    __syncthreads();
+  }
+  if (d == 0) {
+    bool ok = true;
+    for (int p = 0; p < KB; ++p) ok = ok && (int64_t)s_tot[p] == n;
+    if (!ok) atomicOr(err, GBK_EBIT_BAD_STATE);
+    int done = 0;
+    for (int p = 0; p < 8; ++p) {
+      const int act = ok && p < KB && !s_const[p];
+      plan->active[p] = act;
+      plan->src[p] = done & 1;
+      plan->first[p] = act && done == 0;
+      plan->rank_or[p] = p < KB && !s_hot[p];
+      done += act;
+    }
+    plan->final_tmp = done & 1;
+  }
+}
+
 struct ScatterArgs {
   const int64_t* digit_start;  // [256] global start of each digit in this pass
-  const unsigned* counts;      // [nchunks][256] per-chunk digit counts
+  const unsigned* counts;      // [nchunks][256] per-chunk digit counts (the non-first passes)
+  const unsigned* first_counts;  // [nchunks][256] this pass's counts from k_digit_hist (the first active pass)
+  const SortPlan* plan;
   int* err;
   int64_t tiles_per_chunk;
   int64_t wait_limit;
   int shift;
-  int rank_or;  // rank with the shared lane masks (rank_row_or) instead of ballots
+  int pass;
+  int rank_mode;  // 0: the plan's choice, 1: lane masks, 2: ballots
 };
 
 // Grid = nchunks, MINB CTAs per SM.  TMA: kin/vin 16-byte aligned, tiles
 // streamed through the ring; otherwise tiles are loaded with plain loads and
 // stage 0 only holds the reorder.
+// ku / vu: the caller's keys and values, kt / vt: the temporaries; the plan
+// says which pair the pass reads (it writes the other).
 template <int DT, int VB, bool TMA, int VAR>
 __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
-    k_chunk_scatter(const typename Radix<DT>::K* __restrict__ kin, typename Radix<DT>::K* __restrict__ kout,
-                    const typename ValT<VB>::T* __restrict__ vin, typename ValT<VB>::T* __restrict__ vout, int64_t n,
-                    ScatterArgs A) {
+    k_chunk_scatter(typename Radix<DT>::K* ku, typename Radix<DT>::K* kt, typename ValT<VB>::T* vu,
+                    typename ValT<VB>::T* vt, int64_t n, ScatterArgs A) {
   using K = typename Radix<DT>::K;
   using V = typename ValT<VB>::T;
+  const SortPlan* plan = A.plan;
+  if (!plan->active[A.pass]) return;
+  const bool from_tmp = plan->src[A.pass] != 0;
+  const K* __restrict__ kin = from_tmp ? kt : ku;
+  K* __restrict__ kout = from_tmp ? ku : kt;
+  const V* __restrict__ vin = from_tmp ? vt : vu;
+  V* __restrict__ vout = from_tmp ? vu : vt;
+  const unsigned* counts = plan->first[A.pass] ? A.first_counts : A.counts;
+  const int rank_or = A.rank_mode == 1 ? 1 : A.rank_mode == 2 ? 0 : plan->rank_or[A.pass];
   using Sh = ScShape<(int)sizeof(K), VB, VAR>;
   constexpr int BLOCK = Sh::BLOCK, KPT = Sh::KPT, TILE = Sh::TILE, STAGES = Sh::STAGES, WARPS = Sh::WARPS;
   extern __shared__ __align__(128) unsigned char ring[];
@@ -359,7 +446,7 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
   long long run = 0;
   if (threadIdx.x < 256) {
     long long r = A.digit_start[threadIdx.x];
-    const unsigned* cp = A.counts + threadIdx.x;
+    const unsigned* cp = counts + threadIdx.x;
     const int64_t nc = blockIdx.x;
     int64_t q = 0;
     for (; q + 16 <= nc; q += 16) {
@@ -404,7 +491,7 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
         if (VB) val[k] = s_vals[slot];
         dig[k] = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
       }
-      if (A.rank_or) {
+      if (rank_or) {
 #pragma unroll
         for (int k = 0; k < KPT; ++k) rk[k] = rank_row_or<true>(s_cnt[warp], s_rk + warp * 256, dig[k], true, lane);
       } else {
@@ -420,7 +507,7 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
         if (VB) val[k] = slot < cv ? s_vals[slot] : (ok ? vin[base + slot] : V(0));
         dig[k] = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
       }
-      if (A.rank_or) {
+      if (rank_or) {
 #pragma unroll
         for (int k = 0; k < KPT; ++k)
           rk[k] = rank_row_or<false>(s_cnt[warp], s_rk + warp * 256, dig[k], wb + k * 32 + lane < cnt, lane);
@@ -486,7 +573,7 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
       }
     }
     __syncthreads();
-    if (A.rank_or) {  // s_off is dead: clear the lane masks for the next tile (visible after the loop's barrier)
+    if (rank_or) {  // s_off is dead: clear the lane masks for the next tile (visible after the loop's barrier)
       uint4* z = reinterpret_cast<uint4*>(s_rk);
       for (int i = threadIdx.x; i < WARPS * 256 / 4; i += BLOCK) z[i] = make_uint4(0u, 0u, 0u, 0u);
     }
@@ -521,26 +608,24 @@ constexpr int HIST_BLOCK = 512;
 constexpr int HIST_SUB = 4;  // CTAs per chunk for the all-digit histogram
 
 template <int DT, int VB, bool TMA, int VAR>
-int launch_pass(const void* kin, void* kout, const void* vin, void* vout, int64_t n, int64_t nchunks,
-                int64_t chunk_keys, const ScatterArgs& A, unsigned* counts, bool count_first, Workspace* w) {
+int launch_pass(typename Radix<DT>::K* ku, typename Radix<DT>::K* kt, typename ValT<VB>::T* vu,
+                typename ValT<VB>::T* vt, int64_t n, int64_t nchunks, int64_t chunk_keys, const ScatterArgs& A,
+                Workspace* w) {
   using K = typename Radix<DT>::K;
-  using V = typename ValT<VB>::T;
   using Sh = ScShape<(int)sizeof(K), VB, VAR>;
   cudaStream_t s = w->stream;
-  if (count_first) {
-    auto cfn = k_chunk_count<DT, TMA>;
-    constexpr size_t cdyn = TMA ? (size_t)CNT_STAGES * CNT_STAGE_BYTES : 0;
-    static bool cset = false;
-    if (!cset && cdyn) {
-      GBK_CUDA_TRY(cudaFuncSetAttribute(cfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cdyn));
-      cset = true;
-    }
-    GBK_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)nchunks * 256 * 4, s));
-    cfn<<<(unsigned)(nchunks * CNT_SUB), CNT_BLOCK, cdyn, s>>>((const K*)kin, n, chunk_keys, A.shift, counts, w->err,
-                                                               A.wait_limit);
-    note_launch();
-    GBK_CUDA_TRY(cudaGetLastError());
+  auto cfn = k_chunk_count<DT, TMA>;
+  constexpr size_t cdyn = TMA ? (size_t)CNT_STAGES * CNT_STAGE_BYTES : 0;
+  static bool cset = false;
+  if (!cset && cdyn) {
+    GBK_CUDA_TRY(cudaFuncSetAttribute(cfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cdyn));
+    cset = true;
   }
+  GBK_CUDA_TRY(cudaMemsetAsync((void*)A.counts, 0, (size_t)nchunks * 256 * 4, s));
+  cfn<<<(unsigned)(nchunks * CNT_SUB), CNT_BLOCK, cdyn, s>>>(ku, kt, A.plan, A.pass, n, chunk_keys, A.shift,
+                                                             (unsigned*)A.counts, w->err, A.wait_limit);
+  note_launch();
+  GBK_CUDA_TRY(cudaGetLastError());
   auto sfn = k_chunk_scatter<DT, VB, TMA, VAR>;
   constexpr size_t sdyn = (size_t)(TMA ? Sh::STAGES : 1) * Sh::STAGE_BYTES;
   static bool sset = false;
@@ -548,16 +633,26 @@ int launch_pass(const void* kin, void* kout, const void* vin, void* vout, int64_
     GBK_CUDA_TRY(cudaFuncSetAttribute(sfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sdyn));
     sset = true;
   }
-  ScatterArgs a = A;
-  a.counts = counts;
-  sfn<<<(unsigned)nchunks, Sh::BLOCK, sdyn, s>>>((const K*)kin, (K*)kout, (const V*)vin, (V*)vout, n, a);
+  sfn<<<(unsigned)nchunks, Sh::BLOCK, sdyn, s>>>(ku, kt, vu, vt, n, A);
   note_launch();
   return cuda_status(cudaGetLastError());
 }
 
+// After the passes: when an odd number of passes ran, the sorted data is in
+// the temporaries and goes back to the caller's buffers.
+template <class K, class V>
+__global__ void k_sort_copy_back(const SortPlan* __restrict__ plan, const K* __restrict__ kt, K* __restrict__ ku,
+                                 const V* __restrict__ vt, V* __restrict__ vu, int64_t n) {
+  if (!plan->final_tmp) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    ku[i] = kt[i];
+    if (vu) vu[i] = vt[i];
+  }
+}
+
 // Ranking of the scatter passes: GBK_SORT_RANK=masks or =ballot in the
-// environment forces one method for every pass; otherwise it is chosen per
-// pass from the digit histogram.
+// environment forces one method for every pass; otherwise the plan chooses
+// per pass from the digit histogram.
 int sort_rank_mode() {
   static int mode = -1;
   if (mode < 0) {
@@ -582,82 +677,55 @@ int sort_var(void* keys, void* vals, int64_t n, Workspace* w) {
   const int64_t tpc = (ntiles + nchunks - 1) / nchunks;
   nchunks = (ntiles + tpc - 1) / tpc;  // every chunk non-empty
   const int64_t chunk_keys = tpc * TILE;
-  // scratch: histogram | digit starts | per-chunk counts of every digit |
-  // per-chunk counts of one digit | key temp | value temp
+  // scratch: histogram | digit starts | plan | per-chunk counts of every
+  // digit | per-chunk counts of one digit | key temp | value temp
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-  const size_t hb = (size_t)KB * 256 * 8, ob = (size_t)KB * 256 * 8;
+  const size_t hb = (size_t)KB * 256 * 8, ob = (size_t)KB * 256 * 8, pb = 256;
   const size_t ccb = up((size_t)KB * nchunks * 256 * 4), c1b = up((size_t)nchunks * 256 * 4);
   const size_t kb = up((size_t)n * sizeof(K)), vb = VB ? up((size_t)n * VB) : 0;
   int st = GBK_OK;
-  char* scr = ws_scratch(w, hb + ob + ccb + c1b + kb + vb, &st);
+  char* scr = ws_scratch(w, hb + ob + pb + ccb + c1b + kb + vb, &st);
   if (!scr) return st;
   unsigned long long* d_hist = (unsigned long long*)scr;
   int64_t* d_off = (int64_t*)(scr + hb);
-  unsigned* d_cc = (unsigned*)(scr + hb + ob);
-  unsigned* d_c1 = (unsigned*)(scr + hb + ob + ccb);
-  K* ktmp = (K*)(scr + hb + ob + ccb + c1b);
-  V* vtmp = VB ? (V*)(scr + hb + ob + ccb + c1b + kb) : nullptr;
+  SortPlan* d_plan = (SortPlan*)(scr + hb + ob);
+  unsigned* d_cc = (unsigned*)(scr + hb + ob + pb);
+  unsigned* d_c1 = (unsigned*)(scr + hb + ob + pb + ccb);
+  K* ktmp = (K*)(scr + hb + ob + pb + ccb + c1b);
+  V* vtmp = VB ? (V*)(scr + hb + ob + pb + ccb + c1b + kb) : nullptr;
 
   GBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, hb, s));
   GBK_CUDA_TRY(cudaMemsetAsync(d_cc, 0, ccb, s));
   k_digit_hist<DT, HIST_BLOCK><<<(unsigned)(nchunks * HIST_SUB), HIST_BLOCK, 0, s>>>(
       (const K*)keys, n, chunk_keys, HIST_SUB, (int)nchunks, d_hist, d_cc);
-  note_launch();
+  k_sort_plan<KB><<<1, 256, 0, s>>>(d_hist, n, d_off, d_plan, w->err);
+  note_launch(2);
   GBK_CUDA_TRY(cudaGetLastError());
-  std::vector<unsigned long long> h(KB * 256);
-  GBK_CUDA_TRY(cudaMemcpyAsync(h.data(), d_hist, hb, cudaMemcpyDeviceToHost, s));
-  GBK_CUDA_TRY(cudaStreamSynchronize(s));
-  std::vector<int64_t> offs(KB * 256);
-  std::vector<int> passes;
-  for (int p = 0; p < KB; ++p) {
-    int64_t run = 0;
-    bool constant = false;
-    for (int d = 0; d < 256; ++d) {
-      offs[p * 256 + d] = run;
-      run += (int64_t)h[p * 256 + d];
-      if ((int64_t)h[p * 256 + d] == n) constant = true;
-    }
-    if (run != n) return GBK_ERR_CUDA;  // histogram inconsistent
-    if (!constant) passes.push_back(p);
-  }
-  if (passes.empty()) return GBK_OK;
-  GBK_CUDA_TRY(cudaMemcpyAsync(d_off, offs.data(), ob, cudaMemcpyHostToDevice, s));
-  // The host vector must outlive the copy.
-  GBK_CUDA_TRY(cudaStreamSynchronize(s));
-  // Bulk copies want 16-byte aligned sources: the caller's buffers may not be.
+  // Bulk copies want 16-byte aligned sources: the caller's buffers may not be
+  // (the temporaries are); unaligned callers get the plain-load kernels.
   const bool user_aligned = (uintptr_t)keys % 16 == 0 && (!VB || (uintptr_t)vals % 16 == 0);
-  K* kin = (K*)keys;
-  K* kout = ktmp;
-  V* vin = (V*)vals;
-  V* vout = vtmp;
   const int rank_mode = sort_rank_mode();
-  for (size_t i = 0; i < passes.size(); ++i) {
-    const int p = passes[i];
+  for (int p = 0; p < KB; ++p) {
     ScatterArgs A;
     A.digit_start = d_off + p * 256;
-    A.counts = nullptr;
+    A.counts = d_c1;
+    A.first_counts = d_cc + (size_t)p * nchunks * 256;
+    A.plan = d_plan;
     A.err = w->err;
     A.tiles_per_chunk = tpc;
     A.wait_limit = wait_limit();
     A.shift = 8 * p;
-    // Lane-mask ranking unless one digit value holds more than 1/32 of the keys.
-    unsigned long long hmax = 0;
-    for (int d = 0; d < 256; ++d) hmax = std::max(hmax, h[p * 256 + d]);
-    A.rank_or = (rank_mode == 1 || (rank_mode == 0 && (int64_t)hmax * 32 <= n)) ? 1 : 0;
-    // the first pass uses the per-chunk counts of the all-digit histogram
-    unsigned* counts = i == 0 ? d_cc + (size_t)p * nchunks * 256 : d_c1;
-    const bool tma = kin != (K*)keys || user_aligned;
-    st = tma ? launch_pass<DT, VB, true, VAR>(kin, kout, vin, vout, n, nchunks, chunk_keys, A, counts, i > 0, w)
-             : launch_pass<DT, VB, false, VAR>(kin, kout, vin, vout, n, nchunks, chunk_keys, A, counts, i > 0, w);
+    A.pass = p;
+    A.rank_mode = rank_mode;
+    st = user_aligned
+             ? launch_pass<DT, VB, true, VAR>((K*)keys, ktmp, (V*)vals, vtmp, n, nchunks, chunk_keys, A, w)
+             : launch_pass<DT, VB, false, VAR>((K*)keys, ktmp, (V*)vals, vtmp, n, nchunks, chunk_keys, A, w);
     if (st) return st;
-    std::swap(kin, kout);
-    std::swap(vin, vout);
   }
-  if (kin != (K*)keys) {
-    GBK_CUDA_TRY(cudaMemcpyAsync(keys, kin, (size_t)n * sizeof(K), cudaMemcpyDeviceToDevice, s));
-    if (VB) GBK_CUDA_TRY(cudaMemcpyAsync(vals, vin, (size_t)n * VB, cudaMemcpyDeviceToDevice, s));
-  }
-  return GBK_OK;
+  const unsigned cg = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 16);
+  k_sort_copy_back<K, V><<<cg, 256, 0, s>>>(d_plan, ktmp, (K*)keys, vtmp, (V*)vals, n);
+  note_launch();
+  return cuda_status(cudaGetLastError());
 }
 
 template <int DT, int VB>

@@ -52,6 +52,7 @@ _SIGS = {
     "gbk_workspace_reserve": ([vp, i64], ci),
     "gbk_workspace_release_all": ([], ci),
     "gbk_set_wait_limit": ([i64], ci),
+    "gbk_wait_limit": ([], i64),
     "gbk_launch_count": ([], i64),
     "gbk_deep_copy": ([vp, vp, i64, vp], ci),
     "gbk_memset": ([vp, ci, i64, vp], ci),

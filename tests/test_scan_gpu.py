@@ -172,3 +172,32 @@ def test_many_launches_reuse_status_words(env):
         gbk.scan(_dev(torch, x), y, inclusive=True)
         np.testing.assert_array_equal(y.cpu().numpy(), np.cumsum(x.astype(np.int64)))
     gbk.stream_check()
+
+
+def test_bounded_wait_gives_up_cleanly(env):
+    """The device-side wait bound (gbk_set_wait_limit) on the GPU: a scan of
+    2^26 int32 values whose input starts off the 16-byte boundary (the
+    plain-load kernel: its only waits are the look-back polls, no bulk copy is
+    ever in flight) runs with a bound of one poll, so tiles whose predecessor
+    has not published yet give up, publish what they have and end; the call
+    reports GBK_ERR_DEVICE_TIMEOUT (or GBK_OK when no wait ran out), the GPU
+    context stays usable, and the next scan at the default bound is exact."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    n = 1 << 26
+    xh = datagen.uniform_i32(n, 0, 15, seed=4)
+    x = _dev(torch, np.concatenate([np.zeros(1, np.int32), xh]))[1:]
+    y = torch.empty(n, dtype=torch.int64, device="cuda")
+    default = gbk.lib.gbk_wait_limit()
+    assert default > 1000
+    try:
+        assert gbk.lib.gbk_set_wait_limit(1) == 0
+        gbk.scan(x, y, inclusive=True)
+        st = gbk.lib.gbk_stream_check(None)
+        assert st in (0, 4), gbk.lib.gbk_status_string(st)
+        print("bounded wait of one poll:", "timed out" if st == 4 else "no wait ran out")
+    finally:
+        assert gbk.lib.gbk_set_wait_limit(default) == 0
+    gbk.scan(x, y, inclusive=True)
+    gbk.stream_check()
+    np.testing.assert_array_equal(y.cpu().numpy(), np.cumsum(xh, dtype=np.int64))

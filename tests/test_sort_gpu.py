@@ -243,3 +243,62 @@ def test_binsort_vs_oracle_many_bins(env):
     np.testing.assert_array_equal(c.cpu().numpy(), wc)
     np.testing.assert_array_equal(of.cpu().numpy(), wo)
     np.testing.assert_array_equal(p.cpu().numpy(), wp)
+
+
+@pytest.mark.parametrize("varying_bytes", [8, 3])
+def test_graph_with_sort_replays_against_oracle(env, varying_bytes):
+    """Experimental::Graph holding a sort: refill the keys and an iota payload
+    (device copies), sort_by_key, exclusive_scan of the sorted payload into
+    int64, and a Max of the scan, captured once and replayed three times.
+    Every replay is checked against the oracle (the stable sort by key, the
+    reference OpenMP scan and reduce restated).  Keys where only 3 of the 8
+    bytes vary leave 5 constant-digit passes to the device-side plan and an
+    odd number of passes, so the data ends in the temporaries and the final
+    copy-back runs inside the graph."""
+    gbk, torch = env
+    import ctypes
+
+    import oracle
+    from kokkos_gb300 import datagen
+    n = 300007
+    kh = datagen.bits_u64(n, seed=5)
+    if varying_bytes < 8:
+        keep = np.uint64(sum(0xFF << (8 * b) for b in (1, 4, 6)))
+        kh = (kh & keep) | np.uint64(0x0101010101010101) & ~keep
+    iota = np.arange(n, dtype=np.int32)
+    k0, v0 = _dev(torch, kh), _dev(torch, iota)
+    k, v = torch.empty_like(k0), torch.empty_like(v0)
+    y = torch.empty(n, dtype=torch.int64, device="cuda")
+    res = torch.zeros(16, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    P = ctypes.c_void_p
+    gbk.check(gbk.lib.gbk_workspace_reserve(sp, 64 << 20), "reserve")
+
+    def chain():
+        gbk.check(gbk.lib.gbk_deep_copy(P(k.data_ptr()), P(k0.data_ptr()), n * 8, sp), "copy keys")
+        gbk.check(gbk.lib.gbk_deep_copy(P(v.data_ptr()), P(v0.data_ptr()), n * 4, sp), "copy payload")
+        gbk.check(gbk.lib.gbk_sort_by_key(3, P(k.data_ptr()), 4, P(v.data_ptr()), n, sp), "sort_by_key")
+        gbk.scan(v, y, inclusive=False, init=0, stream=s)
+        gbk.reduce("max", y, out=res[0:8], stream=s)
+
+    with torch.cuda.stream(s):
+        chain()  # uncaptured once: the workspace exists before the capture
+    gbk.stream_check(s)
+    ks, perm = oracle.sort_by_key_stable(kh, iota)
+    want_y = oracle.scan(perm, np.int64, inclusive=False, init=0, nthreads=4)
+    want_max = oracle.reduce("max", want_y, 4)
+    g = gbk.Graph(s)
+    with g:
+        chain()
+    for _ in range(3):
+        k.zero_()
+        y.zero_()
+        res.zero_()
+        torch.cuda.synchronize()
+        g.submit()
+        gbk.stream_check(s)
+        np.testing.assert_array_equal(_host(k, np.uint64), ks)
+        np.testing.assert_array_equal(v.cpu().numpy(), perm)
+        np.testing.assert_array_equal(y.cpu().numpy(), want_y)
+        assert gbk.decode_result(res.cpu().numpy()[:8], 3, 1) == want_max
