@@ -25,3 +25,4 @@
 #define KOKKOS_ENABLE_IMPL_MDSPAN
 #define KOKKOS_ENABLE_IMPL_REF_COUNT_BRANCH_UNLIKELY
 #define KOKKOS_ENABLE_LIBDL
+#define KOKKOS_ENABLE_TUNING

@@ -82,6 +82,18 @@ struct Kokkos_Tools_VariableValue {
 };
 
 /* ---- the tool's callbacks (symbols looked up by Kokkos) ------------------- */
+/* Loading and unloading (core/src/impl/Kokkos_Profiling_C_Interface.h:39-52,
+ * typedefs Kokkos_Profiling_initFunction / finalizeFunction).  At finalize,
+ * when the environment variable GBK_TOOL_REPORT names a file, the tool writes
+ * a summary there: the variables Kokkos declared to it (name, id, value type,
+ * candidate count), the number of value requests and contexts, and the best
+ * candidate it found for each tuned context. */
+struct Kokkos_Profiling_KokkosPDeviceInfo {
+  size_t deviceID;
+};
+void kokkosp_init_library(const int load_seq, const uint64_t interface_version, const uint32_t device_info_count,
+                          struct Kokkos_Profiling_KokkosPDeviceInfo* device_info);
+void kokkosp_finalize_library(void);
 void kokkosp_declare_input_type(const char* name, const size_t id, struct Kokkos_Tools_VariableInfo* info);
 void kokkosp_declare_output_type(const char* name, const size_t id, struct Kokkos_Tools_VariableInfo* info);
 void kokkosp_request_values(const size_t context_id, const size_t num_context_values,

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -88,6 +89,8 @@ std::map<size_t, OutVar> g_out;
 std::map<std::string, KeyState> g_states;
 std::map<size_t, Active> g_active;
 std::map<size_t, int> g_goal;  // context id -> Kokkos_Tools_OptimizationType
+int64_t g_requests = 0, g_contexts = 0;
+uint64_t g_interface_version = 0;
 
 std::string value_text(const Kokkos_Tools_VariableValue& v) {
   char buf[96];
@@ -183,6 +186,44 @@ int64_t gbk_tuner_size(void) {
 }
 
 // ---- Kokkos Tools tuning callbacks -------------------------------------------------
+void kokkosp_init_library(const int load_seq, const uint64_t interface_version, const uint32_t device_info_count,
+                          Kokkos_Profiling_KokkosPDeviceInfo* device_info) {
+  (void)load_seq;
+  (void)device_info_count;
+  (void)device_info;
+  std::lock_guard<std::mutex> lk(g_tmu);
+  g_interface_version = interface_version;
+}
+
+void kokkosp_finalize_library(void) {
+  const char* path = std::getenv("GBK_TOOL_REPORT");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "w");
+  if (!f) return;
+  std::lock_guard<std::mutex> lk(g_tmu);
+  std::fprintf(f, "interface_version %llu\n", (unsigned long long)g_interface_version);
+  for (auto& kv : g_in_names) std::fprintf(f, "input %zu %s\n", kv.first, kv.second.c_str());
+  for (auto& kv : g_out)
+    std::fprintf(f, "output %zu %s type %d candidates %zu\n", kv.first, kv.second.name.c_str(), kv.second.type,
+                 kv.second.count());
+  std::fprintf(f, "requests %lld contexts %lld keys %zu\n", (long long)g_requests, (long long)g_contexts,
+               g_states.size());
+  for (auto& kv : g_states) {
+    const KeyState& st = kv.second;
+    if (st.best_time.empty()) continue;
+    const size_t b = (size_t)(std::min_element(st.best_time.begin(), st.best_time.end()) - st.best_time.begin());
+    std::fprintf(f, "best %s ->", kv.first.c_str());
+    for (size_t i = 0; i < st.ids.size() && i < st.comb[b].size(); ++i) {
+      auto it = g_out.find(st.ids[i]);
+      if (it == g_out.end() || it->second.count() == 0) continue;
+      if (it->second.type == kokkos_value_double) std::fprintf(f, " %s=%g", it->second.name.c_str(), it->second.dvals[st.comb[b][i]]);
+      else std::fprintf(f, " %s=%lld", it->second.name.c_str(), (long long)it->second.ivals[st.comb[b][i]]);
+    }
+    std::fprintf(f, " tried %zu of %zu\n", std::min(st.next, st.comb.size()), st.comb.size());
+  }
+  std::fclose(f);
+}
+
 void kokkosp_declare_input_type(const char* name, const size_t id, Kokkos_Tools_VariableInfo* info) {
   (void)info;
   std::lock_guard<std::mutex> lk(g_tmu);
@@ -207,6 +248,17 @@ void kokkosp_declare_output_type(const char* name, const size_t id, Kokkos_Tools
       for (int64_t v = lo; (r.openUpper ? v < r.upper.int_value : v <= r.upper.int_value) && o.ivals.size() < 64;
            v += step)
         o.ivals.push_back(v);
+    } else if (info->valueQuantity == kokkos_value_range && info->type == kokkos_value_double) {
+      // e.g. the coordinates Kokkos' MDRange and team-size tuners declare
+      // (core/src/Kokkos_Tuners.hpp:334-348): at most 16 evenly spread points
+      const auto& r = info->candidates.range;
+      const double lo = r.lower.double_value, hi = r.upper.double_value;
+      double step = r.step.double_value > 0 ? r.step.double_value : (hi - lo) / 16;
+      const double span = hi - lo;
+      if (span > 0 && span / step > 16) step = span / 16;
+      for (double v = lo + (r.openLower ? step : 0.0); (r.openUpper ? v < hi : v <= hi) && o.dvals.size() < 16;
+           v += step)
+        o.dvals.push_back(v);
     }
   }
   std::lock_guard<std::mutex> lk(g_tmu);
@@ -220,6 +272,7 @@ void kokkosp_declare_optimization_goal(const size_t context_id, const Kokkos_Too
 
 void kokkosp_begin_context(const size_t context_id) {
   std::lock_guard<std::mutex> lk(g_tmu);
+  ++g_contexts;
   Active& a = g_active[context_id];
   a.t0 = std::chrono::steady_clock::now();
   a.timed = false;
@@ -228,6 +281,7 @@ void kokkosp_begin_context(const size_t context_id) {
 void kokkosp_request_values(const size_t context_id, const size_t nctx, const Kokkos_Tools_VariableValue* cvals,
                             const size_t ntune, Kokkos_Tools_VariableValue* tvals) {
   std::lock_guard<std::mutex> lk(g_tmu);
+  ++g_requests;
   // Context key and the gbk.* context variables.
   std::vector<std::pair<std::string, std::string>> kv;
   int gk[5] = {-1, -1, -1, -1, 0};

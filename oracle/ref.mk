@@ -21,7 +21,8 @@ CORE_SRCS = $(wildcard $(REF)/core/src/impl/*.cpp) \
             $(REF)/core/src/OpenMP/Kokkos_OpenMP_Instance.cpp \
             $(REF)/core/src/OpenMP/Kokkos_OpenMP_Task.cpp \
             $(REF)/core/src/Serial/Kokkos_Serial.cpp \
-            $(REF)/core/src/Serial/Kokkos_Serial_Task.cpp
+            $(REF)/core/src/Serial/Kokkos_Serial_Task.cpp \
+            $(REF)/containers/src/impl/Kokkos_UnorderedMap_impl.cpp
 CORE_OBJS = $(patsubst $(REF)/%.cpp,$(OUT)/obj/%.o,$(CORE_SRCS))
 
 all: $(OUT)/libkokkos_ref.a $(OUT)/ref_runner

@@ -14,21 +14,28 @@
 //   exscan_i32_i64 <n> <init>               Experimental::exclusive_scan (i32 -> i64)
 //   inscan <dtype> <n>                      Experimental::inclusive_scan (same type)
 //   scan_total_i64 <n>                      parallel_scan with total (i64)
-//   mdrange <op> <dtype> <n0> <n1> <n2>     MDRangePolicy<Rank<3>> over LayoutLeft View<T***>
+//   mdrange <op> <dtype> <n0> <n1> <n2> [reps]  MDRangePolicy<Rank<3>> over LayoutLeft View<T***>
+//                                           (run reps times: the same result each time)
 //   hist <n> <nbins>                        ScatterView histogram into int64 bins
 //   sort_u64 <n>                            Kokkos::sort
 //   sort_pairs_stable <n>                   Kokkos::sort of (key, index) pairs with a comparator
 //   sort_by_key <n>                         Experimental::sort_by_key (u64 keys, i32 values)
 //   binsort <n> <nbins> <kmin> <kmax>       BinSort + BinOp1D: counts, offsets, permutation
 //   team_reduce_sum_f64 <nseg>              TeamPolicy league reduce: per-segment sums (offsets input)
+//   algos_i64 <n>                           std transform_reduce (unary, binary), min/max/minmax_element,
+//                                           transform_exclusive_scan, transform_inclusive_scan
+//   team_scan_i32 <nseg>                    TeamThreadRange parallel_scan per league rank (offsets input)
+//   umap_count <n> <capacity>               UnorderedMap<int32,int64> insert with AtomicAdd: key counts
 #include <Kokkos_Core.hpp>
 #include <Kokkos_ScatterView.hpp>
 #include <Kokkos_Sort.hpp>
 #include <Kokkos_StdAlgorithms.hpp>
+#include <Kokkos_UnorderedMap.hpp>
 
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -102,7 +109,9 @@ void run_reduce(int op, int64_t n, const std::vector<unsigned char>& in, const c
 
 // ---- MDRange over LayoutLeft View<T***>; loc = i + n0*(j + n1*k) --------------
 template <class T>
-void run_mdrange(int op, int64_t n0, int64_t n1, int64_t n2, const std::vector<unsigned char>& in, const char* outp) {
+void run_mdrange(int op, int64_t n0, int64_t n1, int64_t n2, const std::vector<unsigned char>& in, const char* outp,
+                 int reps) {
+  for (int rep = 1; rep < reps; ++rep) run_mdrange<T>(op, n0, n1, n2, in, outp, 1);
   Kokkos::View<T***, Kokkos::LayoutLeft, HostMem> x("x", n0, n1, n2);
   std::memcpy(x.data(), in.data(), sizeof(T) * (size_t)(n0 * n1 * n2));
   Kokkos::MDRangePolicy<Exec, Kokkos::Rank<3>> pol({0, 0, 0}, {n0, n1, n2});
@@ -185,8 +194,9 @@ int main(int argc, char** argv) {
       write_all(outp, y.data(), sizeof(int64_t) * (size_t)(n + 1));
     } else if (cmd == "mdrange") {
       const int op = (int)a(0), dt = (int)a(1);
-      if (dt == 4) run_mdrange<float>(op, a(2), a(3), a(4), in, outp);
-      else if (dt == 5) run_mdrange<double>(op, a(2), a(3), a(4), in, outp);
+      const int reps = argc > 10 ? (int)a(5) : 1;
+      if (dt == 4) run_mdrange<float>(op, a(2), a(3), a(4), in, outp, reps);
+      else if (dt == 5) run_mdrange<double>(op, a(2), a(3), a(4), in, outp, reps);
       else std::exit(3);
     } else if (cmd == "hist") {
       const int64_t n = a(0), nb = a(1);
@@ -269,6 +279,72 @@ int main(int argc, char** argv) {
         Kokkos::single(Kokkos::PerTeam(t), [&]() { r(s) = v; });
       });
       write_all(outp, r.data(), sizeof(double) * (size_t)nseg);
+    } else if (cmd == "algos_i64") {
+      // out: [transform_reduce(x, 3, +, v*v%1009), min_element, max_element,
+      //       minmax_element first, second, transform_reduce(x, x, 11) (dot),
+      //       transform_exclusive_scan(x, 5, +, 2v+1)[n], transform_inclusive_scan(x, +, v%7)[n]]
+      const int64_t n = a(0);
+      auto x = to_view<int64_t>(in, n);
+      Kokkos::View<int64_t*, HostMem> ex("ex", n), inc("inc", n);
+      std::vector<int64_t> o;
+      o.push_back(KE::transform_reduce(Exec(), KE::cbegin(x), KE::cend(x), int64_t{3},
+                                       KOKKOS_LAMBDA(int64_t p, int64_t q) { return p + q; },
+                                       KOKKOS_LAMBDA(int64_t v) { return v * v % 1009; }));
+      o.push_back(KE::min_element(Exec(), x) - KE::begin(x));
+      o.push_back(KE::max_element(Exec(), x) - KE::begin(x));
+      auto mm = KE::minmax_element(Exec(), x);
+      o.push_back(mm.first - KE::begin(x));
+      o.push_back(mm.second - KE::begin(x));
+      o.push_back(KE::transform_reduce(Exec(), KE::cbegin(x), KE::cend(x), KE::cbegin(x), int64_t{11}));
+      KE::transform_exclusive_scan(Exec(), KE::cbegin(x), KE::cend(x), KE::begin(ex), int64_t{5},
+                                   KOKKOS_LAMBDA(int64_t p, int64_t q) { return p + q; },
+                                   KOKKOS_LAMBDA(int64_t v) { return 2 * v + 1; });
+      KE::transform_inclusive_scan(Exec(), KE::cbegin(x), KE::cend(x), KE::begin(inc),
+                                   KOKKOS_LAMBDA(int64_t p, int64_t q) { return p + q; },
+                                   KOKKOS_LAMBDA(int64_t v) { return v % 7; });
+      for (int64_t i = 0; i < n; ++i) o.push_back(ex(i));
+      for (int64_t i = 0; i < n; ++i) o.push_back(inc(i));
+      write_all(outp, o.data(), sizeof(int64_t) * o.size());
+    } else if (cmd == "team_scan_i32") {
+      // input: nseg+1 int64 offsets followed by the int32 values; out: per
+      // segment exclusive scan (TeamThreadRange parallel_scan) into int32
+      const int64_t nseg = a(0);
+      const int64_t* offs = (const int64_t*)in.data();
+      const int64_t n = offs[nseg];
+      Kokkos::View<int64_t*, HostMem> o("o", nseg + 1);
+      std::memcpy(o.data(), offs, sizeof(int64_t) * (size_t)(nseg + 1));
+      Kokkos::View<int32_t*, HostMem> x("x", n), y("y", n);
+      std::memcpy(x.data(), in.data() + sizeof(int64_t) * (nseg + 1), sizeof(int32_t) * (size_t)n);
+      using TP = Kokkos::TeamPolicy<Exec>;
+      Kokkos::parallel_for(TP(nseg, Kokkos::AUTO), KOKKOS_LAMBDA(const TP::member_type& t) {
+        const int64_t s = t.league_rank();
+        Kokkos::parallel_scan(Kokkos::TeamThreadRange(t, o(s), o(s + 1)), [&](int64_t i, int32_t& u, bool fin) {
+          if (fin) y(i) = u;
+          u += x(i);
+        });
+      });
+      write_all(outp, y.data(), sizeof(int32_t) * (size_t)n);
+    } else if (cmd == "umap_count") {
+      // out: [size, failed_insert, (key, count) pairs sorted by key]
+      const int64_t n = a(0), cap = a(1);
+      auto k = to_view<int32_t>(in, n);
+      using Map = Kokkos::UnorderedMap<int32_t, int64_t, HostMem>;
+      Map m(cap);
+      using Op = Kokkos::UnorderedMapInsertOpTypes<Kokkos::View<int64_t*, HostMem>, int32_t>::AtomicAdd;
+      Op op;
+      Kokkos::parallel_for(Kokkos::RangePolicy<Exec>(0, n), KOKKOS_LAMBDA(int64_t i) { m.insert(k(i), int64_t{1}, op); });
+      std::vector<std::pair<int32_t, int64_t>> kv;
+      for (uint32_t i = 0; i < m.capacity(); ++i)
+        if (m.valid_at(i)) kv.push_back({m.key_at(i), m.value_at(i)});
+      std::sort(kv.begin(), kv.end());
+      std::vector<int64_t> o;
+      o.push_back((int64_t)m.size());
+      o.push_back(m.failed_insert() ? 1 : 0);
+      for (auto& e : kv) {
+        o.push_back(e.first);
+        o.push_back(e.second);
+      }
+      write_all(outp, o.data(), sizeof(int64_t) * o.size());
     } else {
       std::fprintf(stderr, "unknown command %s\n", cmd.c_str());
       Kokkos::finalize();

@@ -153,6 +153,20 @@ def main():
     G["teamreduce/f64/50/x"] = xv
     G["teamreduce/f64/50/out"] = run(4, "team_reduce_sum_f64", np.concatenate([offs.view(np.uint8), xv.view(np.uint8)]), 50)
 
+    # -- std algorithms beyond reduce/scan, nested team scan, UnorderedMap ---
+    for n in (1, 1000, 65537):
+        x = datagen.uniform_i64(n, -5000, 5000, seed=n + 21)
+        G[f"algos/i64/{n}/x"] = x
+        G[f"algos/i64/{n}/out"] = run(4, "algos_i64", x, n)
+    G["teamscan/i32/50/offsets"] = offs
+    xs = datagen.uniform_i32(int(offs[-1]), 0, 255, seed=4)
+    G["teamscan/i32/50/x"] = xs
+    G["teamscan/i32/50/out"] = run(4, "team_scan_i32", np.concatenate([offs.view(np.uint8), xs.view(np.uint8)]), 50)
+    keys = datagen.zipf_i32(100000, 3000, 1.1, seed=6)
+    G["umap/i32/100000/x"] = keys
+    G["umap/i32/100000/4096/out"] = run(4, "umap_count", keys, keys.size, 4096)
+    G["umap/i32/100000/1000/out"] = run(1, "umap_count", keys, keys.size, 1000)  # too small: failed inserts
+
     out = os.path.join(ROOT, "tests", "golden", "golden.npz")
     np.savez_compressed(out, **G)
     print(f"wrote {len(G)} arrays to {out} ({os.path.getsize(out) / 1e6:.2f} MB)")

@@ -193,3 +193,57 @@ def test_range_candidates(lib):
         lib.kokkosp_end_context(3, VariableValue())
         got.append(tv[0].value.int_value)
     assert sorted(got) == [1, 2, 3, 4]
+
+
+REF_RUNNER = os.path.join(ROOT, "oracle", "_ref", "ref_runner")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_RUNNER), reason="reference build (oracle/_ref) not present")
+def test_reference_loads_libgbk_as_its_tuning_tool():
+    """The reference's own tool loader (KOKKOS_TOOLS_LIBS,
+    core/src/impl/Kokkos_Profiling.cpp:148-165,581-705) loads libgbk.so as
+    its Kokkos Tools tool, with internal tuning on (KOKKOS_TUNE_INTERNALS):
+    the reference declares its context and tile-size / team-size variables
+    to the tool through the struct layouts of Kokkos_Profiling_C_Interface.h,
+    asks for values once per kernel, and the kernels still give the reference
+    outputs (an MDRange MinLoc run six times, a TeamPolicy(AUTO) scan over
+    uneven segments).  The tool's report (GBK_TOOL_REPORT) shows what it was
+    told and what it answered."""
+    import subprocess
+
+    import numpy as np
+    G = np.load(os.path.join(ROOT, "tests", "golden", "golden.npz"))
+    lib = os.path.join(ROOT, "kokkos_gb300", "libgbk.so")
+    if not os.path.exists(lib):
+        import __graft_entry__
+        __graft_entry__.build()
+    with tempfile.TemporaryDirectory() as td:
+        env = dict(os.environ, OMP_PROC_BIND="false", KOKKOS_TOOLS_LIBS=lib, KOKKOS_TUNE_INTERNALS="1")
+        # MDRange MinLoc, six times: six value requests for the tile sizes
+        x = G["mdrange/f32/37x19x11/x"]
+        x.tofile(os.path.join(td, "x.bin"))
+        rep = os.path.join(td, "md.txt")
+        subprocess.run([REF_RUNNER, "2", "mdrange", os.path.join(td, "x.bin"), os.path.join(td, "o.bin"), "8", "4",
+                        "37", "19", "11", "6"], env=dict(env, GBK_TOOL_REPORT=rep), check=True, capture_output=True)
+        got = np.fromfile(os.path.join(td, "o.bin"), dtype=np.uint8)
+        assert got.tobytes() == G["mdrange/minloc/f32/37x19x11/4/out"].tobytes()
+        lines = open(rep).read().splitlines()
+        assert int(lines[0].split()[1]) > 0  # the reference's tools interface version
+        inputs = [ln.split()[2] for ln in lines if ln.startswith("input ")]
+        assert "kokkos.kernel_name" in inputs and "kokkos.kernel_type" in inputs
+        outs = [ln for ln in lines if ln.startswith("output ")]
+        assert len(outs) == 3 and all("_tile_size_" in ln for ln in outs)
+        assert all(int(ln.split()[-1]) > 0 for ln in outs), outs  # candidates parsed from the reference's ranges
+        req = [ln for ln in lines if ln.startswith("requests ")][0].split()
+        assert int(req[1]) == 6 and int(req[3]) >= 6
+        assert any(ln.startswith("best ") and "tried 6 of" in ln for ln in lines)
+        # TeamPolicy(AUTO): the team-size tuner; the scan result does not depend on it
+        offs, xs = G["teamscan/i32/50/offsets"], G["teamscan/i32/50/x"]
+        np.concatenate([offs.view(np.uint8), xs.view(np.uint8)]).tofile(os.path.join(td, "t.bin"))
+        rep2 = os.path.join(td, "team.txt")
+        subprocess.run([REF_RUNNER, "2", "team_scan_i32", os.path.join(td, "t.bin"), os.path.join(td, "o2.bin"), "50"],
+                       env=dict(env, GBK_TOOL_REPORT=rep2), check=True, capture_output=True)
+        got2 = np.fromfile(os.path.join(td, "o2.bin"), dtype=np.uint8)
+        assert got2.tobytes() == G["teamscan/i32/50/out"].tobytes()
+        team = open(rep2).read()
+        assert "requests 1 " in team, team
