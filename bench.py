@@ -399,6 +399,27 @@ def other_configs(torch, gbk, datagen, stream, dev, hbm, peak_kind, reps=10):
     del k0, bcnt, boff, bperm
     del iota, dk, dv
 
+    # ---- the header-template path for user functors (C++ program) -------------
+    hp = os.path.join(ROOT, "kokkos_gb300", "_build", "bench_header_path")
+    if os.path.exists(hp):
+        lens_h, _ = datagen.lognormal_lengths(10000, median=2048.0, max_len=1 << 21, target_total=1 << 28, seed=0)
+        offs_h = datagen.offsets_from_lengths(lens_h)
+        with tempfile.TemporaryDirectory() as td:
+            fo = os.path.join(td, "offsets.bin")
+            offs_h.astype(np.int64).tofile(fo)
+            torch.cuda.synchronize()
+            r = subprocess.run([hp, fo, str(len(lens_h)), "20"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                               text=True, timeout=600)
+        if r.returncode == 0:
+            hj = json.loads(r.stdout.strip().splitlines()[-1])
+            for v in hj.values():
+                for k in ("GB/s", "library_GB/s"):
+                    if k in v:
+                        v[k.replace("GB/s", "frac_of_" + peak_kind + "_hbm")] = round(v[k] / hbm, 4)
+            out["header_path_user_functors"] = hj
+        else:
+            out["header_path_user_functors"] = {"error": r.stdout[-300:]}
+
     # ---- data movement either side of the path --------------------------------
     nb = 1 << 30
     a_ = torch.empty(nb // 4, dtype=torch.int32, device=dev)

@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <atomic>
 #include <cstdint>
 #include <cstdlib>
@@ -143,13 +144,15 @@ inline void finalize() {
 inline void fence(const std::string& = std::string()) { Experimental::GB300::impl_static_fence(); }
 
 // ---------------------------------------------------------------------------
-// View: rank 1..3, LayoutLeft / LayoutRight, device (GB300Space) or host.
+// View: rank 1..6, LayoutLeft / LayoutRight, device (GB300Space) or host.
 namespace Impl {
-template <class D> struct ViewRank;
+template <class D> struct ViewRank { using value_type = D; static constexpr int rank = 0; };  // View<T>: one value
 template <class T> struct ViewRank<T*> { using value_type = T; static constexpr int rank = 1; };
 template <class T> struct ViewRank<T**> { using value_type = T; static constexpr int rank = 2; };
 template <class T> struct ViewRank<T***> { using value_type = T; static constexpr int rank = 3; };
 template <class T> struct ViewRank<T****> { using value_type = T; static constexpr int rank = 4; };
+template <class T> struct ViewRank<T*****> { using value_type = T; static constexpr int rank = 5; };
+template <class T> struct ViewRank<T******> { using value_type = T; static constexpr int rank = 6; };
 
 template <class... P> struct ViewProps;
 template <> struct ViewProps<> { using layout = LayoutLeft; using space = GB300Space; };
@@ -182,8 +185,13 @@ class View {
   static constexpr bool is_device = std::is_same<memory_space, GB300Space>::value;
 
   KOKKOS_INLINE_FUNCTION View() {}
-  View(const std::string& label, int64_t n0, int64_t n1 = 1, int64_t n2 = 1, int64_t n3 = 1) {
-    set_extents(n0, n1, n2, n3);
+  // rank 0: one value
+  template <int R = rank, std::enable_if_t<R == 0, bool> = true>
+  explicit View(const std::string& label) : View(label, 1) {}
+  KOKKOS_FORCEINLINE_FUNCTION value_type& operator()() const { return ptr_[0]; }
+  View(const std::string& label, int64_t n0, int64_t n1 = 1, int64_t n2 = 1, int64_t n3 = 1, int64_t n4 = 1,
+       int64_t n5 = 1) {
+    set_extents(n0, n1, n2, n3, n4, n5);
     const size_t bytes = sizeof(value_type) * (size_t)size();
     trk_ = new Impl::Tracker();
     trk_->label = label;
@@ -197,11 +205,13 @@ class View {
     ptr_ = (value_type*)trk_->ptr;
   }
   // Unmanaged view of caller memory.
-  KOKKOS_INLINE_FUNCTION View(value_type* p, int64_t n0, int64_t n1 = 1, int64_t n2 = 1, int64_t n3 = 1) : ptr_(p) {
-    set_extents(n0, n1, n2, n3);
+  KOKKOS_INLINE_FUNCTION View(value_type* p, int64_t n0, int64_t n1 = 1, int64_t n2 = 1, int64_t n3 = 1,
+                              int64_t n4 = 1, int64_t n5 = 1)
+      : ptr_(p) {
+    set_extents(n0, n1, n2, n3, n4, n5);
   }
   KOKKOS_INLINE_FUNCTION View(const View& o) : ptr_(o.ptr_), trk_(o.trk_) {
-    for (int d = 0; d < 4; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
+    for (int d = 0; d < kMaxRank; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
     retain();
   }
   // Same data type, layout and memory space spelled with other properties
@@ -212,7 +222,7 @@ class View {
                                  !std::is_same<View<DataType, P2...>, View>::value,
                              bool> = true>
   KOKKOS_INLINE_FUNCTION View(const View<DataType, P2...>& o) : ptr_(o.ptr_), trk_(o.trk_) {
-    for (int d = 0; d < 4; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
+    for (int d = 0; d < kMaxRank; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
     retain();
   }
   template <class D2, class... P2>
@@ -223,7 +233,7 @@ class View {
       release();
       ptr_ = o.ptr_;
       trk_ = o.trk_;
-      for (int d = 0; d < 4; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
+      for (int d = 0; d < kMaxRank; ++d) { ext_[d] = o.ext_[d]; str_[d] = o.str_[d]; }
       retain();
     }
     return *this;
@@ -237,6 +247,13 @@ class View {
   }
   KOKKOS_FORCEINLINE_FUNCTION value_type& operator()(int64_t i, int64_t j, int64_t k, int64_t l) const {
     return ptr_[i * str_[0] + j * str_[1] + k * str_[2] + l * str_[3]];
+  }
+  KOKKOS_FORCEINLINE_FUNCTION value_type& operator()(int64_t i, int64_t j, int64_t k, int64_t l, int64_t m) const {
+    return ptr_[i * str_[0] + j * str_[1] + k * str_[2] + l * str_[3] + m * str_[4]];
+  }
+  KOKKOS_FORCEINLINE_FUNCTION value_type& operator()(int64_t i, int64_t j, int64_t k, int64_t l, int64_t m,
+                                                     int64_t q) const {
+    return ptr_[i * str_[0] + j * str_[1] + k * str_[2] + l * str_[3] + m * str_[4] + q * str_[5]];
   }
   KOKKOS_FORCEINLINE_FUNCTION value_type& operator[](int64_t i) const { return ptr_[i]; }
   KOKKOS_INLINE_FUNCTION value_type* data() const { return ptr_; }
@@ -253,16 +270,16 @@ class View {
   long use_count() const { return trk_ ? trk_->count.load() : 0; }
 
  private:
-  KOKKOS_INLINE_FUNCTION void set_extents(int64_t n0, int64_t n1, int64_t n2, int64_t n3) {
-    const int64_t e[4] = {n0, n1, n2, n3};
-    for (int d = 0; d < 4; ++d) ext_[d] = d < rank ? e[d] : 1;
+  KOKKOS_INLINE_FUNCTION void set_extents(int64_t n0, int64_t n1, int64_t n2, int64_t n3, int64_t n4, int64_t n5) {
+    const int64_t e[kMaxRank] = {n0, n1, n2, n3, n4, n5};
+    for (int d = 0; d < kMaxRank; ++d) ext_[d] = d < rank || (rank == 0 && d == 0) ? e[d] : 1;
     if (std::is_same<array_layout, LayoutLeft>::value) {
       int64_t s = 1;
-      for (int d = 0; d < 4; ++d) { str_[d] = s; s *= ext_[d]; }
+      for (int d = 0; d < kMaxRank; ++d) { str_[d] = s; s *= ext_[d]; }
     } else {
       int64_t s = 1;
       for (int d = rank - 1; d >= 0; --d) { str_[d] = s; s *= ext_[d]; }
-      for (int d = rank; d < 4; ++d) str_[d] = s;
+      for (int d = rank; d < kMaxRank; ++d) str_[d] = s;
     }
   }
   KOKKOS_INLINE_FUNCTION void retain() {
@@ -283,16 +300,18 @@ class View {
 #endif
   }
 
+  static constexpr int kMaxRank = 6;
   value_type* ptr_ = nullptr;
   Impl::Tracker* trk_ = nullptr;
-  int64_t ext_[4] = {0, 1, 1, 1};
-  int64_t str_[4] = {1, 1, 1, 1};
+  int64_t ext_[kMaxRank] = {0, 1, 1, 1, 1, 1};
+  int64_t str_[kMaxRank] = {1, 1, 1, 1, 1, 1};
 };
 
 template <class D, class... P>
 auto create_mirror_view(const View<D, P...>& v) {
   using L = typename View<D, P...>::array_layout;
-  return View<D, L, HostSpace>(v.label() + "_mirror", v.extent(0), v.extent(1), v.extent(2), v.extent(3));
+  return View<D, L, HostSpace>(v.label() + "_mirror", v.extent(0), v.extent(1), v.extent(2), v.extent(3), v.extent(4),
+                               v.extent(5));
 }
 
 // deep_copy between views of equal extents and layout (one contiguous copy)
@@ -356,36 +375,140 @@ class RangePolicy {
 enum class Iterate { Default, Left, Right };
 template <unsigned N, Iterate OuterDir = Iterate::Default, Iterate InnerDir = Iterate::Default>
 struct Rank {
+  static_assert(N >= 2 && N <= 6, "Kokkos::Rank: MDRangePolicy ranks 2..6");
   static constexpr int rank = N;
+  static constexpr Iterate outer_direction = OuterDir;
+  static constexpr Iterate inner_direction = InnerDir;
+};
+template <class T>
+struct IndexType {
+  using type = T;
 };
 
-template <class RankT, class ExecSpace = Experimental::GB300>
-class MDRangePolicy {
+namespace Impl {
+template <class T> struct is_rank : std::false_type {};
+template <unsigned N, Iterate O, Iterate I> struct is_rank<Rank<N, O, I>> : std::true_type {};
+template <class T> struct is_index_type : std::false_type {};
+template <class T> struct is_index_type<IndexType<T>> : std::true_type {};
+// The properties of an MDRangePolicy in any order (the reference's
+// PolicyTraits): the Rank, an execution space, an IndexType and a work tag
+// (any other class type).
+template <class... P> struct MDProps {
+  using rank = void;
+  using space = Experimental::GB300;
+  using tag = void;
+  using index = int64_t;
+};
+template <class P0, class... P> struct MDProps<P0, P...> {
+  using rest = MDProps<P...>;
+  using rank = std::conditional_t<is_rank<P0>::value, P0, typename rest::rank>;
+  using space = std::conditional_t<std::is_same<P0, Experimental::GB300>::value, P0, typename rest::space>;
+  using index = typename std::conditional_t<is_index_type<P0>::value, P0, IndexType<typename rest::index>>::type;
+  using tag = std::conditional_t<is_rank<P0>::value || std::is_same<P0, Experimental::GB300>::value ||
+                                     is_index_type<P0>::value,
+                                 typename rest::tag, P0>;
+};
+}  // namespace Impl
+
+// MDRangePolicy<Rank<N[, outer, inner]>, ...>(lower, upper[, tile])
+// (core/src/KokkosExp_MDRangePolicy.hpp:159-458): ranks 2..6, bounds as
+// braced lists (their length fixes the rank for the deduction guides) or
+// arrays.  Iteration directions default to Iterate::Left on this GPU space
+// (dimension 0 fastest, as the reference's CUDA space,
+// core/src/Cuda/Kokkos_Cuda_MDRangePolicy.hpp:24-36); the inner direction is
+// the dimension that varies fastest between consecutive threads (Right: the
+// last).  Tile sizes are checked as the reference checks them (at most 1024
+// threads in a tile, the abort of KokkosExp_MDRangePolicy.hpp:416-424) and
+// otherwise do not change the walk: every tile shape covers the same
+// elements, and the flat walk keeps warps on consecutive addresses.
+// (declared as a partial specialisation so that only the guides below deduce
+// a braced-list policy, as the reference does, KokkosExp_MDRangePolicy.hpp:168-175)
+template <class... Props>
+class MDRangePolicy;
+template <class P0, class... Props>
+class MDRangePolicy<P0, Props...> {
+  using props = Impl::MDProps<P0, Props...>;
+  static_assert(!std::is_void<typename props::rank>::value, "Kokkos Error: MD iteration pattern not defined");
+
  public:
-  static constexpr int rank = RankT::rank;
-  static_assert(rank >= 2 && rank <= 4, "MDRangePolicy rank 2..4");
-  using execution_space = ExecSpace;
-  MDRangePolicy(std::initializer_list<int64_t> lo, std::initializer_list<int64_t> up) { set(lo, up); }
-  MDRangePolicy(const ExecSpace& s, std::initializer_list<int64_t> lo, std::initializer_list<int64_t> up) : space_(s) {
-    set(lo, up);
+  using rank_type = typename props::rank;
+  using execution_space = typename props::space;
+  using work_tag = typename props::tag;
+  using index_type = typename props::index;
+  using execution_policy = MDRangePolicy;
+  static constexpr int rank = rank_type::rank;
+  static constexpr Iterate outer_direction =
+      rank_type::outer_direction == Iterate::Default ? Iterate::Left : rank_type::outer_direction;
+  static constexpr Iterate inner_direction =
+      rank_type::inner_direction == Iterate::Default ? Iterate::Left : rank_type::inner_direction;
+
+  template <class LT, size_t LN, class UT, size_t UN>
+  MDRangePolicy(const LT (&lo)[LN], const UT (&up)[UN]) {
+    static_assert(LN == rank && UN == rank, "MDRangePolicy: Constructor initializer lists have wrong size");
+    set<LT, UT, int64_t>(lo, up, nullptr, 0);
   }
+  template <class LT, size_t LN, class UT, size_t UN, class TT, size_t TN>
+  MDRangePolicy(const LT (&lo)[LN], const UT (&up)[UN], const TT (&tile)[TN]) {
+    static_assert(LN == rank && UN == rank && TN <= rank, "MDRangePolicy: Constructor initializer lists have wrong size");
+    set(lo, up, tile, TN);
+  }
+  template <class LT, size_t LN, class UT, size_t UN>
+  MDRangePolicy(const execution_space& s, const LT (&lo)[LN], const UT (&up)[UN]) : space_(s) {
+    static_assert(LN == rank && UN == rank, "MDRangePolicy: Constructor initializer lists have wrong size");
+    set<LT, UT, int64_t>(lo, up, nullptr, 0);
+  }
+  template <class LT, size_t LN, class UT, size_t UN, class TT, size_t TN>
+  MDRangePolicy(const execution_space& s, const LT (&lo)[LN], const UT (&up)[UN], const TT (&tile)[TN]) : space_(s) {
+    static_assert(LN == rank && UN == rank && TN <= rank, "MDRangePolicy: Constructor initializer lists have wrong size");
+    set(lo, up, tile, TN);
+  }
+
+  // bounds of mixed integer types ({0, n}): the reference's point_type
+  // constructors (KokkosExp_MDRangePolicy.hpp:249-259)
+  using point_type = std::array<int64_t, rank>;
+  MDRangePolicy(const point_type& lo, const point_type& up, const point_type& tile = point_type{}) {
+    set<int64_t, int64_t, int64_t>(lo.data(), up.data(), tile.data(), rank);
+  }
+  MDRangePolicy(const execution_space& s, const point_type& lo, const point_type& up,
+                const point_type& tile = point_type{})
+      : space_(s) {
+    set<int64_t, int64_t, int64_t>(lo.data(), up.data(), tile.data(), rank);
+  }
+
   int64_t lower(int d) const { return lo_[d]; }
   int64_t upper(int d) const { return up_[d]; }
-  const ExecSpace& space() const { return space_; }
+  int64_t tile(int d) const { return tile_[d]; }
+  const execution_space& space() const { return space_; }
 
  private:
-  void set(std::initializer_list<int64_t> lo, std::initializer_list<int64_t> up) {
-    if ((int)lo.size() != rank || (int)up.size() != rank) throw std::runtime_error("MDRangePolicy: wrong rank");
-    int d = 0;
-    for (auto v : lo) lo_[d++] = v;
-    d = 0;
-    for (auto v : up) up_[d++] = v;
-    for (d = 0; d < rank; ++d)
-      if (up_[d] < lo_[d]) throw std::runtime_error("MDRangePolicy bounds error");
+  template <class LT, class UT, class TT>
+  void set(const LT* lo, const UT* up, const TT* tile, size_t nt) {
+    int64_t prod = 1;
+    for (int d = 0; d < rank; ++d) {
+      lo_[d] = (int64_t)lo[d];
+      up_[d] = (int64_t)up[d];
+      if (up_[d] < lo_[d])
+        throw std::runtime_error("Kokkos::MDRangePolicy bounds error: The lower bound is greater than its upper bound");
+      tile_[d] = tile && (size_t)d < nt ? (int64_t)tile[d] : 0;
+      prod *= tile_[d] > 0 ? tile_[d] : 1;
+    }
+    if (prod > 1024)
+      throw std::runtime_error(
+          "ExecSpace Error: MDRange tile dims exceed maximum number of threads per block - choose smaller tile dims");
   }
-  ExecSpace space_{};
-  int64_t lo_[4] = {0, 0, 0, 0}, up_[4] = {0, 0, 0, 0};
+  execution_space space_{};
+  int64_t lo_[6] = {0, 0, 0, 0, 0, 0}, up_[6] = {0, 0, 0, 0, 0, 0}, tile_[6] = {0, 0, 0, 0, 0, 0};
 };
+
+// deduction guides (KokkosExp_MDRangePolicy.hpp:429-458)
+template <class LT, size_t N, class UT>
+MDRangePolicy(const LT (&)[N], const UT (&)[N]) -> MDRangePolicy<Rank<N>>;
+template <class LT, size_t N, class UT, class TT, size_t TN>
+MDRangePolicy(const LT (&)[N], const UT (&)[N], const TT (&)[TN]) -> MDRangePolicy<Rank<N>>;
+template <class LT, size_t N, class UT>
+MDRangePolicy(const Experimental::GB300&, const LT (&)[N], const UT (&)[N]) -> MDRangePolicy<Rank<N>>;
+template <class LT, size_t N, class UT, class TT, size_t TN>
+MDRangePolicy(const Experimental::GB300&, const LT (&)[N], const UT (&)[N], const TT (&)[TN]) -> MDRangePolicy<Rank<N>>;
 
 // Kokkos::pair (core/src/Kokkos_Pair.hpp): a host-device pair.
 template <class T1, class T2>

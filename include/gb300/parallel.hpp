@@ -94,11 +94,20 @@ __device__ inline void cta_share(int64_t n, int64_t* c0, int64_t* c1) {
 }
 
 // ---- RangePolicy ------------------------------------------------------------
+// Each thread takes kUnroll indices per step (kBlock apart), so that many
+// independent loads of the functor are in flight per thread although the
+// functor folds into one value.
+constexpr int kUnroll = 4;
 template <class F>
 __global__ void __launch_bounds__(kBlock) k_range_for(F f, int64_t b, int64_t n) {
   int64_t c0, c1;
   cta_share(n, &c0, &c1);
-  for (int64_t i = c0 + threadIdx.x; i < c1; i += kBlock) f(b + i);
+  int64_t i = c0 + threadIdx.x;
+  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) f(b + i + u * kBlock);
+  }
+  for (; i < c1; i += kBlock) f(b + i);
 }
 
 template <class F, class Red, class V>
@@ -108,44 +117,101 @@ __global__ void __launch_bounds__(kBlock)
   red.init(v);
   int64_t c0, c1;
   cta_share(n, &c0, &c1);
-  for (int64_t i = c0 + threadIdx.x; i < c1; i += kBlock) f(b + i, v);
+  int64_t i = c0 + threadIdx.x;
+  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) f(b + i + u * kBlock, v);
+  }
+  for (; i < c1; i += kBlock) f(b + i, v);
   grid_finish_obj(red, v, partials, counter, out);
 }
 
-// ---- MDRangePolicy (index 0 fastest: the GPU default Iterate::Left) -----------
+// ---- MDRangePolicy -------------------------------------------------------------
+// The box is walked as one flat index space; walk dimension 0 (the policy's
+// inner direction: dimension 0 for Iterate::Left, the last for Right) varies
+// fastest between consecutive threads.
 struct MDArgs {
-  int64_t lo[4], ext[4];
+  int64_t lo[6], ext[6];
+  int dim[6];  // walk order -> policy dimension
   int rank;
+  bool fits32;
 };
-template <int R, class F, class... A>
-__device__ __forceinline__ void md_call(const F& f, const MDArgs& m, int64_t flat, A&... a) {
-  int64_t i[4];
-  int64_t r = flat;
-#pragma unroll
-  for (int d = 0; d < R; ++d) {
-    const int64_t e = m.ext[d];
-    i[d] = m.lo[d] + (d == R - 1 ? r : r % e);
-    r = (d == R - 1) ? 0 : r / e;
-  }
-  if constexpr (R == 2) f(i[0], i[1], a...);
-  else if constexpr (R == 3) f(i[0], i[1], i[2], a...);
-  else f(i[0], i[1], i[2], i[3], a...);
+template <class Tag, class F, class... A>
+__device__ __forceinline__ void tag_call(const F& f, A&&... a) {
+  if constexpr (std::is_void<Tag>::value) f(static_cast<A&&>(a)...);
+  else f(Tag(), static_cast<A&&>(a)...);
 }
-template <int R, class F>
+template <int R, class Tag, class F, class... A>
+__device__ __forceinline__ void md_call(const F& f, const MDArgs& m, int64_t flat, A&... a) {
+  int64_t i[6];
+  if (m.fits32) {
+    uint32_t r = (uint32_t)flat;
+#pragma unroll
+    for (int d = 0; d < R - 1; ++d) {
+      const uint32_t e = (uint32_t)m.ext[d];
+      i[m.dim[d]] = m.lo[m.dim[d]] + (int64_t)(r % e);
+      r /= e;
+    }
+    i[m.dim[R - 1]] = m.lo[m.dim[R - 1]] + (int64_t)r;
+  } else {
+    int64_t r = flat;
+#pragma unroll
+    for (int d = 0; d < R - 1; ++d) {
+      const int64_t e = m.ext[d];
+      i[m.dim[d]] = m.lo[m.dim[d]] + r % e;
+      r /= e;
+    }
+    i[m.dim[R - 1]] = m.lo[m.dim[R - 1]] + r;
+  }
+  if constexpr (R == 2) tag_call<Tag>(f, i[0], i[1], a...);
+  else if constexpr (R == 3) tag_call<Tag>(f, i[0], i[1], i[2], a...);
+  else if constexpr (R == 4) tag_call<Tag>(f, i[0], i[1], i[2], i[3], a...);
+  else if constexpr (R == 5) tag_call<Tag>(f, i[0], i[1], i[2], i[3], i[4], a...);
+  else tag_call<Tag>(f, i[0], i[1], i[2], i[3], i[4], i[5], a...);
+}
+template <int R, class Tag, class F>
 __global__ void __launch_bounds__(kBlock) k_md_for(F f, MDArgs m, int64_t n) {
   int64_t c0, c1;
   cta_share(n, &c0, &c1);
-  for (int64_t i = c0 + threadIdx.x; i < c1; i += kBlock) md_call<R>(f, m, i);
+  int64_t i = c0 + threadIdx.x;
+  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) md_call<R, Tag>(f, m, i + u * kBlock);
+  }
+  for (; i < c1; i += kBlock) md_call<R, Tag>(f, m, i);
 }
-template <int R, class F, class Red, class V>
+template <int R, class Tag, class F, class Red, class V>
 __global__ void __launch_bounds__(kBlock)
     k_md_reduce(F f, Red red, MDArgs m, int64_t n, V* partials, unsigned* counter, V* out) {
   V v;
   red.init(v);
   int64_t c0, c1;
   cta_share(n, &c0, &c1);
-  for (int64_t i = c0 + threadIdx.x; i < c1; i += kBlock) md_call<R>(f, m, i, v);
+  int64_t i = c0 + threadIdx.x;
+  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) md_call<R, Tag>(f, m, i + u * kBlock, v);
+  }
+  for (; i < c1; i += kBlock) md_call<R, Tag>(f, m, i, v);
   grid_finish_obj(red, v, partials, counter, out);
+}
+template <class P>
+MDArgs md_args(const P& p, int64_t* total) {
+  constexpr int R = P::rank;
+  const bool left = P::inner_direction == Iterate::Left;
+  MDArgs m{};
+  int64_t n = 1;
+  for (int d = 0; d < R; ++d) {
+    const int pd = left ? d : R - 1 - d;
+    m.dim[d] = pd;
+    m.lo[pd] = p.lower(pd);
+    m.ext[d] = p.upper(pd) - p.lower(pd);
+    n *= m.ext[d];
+  }
+  m.rank = R;
+  m.fits32 = n < (int64_t(1) << 31);
+  *total = n;
+  return m;
 }
 
 // ---- TeamPolicy: one CTA per team, league ranks strided over the grid ----------
@@ -212,20 +278,15 @@ template <class F>
 void parallel_for(int64_t n, const F& f) {
   parallel_for(RangePolicy<>(0, n), f);
 }
-template <class RankT, class E, class F>
-void parallel_for(const MDRangePolicy<RankT, E>& p, const F& f) {
+template <class... PP, class F>
+void parallel_for(const MDRangePolicy<PP...>& p, const F& f) {
+  using P = MDRangePolicy<PP...>;
   Tools::Impl::Region<F> tool_region(Tools::Impl::kFor, p.space().stream());
-  constexpr int R = RankT::rank;
-  Impl::MDArgs m{};
-  int64_t n = 1;
-  for (int d = 0; d < R; ++d) {
-    m.lo[d] = p.lower(d);
-    m.ext[d] = p.upper(d) - p.lower(d);
-    n *= m.ext[d];
-  }
-  m.rank = R;
+  int64_t n = 0;
+  const Impl::MDArgs m = Impl::md_args(p, &n);
   if (n <= 0) return;
-  Impl::k_md_for<R><<<(unsigned)Impl::grid_for(n), Impl::kBlock, 0, p.space().stream()>>>(f, m, n);
+  Impl::k_md_for<P::rank, typename P::work_tag>
+      <<<(unsigned)Impl::grid_for(n), Impl::kBlock, 0, p.space().stream()>>>(f, m, n);
   Impl::launched(cudaGetLastError(), "parallel_for(MDRange)");
 }
 template <class E, class... R, class F>
@@ -259,23 +320,17 @@ void parallel_reduce(const RangePolicy<E, R...>& p, const F& f, const Red& red) 
     return cudaGetLastError();
   });
 }
-template <class RankT, class E, class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
-void parallel_reduce(const MDRangePolicy<RankT, E>& p, const F& f, const Red& red) {
+template <class... PP, class F, class Red, std::enable_if_t<Impl::is_reducer<Red>::value, bool> = true>
+void parallel_reduce(const MDRangePolicy<PP...>& p, const F& f, const Red& red) {
+  using P = MDRangePolicy<PP...>;
   Tools::Impl::Region<F> tool_region(Tools::Impl::kReduce, p.space().stream());
   using V = typename Red::value_type;
-  constexpr int R = RankT::rank;
-  Impl::MDArgs m{};
-  int64_t n = 1;
-  for (int d = 0; d < R; ++d) {
-    m.lo[d] = p.lower(d);
-    m.ext[d] = p.upper(d) - p.lower(d);
-    n *= m.ext[d];
-  }
-  m.rank = R;
+  int64_t n = 0;
+  const Impl::MDArgs m = Impl::md_args(p, &n);
   const int64_t g = Impl::grid_for(n);
   cudaStream_t s = p.space().stream();
   Impl::run_reduce(s, g, red, [&](V* part, unsigned* ctr, V* out) {
-    Impl::k_md_reduce<R><<<(unsigned)g, Impl::kBlock, 0, s>>>(f, red, m, n, part, ctr, out);
+    Impl::k_md_reduce<P::rank, typename P::work_tag><<<(unsigned)g, Impl::kBlock, 0, s>>>(f, red, m, n, part, ctr, out);
     return cudaGetLastError();
   });
 }
@@ -298,7 +353,7 @@ void parallel_reduce(const TeamPolicy<E, R...>& p, const F& f, const Red& red) {
 namespace Impl {
 template <class P> struct is_policy : std::false_type {};
 template <class E, class... R> struct is_policy<RangePolicy<E, R...>> : std::true_type {};
-template <class K, class E> struct is_policy<MDRangePolicy<K, E>> : std::true_type {};
+template <class... PP> struct is_policy<MDRangePolicy<PP...>> : std::true_type {};
 template <class E, class... R> struct is_policy<TeamPolicy<E, R...>> : std::true_type {};
 }  // namespace Impl
 
@@ -387,6 +442,12 @@ struct CombinedFunctor {
   __device__ void operator()(int64_t i, int64_t j, int64_t k, VP& v) const { f(i, j, k, PackGet<Is>::get(v)...); }
   __device__ void operator()(int64_t i, int64_t j, int64_t k, int64_t l, VP& v) const {
     f(i, j, k, l, PackGet<Is>::get(v)...);
+  }
+  __device__ void operator()(int64_t i, int64_t j, int64_t k, int64_t l, int64_t m, VP& v) const {
+    f(i, j, k, l, m, PackGet<Is>::get(v)...);
+  }
+  __device__ void operator()(int64_t i, int64_t j, int64_t k, int64_t l, int64_t m, int64_t q, VP& v) const {
+    f(i, j, k, l, m, q, PackGet<Is>::get(v)...);
   }
   __device__ void operator()(const TeamMember& m, VP& v) const { f(m, PackGet<Is>::get(v)...); }
 };

@@ -27,6 +27,9 @@ HOSTLIB = os.path.join(HERE, "libgbk_host.so")
 # thrust comparator for the sort benchmarks (not part of libgbk.so)
 CMP_SRC = os.path.join(HERE, "comparators", "thrust_sort.cu")
 CMP_LIB = os.path.join(HERE, "comparators", "libgbk_thrust.so")
+# throughput of the header-template path for user functors (run by bench.py)
+HP_SRC = os.path.join(HERE, "bench_header_path.cu")
+HP_BIN = os.path.join(OBJ, "bench_header_path")
 
 
 def nvcc():
@@ -76,6 +79,10 @@ def build(verbose=False, jobs=None):
                 print(out)
     if todo or _stale(LIB, objs):
         _run([nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB] + objs)
+    hp_deps = [HP_SRC, LIB] + glob.glob(os.path.join(ROOT, "include", "gb300", "*.hpp")) + hdrs
+    if _stale(HP_BIN, hp_deps):
+        _run([nvcc()] + ARCH + ["-O3", "-std=c++17", "--extended-lambda", "-I" + os.path.join(ROOT, "include"), HP_SRC,
+                                "-L" + HERE, "-lgbk", "-Xlinker", "-rpath", "-Xlinker", HERE, "-o", HP_BIN])
     src = os.path.join(CSRC, "gbk_datagen.c")
     if _stale(HOSTLIB, [src]):
         _run(["gcc", "-O3", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-Wall", src, "-o", HOSTLIB, "-lm"])

@@ -464,6 +464,37 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity
   return false;
 }
 
+// Programmatic dependent launch.  A kernel launched with launch_pdl may start
+// while the previous kernel of its stream is still finishing: it lets the
+// next kernel be scheduled at once (pdl_release), then waits for its
+// predecessor's completion and memory (pdl_acquire) before its first global
+// memory access, so stream order holds for every buffer it touches.  What it
+// gains is the launch and CTA ramp of back-to-back kernels.
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_acquire() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_entry() {
+  pdl_release();
+  pdl_acquire();
+}
+
+// PDL is on unless the environment sets GBK_PDL=0.
+bool pdl_enabled();
+
+template <class... KArgs, class... Args>
+cudaError_t launch_pdl(void (*kfn)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kfn, static_cast<Args&&>(args)...);
+}
+
 }  // namespace gbk
 
 #define GBK_CUDA_TRY(expr)                      \

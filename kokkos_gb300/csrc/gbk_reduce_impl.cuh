@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(BLOCK)
   __shared__ V sm[BLOCK / 32];
   V acc = R::init();
   const int64_t gtid = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  pdl_entry();
   // Unaligned head [0, head): one element per thread.
   if (gtid < head) R::template update<true>(acc, x[gtid], loc0 + gtid);
   const T* xb = x + head;
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(BLOCK)
   __shared__ V sm[BLOCK / 32];
   V acc = R::init();
   const int64_t gtid = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  pdl_entry();
   if (gtid < head) R::template update<true>(acc, x[gtid], loc0 + gtid);
   const T* xb = x + head;
   const int64_t nvec = (n - head) / VEC;
@@ -266,10 +268,10 @@ int launch_flat(const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, in
   int st = GBK_OK;
   char* scr = ws_scratch(w, sizeof(V) * (size_t)grid + 256, &st);
   if (!scr) return st;
-  k_reduce_flat<R, T, BLOCK, UNROLL><<<(unsigned)grid, BLOCK, 0, s>>>(x, n, head, loc0, (V*)scr,
-                                                                       w->counters + SLOT_REDUCE, (V*)out);
+  GBK_CUDA_TRY(launch_pdl(k_reduce_flat<R, T, BLOCK, UNROLL>, dim3((unsigned)grid), dim3(BLOCK), 0, s, x, n, head,
+                          loc0, (V*)scr, w->counters + SLOT_REDUCE, (V*)out));
   note_launch();
-  return cuda_status(cudaGetLastError());
+  return GBK_OK;
 }
 
 // Ring reduce: 256 threads, chunks of 1024 vectors (16 KiB), 4 stages: three
@@ -303,10 +305,10 @@ int launch_tma(const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, int
   int st = GBK_OK;
   char* scr = ws_scratch(w, sizeof(V) * (size_t)grid + 256, &st);
   if (!scr) return st;
-  kfn<<<(unsigned)grid, BLOCK, dyn, s>>>(x, n, head, loc0, (V*)scr, w->counters + SLOT_REDUCE, (V*)out, w->err,
-                                        wait_limit());
+  GBK_CUDA_TRY(launch_pdl(kfn, dim3((unsigned)grid), dim3(BLOCK), dyn, s, x, n, head, loc0, (V*)scr,
+                          w->counters + SLOT_REDUCE, (V*)out, w->err, wait_limit()));
   note_launch();
-  return cuda_status(cudaGetLastError());
+  return GBK_OK;
 }
 
 // variant 1: the load-pipelined kernel (block, items_per_thread, ctas_per_sm

@@ -9,6 +9,7 @@
 
 #include <cstring>
 #include <map>
+#include <cstdlib>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -52,6 +53,14 @@ int sm_count() {
 }
 
 int64_t wait_limit() { return g_wait_limit.load(); }
+
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBK_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 void note_launch(int64_t k) { g_launches += k; }
 
 Workspace* ws_get(cudaStream_t s, int* status) {

@@ -121,7 +121,15 @@ __global__ void __launch_bounds__(BLOCK)
 // Overflow is therefore impossible and no carry ever reaches the
 // neighbouring bin.  Keys for the next round are loaded before the current
 // round is counted, so two rounds of loads are in flight.
-template <int BLOCK, bool AGG>
+//
+// NODRAIN: no periodic drains.  Each increment reads the counter's old value
+// (the shared atomic returns it); the one increment that takes a 16-bit
+// counter from 0x7FFF to 0x8000 moves 0x8000 to the global bin itself (a
+// shared atomic subtract and a global red.add).  Until that subtract lands,
+// other increments can raise the counter by less than the 0x7FFF headroom
+// left (far fewer increments are in flight in one CTA), so no carry reaches
+// the neighbouring bin.
+template <int BLOCK, bool AGG, bool NODRAIN>
 __global__ void __launch_bounds__(BLOCK, 1)
     k_hist16(const int32_t* __restrict__ keys, int64_t nvec, int64_t nbins, unsigned long long* bins, int* err) {
   extern __shared__ __align__(16) unsigned sh[];
@@ -131,6 +139,7 @@ __global__ void __launch_bounds__(BLOCK, 1)
   static_assert(DRAIN >= 1, "round too large for 16-bit counters");
   const int nwords = (int)((nbins + 1) >> 1);
   for (int i = threadIdx.x; i <= nwords; i += BLOCK) sh[i] = 0u;  // the counters and the spare word
+  pdl_entry();
   __syncthreads();
   bool bad = false;
   // Contiguous, balanced share of the vectors for this CTA.
@@ -158,7 +167,11 @@ __global__ void __launch_bounds__(BLOCK, 1)
       bad = bad || !ok;
       const unsigned hi = uk >= nw32 ? 1u : 0u;
       const unsigned word = ok ? uk - (hi ? nw32 : 0u) : nw32;
-      atomicAdd(sh + word, 1u << (hi << 4));
+      const unsigned old = atomicAdd(sh + word, 1u << (hi << 4));
+      if (NODRAIN && ok && ((old >> (hi << 4)) & 0xFFFFu) == 0x7FFFu) {
+        atomicSub(sh + word, 0x8000u << (hi << 4));
+        red_add_u64(bins + (hi ? nw32 + word : word), 0x8000ull);
+      }
     }
   };
   auto drain_word = [&](int i, unsigned w) {
@@ -213,129 +226,13 @@ __global__ void __launch_bounds__(BLOCK, 1)
 #pragma unroll
     for (int j = 0; j < VPT; ++j) cur[j] = nxt[j];
     v = vn;
-    if (++since == DRAIN) {
+    if (!NODRAIN && ++since == DRAIN) {
       since = 0;
       drain();
     }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nwords; i += BLOCK) {
-    const unsigned w = sh[i];
-    if (w & 0xFFFFu) red_add_u64(bins + i, (unsigned long long)(w & 0xFFFFu));
-    if ((w >> 16) && nwords + i < nbins) red_add_u64(bins + nwords + i, (unsigned long long)(w >> 16));
-  }
-  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, GBK_EBIT_KEY_RANGE);
-}
-
-// The same 16-bit pairing and drains with fewer instructions per key: each
-// 16-byte vector of four keys is range-checked at once (unsigned max below
-// nbins; only a vector holding an out-of-range key takes the per-key path,
-// which skips such keys), a power-of-two word count turns the word index into
-// a mask and the increment into one multiply-add (1 or 1 << 16), every thread
-// takes four vectors (16 keys) per round with the next round's loads issued
-// before the current round is counted (two register sets, no copies), and
-// in-CTA indices are 32-bit.  A drain follows every 32,768 keys of the CTA,
-// as in k_hist16.
-template <int BLOCK, bool POW2>
-__global__ void __launch_bounds__(BLOCK, 1)
-    k_hist16b(const int32_t* __restrict__ keys, int64_t nvec, unsigned nbins, unsigned nwords, int lw,
-              unsigned long long* bins, int* err) {
-  extern __shared__ __align__(16) unsigned sh[];
-  constexpr int VPT = 4;
-  constexpr int ROUND = BLOCK * VPT;           // vectors per round
-  constexpr int DRAIN = 32768 / (ROUND * 4);   // rounds between drains
-  static_assert(DRAIN >= 1, "round too large for 16-bit counters");
-  for (unsigned i = threadIdx.x; i < nwords; i += BLOCK) sh[i] = 0u;
-  __syncthreads();
-  bool bad = false;
-  const int64_t per = nvec / gridDim.x, rem = nvec % gridDim.x;
-  const int64_t v0 = blockIdx.x * per + (blockIdx.x < rem ? blockIdx.x : rem);
-  const unsigned nv = (unsigned)(per + (blockIdx.x < rem ? 1 : 0));
-  const int32_t* kb = keys + 4 * v0;
-  const unsigned mask = nwords - 1u;
-  auto add_key = [&](unsigned k) {
-    unsigned word, inc;
-    if (POW2) {
-      word = k & mask;
-      inc = 1u + (k >> lw) * 0xFFFFu;
-    } else {
-      const bool hi = k >= nwords;
-      word = hi ? k - nwords : k;
-      inc = hi ? 0x10000u : 1u;
-    }
-    atomicAdd(sh + word, inc);
-  };
-  auto count_vec = [&](const Vec16<int32_t>& q) {
-    const unsigned a = (unsigned)q.v[0], b = (unsigned)q.v[1], c = (unsigned)q.v[2], d = (unsigned)q.v[3];
-    if (max(max(a, b), max(c, d)) < nbins) {
-      add_key(a);
-      add_key(b);
-      add_key(c);
-      add_key(d);
-    } else {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const unsigned k = (unsigned)q.v[e];
-        if (k < nbins) add_key(k);
-        else bad = true;
-      }
-    }
-  };
-  auto drain_word = [&](unsigned i, unsigned w) {
-    const unsigned hi = w & 0x80008000u;
-    if (hi) {
-      sh[i] = w - hi;
-      if (hi & 0x8000u) red_add_u64(bins + i, 0x8000ull);
-      if (hi & 0x80000000u) red_add_u64(bins + nwords + i, 0x8000ull);
-    }
-  };
-  auto drain = [&]() {
-    __syncthreads();
-    const unsigned nq = nwords >> 2;
-    const uint4* sq = reinterpret_cast<const uint4*>(sh);
-    for (unsigned i = threadIdx.x; i < nq; i += BLOCK) {
-      const uint4 w = sq[i];
-      if ((w.x | w.y | w.z | w.w) & 0x80008000u) {
-        drain_word(4 * i, w.x);
-        drain_word(4 * i + 1, w.y);
-        drain_word(4 * i + 2, w.z);
-        drain_word(4 * i + 3, w.w);
-      }
-    }
-    for (unsigned i = 4 * nq + threadIdx.x; i < nwords; i += BLOCK) drain_word(i, sh[i]);
-    __syncthreads();
-  };
-  const Vec16<int32_t> none = {make_uint4(0u, 0u, 0u, 0u)};
-  auto load = [&](Vec16<int32_t> (&r)[VPT], unsigned round) {
-#pragma unroll
-    for (int j = 0; j < VPT; ++j) {
-      const unsigned q = round * ROUND + j * BLOCK + threadIdx.x;
-      r[j] = none;
-      if (q < nv) r[j].u = ld_stream16(kb + 4 * (size_t)q);
-    }
-  };
-  auto count_round = [&](const Vec16<int32_t> (&r)[VPT], unsigned round) {
-    const bool full = (round + 1) * ROUND <= nv;
-#pragma unroll
-    for (int j = 0; j < VPT; ++j) {
-      if (full || round * ROUND + j * BLOCK + threadIdx.x < nv) count_vec(r[j]);
-    }
-  };
-  const unsigned rounds = (nv + ROUND - 1) / ROUND;
-  Vec16<int32_t> ra[VPT], rb[VPT];
-  load(ra, 0);
-  unsigned since = 0;
-  for (unsigned r = 0; r < rounds; r += 2) {
-    load(rb, r + 1);
-    count_round(ra, r);
-    if (++since == DRAIN) { since = 0; drain(); }
-    if (r + 1 >= rounds) break;
-    load(ra, r + 2);
-    count_round(rb, r + 1);
-    if (++since == DRAIN) { since = 0; drain(); }
-  }
-  __syncthreads();
-  for (unsigned i = threadIdx.x; i < nwords; i += BLOCK) {
     const unsigned w = sh[i];
     if (w & 0xFFFFu) red_add_u64(bins + i, (unsigned long long)(w & 0xFFFFu));
     if ((w >> 16) && nwords + i < nbins) red_add_u64(bins + nwords + i, (unsigned long long)(w >> 16));
@@ -356,41 +253,11 @@ __global__ void k_hist_edges(const int32_t* __restrict__ keys, int64_t head, int
   else atomicOr(err, GBK_EBIT_KEY_RANGE);
 }
 
-int launch_hist16b(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, Workspace* w) {
-  constexpr int BLOCK = 1024;
-  const unsigned nwords = (unsigned)((nbins + 1) >> 1);
-  const bool pow2 = (nbins & (nbins - 1)) == 0 && nbins >= 2;
-  int lw = 0;
-  while ((1u << lw) < nwords) ++lw;
-  const size_t smem = (size_t)nwords * 4;
-  auto kfn = pow2 ? k_hist16b<BLOCK, true> : k_hist16b<BLOCK, false>;
-  GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const uintptr_t a = (uintptr_t)keys;
-  int64_t head = (int64_t)(((16 - (a & 15)) & 15) / 4);
-  if (head > n) head = n;
-  const int64_t nvec = (n - head) / 4;
-  const int64_t tail0 = head + nvec * 4;
-  if (head || tail0 < n) {
-    k_hist_edges<<<1, 32, 0, w->stream>>>(keys, head, tail0, n, nbins, (unsigned long long*)bins, w->err);
-    note_launch();
-  }
-  if (nvec > 0) {
-    int64_t grid = sm_count();
-    const int64_t need = (nvec + BLOCK * 4 - 1) / (BLOCK * 4);
-    if (grid > need) grid = need;
-    while (nvec / grid >= (int64_t(1) << 30)) grid += sm_count();  // in-CTA vector indices stay 32-bit
-    kfn<<<(unsigned)grid, BLOCK, smem, w->stream>>>(keys + head, nvec, (unsigned)nbins, nwords, lw,
-                                                    (unsigned long long*)bins, w->err);
-    note_launch();
-  }
-  return cuda_status(cudaGetLastError());
-}
-
-template <bool AGG>
+template <bool AGG, bool NODRAIN>
 int launch_hist16(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, Workspace* w) {
   constexpr int BLOCK = 1024;
   const size_t smem = (size_t)((nbins + 1) >> 1) * 4 + 16;  // counters, then the spare word for keys outside the bins
-  auto kfn = k_hist16<BLOCK, AGG>;
+  auto kfn = k_hist16<BLOCK, AGG, NODRAIN>;
   GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uintptr_t a = (uintptr_t)keys;
   int64_t head = (int64_t)(((16 - (a & 15)) & 15) / 4);
@@ -405,7 +272,8 @@ int launch_hist16(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, 
     int64_t grid = sm_count();
     const int64_t need = (nvec + BLOCK * 2 - 1) / (BLOCK * 2);
     if (grid > need) grid = need;
-    kfn<<<(unsigned)grid, BLOCK, smem, w->stream>>>(keys + head, nvec, nbins, (unsigned long long*)bins, w->err);
+    GBK_CUDA_TRY(launch_pdl(kfn, dim3((unsigned)grid), dim3(BLOCK), smem, w->stream, keys + head, nvec, nbins,
+                            (unsigned long long*)bins, w->err));
     note_launch();
   }
   return cuda_status(cudaGetLastError());
@@ -468,7 +336,7 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   if (n == 0) return GBK_OK;
   // variant bits: 0x0F cluster size of the 32-bit privatised kernel (1, 2,
   // 4, 8); 0x10 warp aggregation; 0x20 the 16-bit one-CTA-per-SM kernel;
-  // 0x40 no privatisation; 0x80 the 16-bit kernel's lean form (k_hist16b).
+  // 0x40 no privatisation; 0x80 the 16-bit kernel without drains.
   // 0 = automatic choice.
   const int var = t ? t->variant : 0;
   int cl = var & 0xF;
@@ -479,12 +347,12 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   const bool force_global = (var & 0x40) != 0;
   if (var == 0) {
     if (nbins * 4 <= 96 * 1024) cl = 1;
-    else if ((nbins + 1) / 2 * 4 <= max_smem) { use16 = true; agg = false; }
+    else if ((nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, true>(keys, n, nbins, bins, w);
     else { cl = 2; while (cl <= 8 && (nbins + cl - 1) / cl * 4 > max_smem) cl *= 2; }
   }
-  if ((var & 0x80) && (nbins + 1) / 2 * 4 <= max_smem) return launch_hist16b(keys, n, nbins, bins, w);
+  if ((var & 0x80) && (nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, true>(keys, n, nbins, bins, w);
   if (use16 && !force_global && (nbins + 1) / 2 * 4 <= max_smem) {
-    return agg ? launch_hist16<true>(keys, n, nbins, bins, w) : launch_hist16<false>(keys, n, nbins, bins, w);
+    return agg ? launch_hist16<true, false>(keys, n, nbins, bins, w) : launch_hist16<false, false>(keys, n, nbins, bins, w);
   }
   if (cl == 0) cl = 1;
   if (force_global || (nbins + cl - 1) / cl * 4 > max_smem || cl > 8) {

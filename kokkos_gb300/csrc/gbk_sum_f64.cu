@@ -34,6 +34,7 @@ __global__ void __launch_bounds__(BLOCK)
   FixAcc a;
   fix_init(a);
   const int64_t gtid = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  pdl_entry();
   if (gtid < head) fa += x[gtid];  // unaligned head: one element per thread
   const double* xb = x + head;
   const int64_t nvec = (n - head) / 2;
@@ -109,9 +110,10 @@ int launch_split(const double* x, int64_t n, double* out, Workspace* w, int ctas
   int st = GBK_OK;
   char* scr = ws_scratch(w, sizeof(double) * (size_t)grid + 256, &st);
   if (!scr) return st;
-  kfn<<<(unsigned)grid, BLOCK, 0, w->stream>>>(x, n, head, (double*)scr, w->counters + SLOT_REDUCE, out);
+  GBK_CUDA_TRY(launch_pdl(kfn, dim3((unsigned)grid), dim3(BLOCK), 0, w->stream, x, n, head, (double*)scr,
+                          w->counters + SLOT_REDUCE, out));
   note_launch();
-  return cuda_status(cudaGetLastError());
+  return GBK_OK;
 }
 
 }  // namespace

@@ -214,6 +214,12 @@ static void test_range_reducers() {
   report(std::fabs(hres[0] - cs) <= 1e-12 * a, "range_sum_into_view");
 }
 
+// a tagged MDRange functor (kernel template arguments may not be local types)
+struct TagSq {};
+struct Sq {
+  KOKKOS_INLINE_FUNCTION void operator()(TagSq, int64_t i, int64_t j, int64_t& u) const { u += i * j; }
+};
+
 static void test_mdrange() {
   // TestMDRangeReduce.hpp-style: LayoutLeft View<float***>, loc = i + n0*(j + n1*k)
   const int64_t n0 = 96, n1 = 80, n2 = 33;
@@ -273,6 +279,78 @@ static void test_mdrange() {
     for (int64_t j = 2; j < n1; ++j)
       for (int64_t i = 1; i < n0; ++i) hs += h[i + n0 * (j + n1 * k)];
   report(std::fabs(s - hs) <= 1e-9 * std::fabs(hs) + 1e-9, "mdrange_subbox_sum");
+  // the reference's tile-list constructor with Iterate::Right on a LayoutRight
+  // view, and the deduction guide of a braced-list policy
+  // (KokkosExp_MDRangePolicy.hpp:283-307, 429-458)
+  {
+    Kokkos::View<int32_t***, Kokkos::LayoutRight> z("z", 33, 17, 65);
+    Kokkos::parallel_for(
+        Kokkos::MDRangePolicy<Kokkos::Rank<3, Kokkos::Iterate::Right, Kokkos::Iterate::Right>>({0, 0, 0}, {33, 17, 65},
+                                                                                            {2, 4, 32}),
+        KOKKOS_LAMBDA(int64_t i, int64_t j, int64_t k) { z(i, j, k) = (int32_t)(i * 10000 + j * 100 + k); });
+    int64_t zs = 0;
+    Kokkos::parallel_reduce(Kokkos::MDRangePolicy({0, 0, 0}, {33, 17, 65}),
+                            KOKKOS_LAMBDA(int64_t i, int64_t j, int64_t k, int64_t& u) { u += z(i, j, k); }, zs);
+    int64_t hz = 0;
+    for (int64_t i = 0; i < 33; ++i)
+      for (int64_t j = 0; j < 17; ++j)
+        for (int64_t k = 0; k < 65; ++k) hz += i * 10000 + j * 100 + k;
+    report(zs == hz, "mdrange_tiles_iterate_right_ctad");
+    bool threw = false;
+    try {
+      Kokkos::MDRangePolicy<Kokkos::Rank<3>> bad({0, 0, 0}, {8, 8, 8}, {16, 16, 16});  // 4096 threads in a tile
+    } catch (const std::runtime_error&) {
+      threw = true;
+    }
+    report(threw, "mdrange_tile_too_large_rejected");
+  }
+  // ranks 5 and 6 (the reference's maximum, KokkosExp_MDRangePolicy.hpp:196)
+  {
+    Kokkos::View<int32_t*****> a5("a5", 3, 4, 5, 6, 7);
+    Kokkos::parallel_for(Kokkos::MDRangePolicy<Kokkos::Rank<5>>({0, 0, 0, 0, 0}, {3, 4, 5, 6, 7}),
+                         KOKKOS_LAMBDA(int64_t a, int64_t b, int64_t c, int64_t d, int64_t e) {
+                           a5(a, b, c, d, e) = (int32_t)(a + 3 * b + 5 * c + 7 * d + 11 * e);
+                         });
+    Kokkos::View<double******, Kokkos::LayoutRight> a6("a6", 2, 3, 4, 3, 2, 5);
+    Kokkos::parallel_for(
+        Kokkos::MDRangePolicy<Kokkos::Rank<6, Kokkos::Iterate::Right, Kokkos::Iterate::Right>>({0, 0, 0, 0, 0, 0},
+                                                                                            {2, 3, 4, 3, 2, 5}),
+        KOKKOS_LAMBDA(int64_t a, int64_t b, int64_t c, int64_t d, int64_t e, int64_t f) {
+          a6(a, b, c, d, e, f) = (double)(a + b * 2 + c * 4 + d * 8 + e * 16 + f * 32);
+        });
+    int64_t s5 = 0;
+    double s6 = 0;
+    Kokkos::parallel_reduce(Kokkos::MDRangePolicy<Kokkos::Rank<5>>({1, 0, 2, 0, 3}, {3, 4, 5, 6, 7}),
+                            KOKKOS_LAMBDA(int64_t a, int64_t b, int64_t c, int64_t d, int64_t e, int64_t& u) {
+                              u += a5(a, b, c, d, e);
+                            },
+                            s5);
+    Kokkos::parallel_reduce(Kokkos::MDRangePolicy<Kokkos::Rank<6>>({0, 0, 0, 0, 0, 0}, {2, 3, 4, 3, 2, 5}),
+                            KOKKOS_LAMBDA(int64_t a, int64_t b, int64_t c, int64_t d, int64_t e, int64_t f, double& u) {
+                              u += a6(a, b, c, d, e, f);
+                            },
+                            s6);
+    int64_t h5 = 0;
+    for (int64_t a = 1; a < 3; ++a)
+      for (int64_t b = 0; b < 4; ++b)
+        for (int64_t c = 2; c < 5; ++c)
+          for (int64_t d = 0; d < 6; ++d)
+            for (int64_t e = 3; e < 7; ++e) h5 += a + 3 * b + 5 * c + 7 * d + 11 * e;
+    double h6 = 0;
+    for (int64_t a = 0; a < 2; ++a)
+      for (int64_t b = 0; b < 3; ++b)
+        for (int64_t c = 0; c < 4; ++c)
+          for (int64_t d = 0; d < 3; ++d)
+            for (int64_t e = 0; e < 2; ++e)
+              for (int64_t f = 0; f < 5; ++f) h6 += (double)(a + b * 2 + c * 4 + d * 8 + e * 16 + f * 32);
+    report(s5 == h5 && s6 == h6, "mdrange_rank5_rank6");
+  }
+  // a work tag among the policy's properties
+  {
+    int64_t t = 0;
+    Kokkos::parallel_reduce(Kokkos::MDRangePolicy<Kokkos::Rank<2>, TagSq>({0, 0}, {100, 50}), Sq{}, t);
+    report(t == (int64_t)(99 * 100 / 2) * (49 * 50 / 2), "mdrange_work_tag");
+  }
 }
 
 static void test_team() {
