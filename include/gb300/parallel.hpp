@@ -127,89 +127,127 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 // ---- MDRangePolicy -------------------------------------------------------------
-// The box is walked as one flat index space; walk dimension 0 (the policy's
-// inner direction: dimension 0 for Iterate::Left, the last for Right) varies
-// fastest between consecutive threads.
+// The box is walked as one flat index space in which walk dimension 0 (the
+// policy's inner direction: dimension 0 for Iterate::Left, the last for
+// Right) varies fastest between consecutive threads, so a functor reading
+// x(i0, ...) of a matching layout reads coalesced.  Each thread turns its
+// first flat index into walk-order digits once (divisions) and then steps by
+// the CTA width with a mixed-radix add of the step's digits (an add, a
+// compare and a conditional subtract per dimension, no division per
+// element).  The digit-to-argument order is fixed at compile time (LEFT).
 struct MDArgs {
-  int64_t lo[6], ext[6];
-  int dim[6];  // walk order -> policy dimension
-  int rank;
-  bool fits32;
+  int64_t lo[6];    // lower bounds, policy order
+  int64_t ext[6];   // extents, walk order
+  int64_t step[6];  // kBlock in the mixed radix of ext (walk order)
+  bool fits32;      // every flat index below 2^31
 };
 template <class Tag, class F, class... A>
 __device__ __forceinline__ void tag_call(const F& f, A&&... a) {
   if constexpr (std::is_void<Tag>::value) f(static_cast<A&&>(a)...);
   else f(Tag(), static_cast<A&&>(a)...);
 }
-template <int R, class Tag, class F, class... A>
-__device__ __forceinline__ void md_call(const F& f, const MDArgs& m, int64_t flat, A&... a) {
-  int64_t i[6];
-  if (m.fits32) {
-    uint32_t r = (uint32_t)flat;
+template <int R, class IT>
+struct MDWalk {
+  IT d[R];  // walk-order digits of the current flat index
+  __device__ __forceinline__ void start(const MDArgs& m, int64_t flat) {
+    IT r = (IT)flat;
 #pragma unroll
-    for (int d = 0; d < R - 1; ++d) {
-      const uint32_t e = (uint32_t)m.ext[d];
-      i[m.dim[d]] = m.lo[m.dim[d]] + (int64_t)(r % e);
+    for (int k = 0; k < R - 1; ++k) {
+      const IT e = (IT)m.ext[k];
+      d[k] = r % e;
       r /= e;
     }
-    i[m.dim[R - 1]] = m.lo[m.dim[R - 1]] + (int64_t)r;
-  } else {
-    int64_t r = flat;
-#pragma unroll
-    for (int d = 0; d < R - 1; ++d) {
-      const int64_t e = m.ext[d];
-      i[m.dim[d]] = m.lo[m.dim[d]] + r % e;
-      r /= e;
-    }
-    i[m.dim[R - 1]] = m.lo[m.dim[R - 1]] + r;
+    d[R - 1] = r;
   }
-  if constexpr (R == 2) tag_call<Tag>(f, i[0], i[1], a...);
-  else if constexpr (R == 3) tag_call<Tag>(f, i[0], i[1], i[2], a...);
-  else if constexpr (R == 4) tag_call<Tag>(f, i[0], i[1], i[2], i[3], a...);
-  else if constexpr (R == 5) tag_call<Tag>(f, i[0], i[1], i[2], i[3], i[4], a...);
-  else tag_call<Tag>(f, i[0], i[1], i[2], i[3], i[4], i[5], a...);
+  __device__ __forceinline__ void advance(const MDArgs& m) {
+    IT carry = 0;
+#pragma unroll
+    for (int k = 0; k < R - 1; ++k) {
+      const IT v = d[k] + (IT)m.step[k] + carry;
+      const IT e = (IT)m.ext[k];
+      carry = v >= e ? IT(1) : IT(0);
+      d[k] = carry ? v - e : v;
+    }
+    d[R - 1] += (IT)m.step[R - 1] + carry;
+  }
+  // policy-order argument p from the walk digits
+  template <bool LEFT, int P>
+  __device__ __forceinline__ int64_t arg(const MDArgs& m) const {
+    return m.lo[P] + (int64_t)d[LEFT ? P : R - 1 - P];
+  }
+};
+template <int R, bool LEFT, class Tag, class IT, class F, class... A>
+__device__ __forceinline__ void md_call(const F& f, const MDArgs& m, const MDWalk<R, IT>& w, A&... a) {
+  if constexpr (R == 2) tag_call<Tag>(f, w.template arg<LEFT, 0>(m), w.template arg<LEFT, 1>(m), a...);
+  else if constexpr (R == 3)
+    tag_call<Tag>(f, w.template arg<LEFT, 0>(m), w.template arg<LEFT, 1>(m), w.template arg<LEFT, 2>(m), a...);
+  else if constexpr (R == 4)
+    tag_call<Tag>(f, w.template arg<LEFT, 0>(m), w.template arg<LEFT, 1>(m), w.template arg<LEFT, 2>(m),
+                  w.template arg<LEFT, 3>(m), a...);
+  else if constexpr (R == 5)
+    tag_call<Tag>(f, w.template arg<LEFT, 0>(m), w.template arg<LEFT, 1>(m), w.template arg<LEFT, 2>(m),
+                  w.template arg<LEFT, 3>(m), w.template arg<LEFT, 4>(m), a...);
+  else
+    tag_call<Tag>(f, w.template arg<LEFT, 0>(m), w.template arg<LEFT, 1>(m), w.template arg<LEFT, 2>(m),
+                  w.template arg<LEFT, 3>(m), w.template arg<LEFT, 4>(m), w.template arg<LEFT, 5>(m), a...);
 }
-template <int R, class Tag, class F>
+// Walk [c0, c1) of the flat space in steps of kBlock from c0 + threadIdx.x,
+// kUnroll steps per loop trip (their loads independent of one another).
+template <int R, bool LEFT, class Tag, class IT, class F, class... A>
+__device__ __forceinline__ void md_walk(const F& f, const MDArgs& m, int64_t c0, int64_t c1, A&... a) {
+  int64_t i = c0 + threadIdx.x;
+  if (i >= c1) return;
+  MDWalk<R, IT> w;
+  w.start(m, i);
+  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      md_call<R, LEFT, Tag>(f, m, w, a...);
+      w.advance(m);
+    }
+  }
+  for (; i < c1; i += kBlock) {
+    md_call<R, LEFT, Tag>(f, m, w, a...);
+    w.advance(m);
+  }
+}
+template <int R, bool LEFT, class Tag, class IT, class F>
 __global__ void __launch_bounds__(kBlock) k_md_for(F f, MDArgs m, int64_t n) {
   int64_t c0, c1;
   cta_share(n, &c0, &c1);
-  int64_t i = c0 + threadIdx.x;
-  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) md_call<R, Tag>(f, m, i + u * kBlock);
-  }
-  for (; i < c1; i += kBlock) md_call<R, Tag>(f, m, i);
+  md_walk<R, LEFT, Tag, IT>(f, m, c0, c1);
 }
-template <int R, class Tag, class F, class Red, class V>
+template <int R, bool LEFT, class Tag, class IT, class F, class Red, class V>
 __global__ void __launch_bounds__(kBlock)
     k_md_reduce(F f, Red red, MDArgs m, int64_t n, V* partials, unsigned* counter, V* out) {
   V v;
   red.init(v);
   int64_t c0, c1;
   cta_share(n, &c0, &c1);
-  int64_t i = c0 + threadIdx.x;
-  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) md_call<R, Tag>(f, m, i + u * kBlock, v);
-  }
-  for (; i < c1; i += kBlock) md_call<R, Tag>(f, m, i, v);
+  md_walk<R, LEFT, Tag, IT>(f, m, c0, c1, v);
   grid_finish_obj(red, v, partials, counter, out);
 }
 template <class P>
 MDArgs md_args(const P& p, int64_t* total) {
   constexpr int R = P::rank;
-  const bool left = P::inner_direction == Iterate::Left;
+  constexpr bool left = P::inner_direction == Iterate::Left;
   MDArgs m{};
   int64_t n = 1;
   for (int d = 0; d < R; ++d) {
     const int pd = left ? d : R - 1 - d;
-    m.dim[d] = pd;
-    m.lo[pd] = p.lower(pd);
+    m.lo[d] = p.lower(d);
     m.ext[d] = p.upper(pd) - p.lower(pd);
-    n *= m.ext[d];
+    n *= m.ext[d] > 0 ? m.ext[d] : 0;
   }
-  m.rank = R;
-  m.fits32 = n < (int64_t(1) << 31);
+  // kBlock written in the mixed radix of the walk extents
+  int64_t r = kBlock;
+  for (int d = 0; d < R - 1; ++d) {
+    const int64_t e = m.ext[d] > 0 ? m.ext[d] : 1;
+    m.step[d] = r % e;
+    r /= e;
+  }
+  m.step[R - 1] = r;
+  m.fits32 = n + 2 * kUnroll * kBlock < (int64_t(1) << 31);
   *total = n;
   return m;
 }
@@ -244,8 +282,12 @@ void run_reduce(cudaStream_t s, int64_t grid, const Red& red, Launch launch) {
   V* partials = reinterpret_cast<V*>(sc.base + 256);
   launched(launch(partials, sc.counters + kSlotReduce, dev_out), "parallel_reduce");
   if (!red.res.device) {
-    check_cuda(cudaMemcpyAsync(red.res.ptr, dev_out, sizeof(V), cudaMemcpyDeviceToHost, s), "parallel_reduce");
-    check(gbk_stream_check((gbk_stream_t)s), "parallel_reduce");
+    if (sizeof(V) <= 256) {  // through the workspace's pinned slot: one synchronisation
+      check(gbk_fence_read((gbk_stream_t)s, dev_out, red.res.ptr, (int64_t)sizeof(V)), "parallel_reduce");
+    } else {
+      check_cuda(cudaMemcpyAsync(red.res.ptr, dev_out, sizeof(V), cudaMemcpyDeviceToHost, s), "parallel_reduce");
+      check(gbk_stream_check((gbk_stream_t)s), "parallel_reduce");
+    }
   }
 }
 
@@ -285,8 +327,12 @@ void parallel_for(const MDRangePolicy<PP...>& p, const F& f) {
   int64_t n = 0;
   const Impl::MDArgs m = Impl::md_args(p, &n);
   if (n <= 0) return;
-  Impl::k_md_for<P::rank, typename P::work_tag>
-      <<<(unsigned)Impl::grid_for(n), Impl::kBlock, 0, p.space().stream()>>>(f, m, n);
+  constexpr bool left = P::inner_direction == Iterate::Left;
+  const unsigned g = (unsigned)Impl::grid_for(n);
+  if (m.fits32)
+    Impl::k_md_for<P::rank, left, typename P::work_tag, int32_t><<<g, Impl::kBlock, 0, p.space().stream()>>>(f, m, n);
+  else
+    Impl::k_md_for<P::rank, left, typename P::work_tag, int64_t><<<g, Impl::kBlock, 0, p.space().stream()>>>(f, m, n);
   Impl::launched(cudaGetLastError(), "parallel_for(MDRange)");
 }
 template <class E, class... R, class F>
@@ -329,8 +375,14 @@ void parallel_reduce(const MDRangePolicy<PP...>& p, const F& f, const Red& red) 
   const Impl::MDArgs m = Impl::md_args(p, &n);
   const int64_t g = Impl::grid_for(n);
   cudaStream_t s = p.space().stream();
+  constexpr bool left = P::inner_direction == Iterate::Left;
   Impl::run_reduce(s, g, red, [&](V* part, unsigned* ctr, V* out) {
-    Impl::k_md_reduce<P::rank, typename P::work_tag><<<(unsigned)g, Impl::kBlock, 0, s>>>(f, red, m, n, part, ctr, out);
+    if (m.fits32)
+      Impl::k_md_reduce<P::rank, left, typename P::work_tag, int32_t>
+          <<<(unsigned)g, Impl::kBlock, 0, s>>>(f, red, m, n, part, ctr, out);
+    else
+      Impl::k_md_reduce<P::rank, left, typename P::work_tag, int64_t>
+          <<<(unsigned)g, Impl::kBlock, 0, s>>>(f, red, m, n, part, ctr, out);
     return cudaGetLastError();
   });
 }
@@ -509,10 +561,23 @@ void parallel_reduce(const std::string& label, N n, const F& f, A0&& a0, A1&& a1
 // ---- nested patterns inside a TeamPolicy functor ---------------------------------
 // (host-device because they are called from KOKKOS_LAMBDA bodies; they only
 // do work in device code)
+// A team thread takes indices team_rank, team_rank + team_size, ... of the
+// range, kTeamUnroll of them per loop trip so that as many loads of the
+// functor are in flight (calls stay in increasing index order per thread).
+constexpr int kTeamUnroll = 8;
+template <class F, class... A>
+__device__ __forceinline__ void team_range_walk(int64_t b, int64_t e, int64_t step, const F& f, A&... a) {
+  int64_t i = b;
+  for (; i + (kTeamUnroll - 1) * step < e; i += kTeamUnroll * step) {
+#pragma unroll
+    for (int u = 0; u < kTeamUnroll; ++u) f(i + u * step, a...);
+  }
+  for (; i < e; i += step) f(i, a...);
+}
 template <class F>
 KOKKOS_INLINE_FUNCTION void parallel_for(const TeamThreadRangeBoundaries<>& r, const F& f) {
 #ifdef __CUDA_ARCH__
-  for (int64_t i = r.begin + r.member.team_rank(); i < r.end; i += r.member.team_size()) f(i);
+  team_range_walk(r.begin + r.member.team_rank(), r.end, (int64_t)r.member.team_size(), f);
 #endif
 }
 
@@ -550,7 +615,7 @@ template <class F, class T, std::enable_if_t<std::is_arithmetic<T>::value, bool>
 KOKKOS_INLINE_FUNCTION void parallel_reduce(const TeamThreadRangeBoundaries<>& r, const F& f, T& result) {
 #ifdef __CUDA_ARCH__
   T v = T(0);
-  for (int64_t i = r.begin + r.member.team_rank(); i < r.end; i += r.member.team_size()) f(i, v);
+  team_range_walk(r.begin + r.member.team_rank(), r.end, (int64_t)r.member.team_size(), f, v);
   result = Impl::team_allreduce(Impl::DevSum<T>{}, v);
 #endif
 }
@@ -559,7 +624,7 @@ KOKKOS_INLINE_FUNCTION void parallel_reduce(const TeamThreadRangeBoundaries<>& r
 #ifdef __CUDA_ARCH__
   typename Red::value_type v;
   red.init(v);
-  for (int64_t i = r.begin + r.member.team_rank(); i < r.end; i += r.member.team_size()) f(i, v);
+  team_range_walk(r.begin + r.member.team_rank(), r.end, (int64_t)r.member.team_size(), f, v);
   red.reference() = Impl::team_allreduce(red, v);
 #endif
 }

@@ -75,6 +75,14 @@ void GB300::fence(const std::string& name) const {
       });
 }
 
+void GB300::impl_fence_read(const std::string& name, const void* device_src, void* host_dst, size_t bytes) const {
+  Kokkos::Tools::Experimental::Impl::profile_fence_event<GB300>(
+      name, Kokkos::Tools::Experimental::Impl::DirectFenceIDHandle{impl_instance_id()}, [&]() {
+        Kokkos::Impl::gb300_check(gbk_fence_read((gbk_stream_t)stream(), device_src, host_dst, (int64_t)bytes),
+                                  "fence");
+      });
+}
+
 void GB300::impl_static_fence(const std::string& name) {
   Kokkos::Tools::Experimental::Impl::profile_fence_event<GB300>(
       name, Kokkos::Tools::Experimental::SpecialSynchronizationCases::GlobalDeviceSynchronization,

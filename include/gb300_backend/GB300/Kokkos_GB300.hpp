@@ -121,6 +121,9 @@ class GB300 {
   // (core/src/Cuda/Kokkos_Cuda_Error.hpp:33-67).
   void fence(const std::string& name = "Kokkos::Experimental::GB300::fence: Unnamed Instance Fence") const;
   static void impl_static_fence(const std::string& name);
+  // fence() that also copies `bytes` (at most 256) from device memory into
+  // host memory behind the same synchronisation (a host-scalar reduce result)
+  void impl_fence_read(const std::string& name, const void* device_src, void* host_dst, size_t bytes) const;
 
   int concurrency() const;  // SMs x 2048 resident threads
   void print_configuration(std::ostream& os, bool verbose = false) const;

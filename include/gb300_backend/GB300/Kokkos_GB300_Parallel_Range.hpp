@@ -96,9 +96,9 @@ void gb300_run_reduce(const Kokkos::Experimental::GB300& exec, const ReducerType
     gb300_check_cuda(cudaMemcpyAsync(result, dev_out, vsize, cudaMemcpyDeviceToDevice, exec.stream()),
                      "parallel_reduce");
   } else {
-    gb300_check_cuda(cudaMemcpyAsync(result, dev_out, vsize, cudaMemcpyDeviceToHost, exec.stream()),
-                     "parallel_reduce");
-    exec.fence("Kokkos::Impl::ParallelReduce<GB300>: result not device accessible");
+    // value sizes are at most VB = 256 bytes (checked above)
+    exec.impl_fence_read("Kokkos::Impl::ParallelReduce<GB300>: result not device accessible", dev_out, result,
+                         vsize);
   }
 }
 

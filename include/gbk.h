@@ -92,6 +92,13 @@ int gbk_device_info(int* sm_count, int* cc_major, int* cc_minor, int64_t* l2_byt
  * its workspace (fence(), core/src/Cuda/Kokkos_Cuda.hpp; error convention of
  * core/src/Cuda/Kokkos_Cuda_Error.hpp:33-67). */
 int gbk_stream_check(gbk_stream_t stream);
+/* gbk_stream_check that also returns `bytes` (at most 256) read from device
+ * memory at device_src once the stream's earlier work is done, into
+ * host_dst: both reads land in a pinned host slot of the workspace, behind
+ * one stream synchronisation.  The host-scalar result of a parallel_reduce:
+ * the reference reads it from pinned "unified" scratch after one fence
+ * (core/src/Cuda/Kokkos_Cuda_Parallel_Range.hpp:344-359). */
+int gbk_fence_read(gbk_stream_t stream, const void* device_src, void* host_dst, int64_t bytes);
 /* Pre-size the stream's workspace (needed before graph capture). */
 int gbk_workspace_reserve(gbk_stream_t stream, int64_t bytes);
 /* Free every workspace (after all work on them has finished). */

@@ -43,6 +43,10 @@ struct Workspace {
   size_t flags_bytes = 0;
   uint32_t epoch = 0;
   std::mutex mu;
+  // Pinned host slot for fences: [0, 4) the error word's copy, [256, 512) a
+  // small result read back with it (one stream synchronisation for both).
+  char* host_slot = nullptr;
+  std::mutex slot_mu;
 };
 
 Workspace* ws_get(cudaStream_t s, int* status);

@@ -198,22 +198,36 @@ int gbk_device_info(int* sm, int* major, int* minor, int64_t* l2) {
   return GBK_OK;
 }
 
-int gbk_stream_check(gbk_stream_t stream) {
+int gbk_stream_check(gbk_stream_t stream) { return gbk_fence_read(stream, nullptr, nullptr, 0); }
+
+int gbk_fence_read(gbk_stream_t stream, const void* device_src, void* host_dst, int64_t bytes) {
+  if (bytes < 0 || bytes > 256 || (bytes > 0 && (!device_src || !host_dst))) return GBK_ERR_INVALID_ARGUMENT;
   cudaStream_t s = (cudaStream_t)stream;
-  GBK_CUDA_TRY(cudaStreamSynchronize(s));
   int st = GBK_OK;
   Workspace* w = ws_get(s, &st);
   if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->slot_mu);
+  if (!w->host_slot) {
+    void* p = nullptr;
+    GBK_CUDA_TRY(cudaHostAlloc(&p, 512, cudaHostAllocDefault));
+    w->host_slot = (char*)p;
+  }
+  // Both copies queue behind all earlier work on the stream, so the error
+  // word holds every status the stream's kernels raised; one synchronisation.
+  if (bytes) GBK_CUDA_TRY(cudaMemcpyAsync(w->host_slot + 256, device_src, (size_t)bytes, cudaMemcpyDeviceToHost, s));
+  GBK_CUDA_TRY(cudaMemcpyAsync(w->host_slot, w->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GBK_CUDA_TRY(cudaStreamSynchronize(s));
   int bits = 0;
-  GBK_CUDA_TRY(cudaMemcpy(&bits, w->err, sizeof(int), cudaMemcpyDeviceToHost));
+  std::memcpy(&bits, w->host_slot, sizeof(int));
+  if (bytes) std::memcpy(host_dst, w->host_slot + 256, (size_t)bytes);
   if (bits) {
-    int zero = 0;
-    GBK_CUDA_TRY(cudaMemcpy(w->err, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    GBK_CUDA_TRY(cudaMemsetAsync(w->err, 0, sizeof(int), s));
     // After a timed-out wait the ticket counters may be left non-zero.
     if (bits & (GBK_EBIT_TIMEOUT | GBK_EBIT_BAD_STATE)) {
-      GBK_CUDA_TRY(cudaMemset(w->counters, 0, 64 * sizeof(unsigned)));
-      if (w->scratch) GBK_CUDA_TRY(cudaMemset(w->scratch, 0, w->scratch_bytes));
+      GBK_CUDA_TRY(cudaMemsetAsync(w->counters, 0, 64 * sizeof(unsigned), s));
+      if (w->scratch) GBK_CUDA_TRY(cudaMemsetAsync(w->scratch, 0, w->scratch_bytes, s));
     }
+    GBK_CUDA_TRY(cudaStreamSynchronize(s));
   }
   if (bits & GBK_EBIT_TIMEOUT) return GBK_ERR_DEVICE_TIMEOUT;
   if (bits & GBK_EBIT_BAD_STATE) return GBK_ERR_CUDA;

@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(BLOCK)
 // other increments can raise the counter by less than the 0x7FFF headroom
 // left (far fewer increments are in flight in one CTA), so no carry reaches
 // the neighbouring bin.
-template <int BLOCK, bool AGG, bool NODRAIN>
+template <int BLOCK, bool AGG, int MODE>
 __global__ void __launch_bounds__(BLOCK, 1)
     k_hist16(const int32_t* __restrict__ keys, int64_t nvec, int64_t nbins, unsigned long long* bins, int* err) {
   extern __shared__ __align__(16) unsigned sh[];
@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(BLOCK, 1)
   constexpr int ROUND = BLOCK * VPT;           // vectors per round
   constexpr int DRAIN = 32768 / (ROUND * 4);   // rounds between drains
   static_assert(DRAIN >= 1, "round too large for 16-bit counters");
+  constexpr bool NODRAIN = MODE != 0;
   const int nwords = (int)((nbins + 1) >> 1);
   for (int i = threadIdx.x; i <= nwords; i += BLOCK) sh[i] = 0u;  // the counters and the spare word
   pdl_entry();
@@ -215,12 +216,46 @@ __global__ void __launch_bounds__(BLOCK, 1)
       const int64_t q = vn + (int64_t)j * BLOCK + threadIdx.x;
       nxt[j].u = q < v1 ? ld_stream16(keys + 4 * q) : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
     }
+    if constexpr (MODE == 2 && !AGG) {
+      // All 4 x VPT shared atomics of the round are issued before any of
+      // their old values is tested, so they are in flight together; the one
+      // thread whose increment took a half from 0x7FFF to 0x8000 moves 0x8000
+      // to the global bin afterwards (others may have counted past 0x8000 in
+      // between: the half has 0x8000 of headroom).  Vectors past the share
+      // add 0 to the spare word.
+      unsigned o[VPT][4], wd[VPT][4], hs[VPT][4];
 #pragma unroll
-    for (int j = 0; j < VPT; ++j) {
-      const int64_t q = v + (int64_t)j * BLOCK + threadIdx.x;
-      if (q < v1) {
+      for (int j = 0; j < VPT; ++j) {
+        const bool in = v + (int64_t)j * BLOCK + threadIdx.x < v1;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) count(cur[j].v[e]);
+        for (int e = 0; e < 4; ++e) {
+          const unsigned uk = (unsigned)cur[j].v[e];
+          const bool ok = uk < nb32;
+          bad = bad || (in && !ok);
+          const unsigned hi = uk >= nw32 ? 16u : 0u;
+          wd[j][e] = ok ? uk - (hi ? nw32 : 0u) : nw32;
+          hs[j][e] = (ok && in) ? hi : 32u;  // 32: nothing counted, nothing to test
+          o[j][e] = atomicAdd(sh + wd[j][e], (ok && in) ? 1u << hi : 0u);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < VPT; ++j) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (hs[j][e] < 32u && ((o[j][e] >> hs[j][e]) & 0xFFFFu) == 0x7FFFu) {
+            atomicSub(sh + wd[j][e], 0x8000u << hs[j][e]);
+            red_add_u64(bins + (hs[j][e] ? nw32 + wd[j][e] : wd[j][e]), 0x8000ull);
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < VPT; ++j) {
+        const int64_t q = v + (int64_t)j * BLOCK + threadIdx.x;
+        if (q < v1) {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) count(cur[j].v[e]);
+        }
       }
     }
 #pragma unroll
@@ -253,11 +288,11 @@ __global__ void k_hist_edges(const int32_t* __restrict__ keys, int64_t head, int
   else atomicOr(err, GBK_EBIT_KEY_RANGE);
 }
 
-template <bool AGG, bool NODRAIN>
+template <bool AGG, int MODE>
 int launch_hist16(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, Workspace* w) {
   constexpr int BLOCK = 1024;
   const size_t smem = (size_t)((nbins + 1) >> 1) * 4 + 16;  // counters, then the spare word for keys outside the bins
-  auto kfn = k_hist16<BLOCK, AGG, NODRAIN>;
+  auto kfn = k_hist16<BLOCK, AGG, MODE>;
   GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uintptr_t a = (uintptr_t)keys;
   int64_t head = (int64_t)(((16 - (a & 15)) & 15) / 4);
@@ -336,7 +371,8 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   if (n == 0) return GBK_OK;
   // variant bits: 0x0F cluster size of the 32-bit privatised kernel (1, 2,
   // 4, 8); 0x10 warp aggregation; 0x20 the 16-bit one-CTA-per-SM kernel;
-  // 0x40 no privatisation; 0x80 the 16-bit kernel without drains.
+  // 0x40 no privatisation; 0x80 the 16-bit kernel without drains; 0x100
+  // the same with each round's atomics issued before their tests.
   // 0 = automatic choice.
   const int var = t ? t->variant : 0;
   int cl = var & 0xF;
@@ -347,12 +383,13 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   const bool force_global = (var & 0x40) != 0;
   if (var == 0) {
     if (nbins * 4 <= 96 * 1024) cl = 1;
-    else if ((nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, true>(keys, n, nbins, bins, w);
+    else if ((nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, 1>(keys, n, nbins, bins, w);
     else { cl = 2; while (cl <= 8 && (nbins + cl - 1) / cl * 4 > max_smem) cl *= 2; }
   }
-  if ((var & 0x80) && (nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, true>(keys, n, nbins, bins, w);
+  if ((var & 0x100) && (nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, 2>(keys, n, nbins, bins, w);
+  if ((var & 0x80) && (nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, 1>(keys, n, nbins, bins, w);
   if (use16 && !force_global && (nbins + 1) / 2 * 4 <= max_smem) {
-    return agg ? launch_hist16<true, false>(keys, n, nbins, bins, w) : launch_hist16<false, false>(keys, n, nbins, bins, w);
+    return agg ? launch_hist16<true, 0>(keys, n, nbins, bins, w) : launch_hist16<false, 0>(keys, n, nbins, bins, w);
   }
   if (cl == 0) cl = 1;
   if (force_global || (nbins + cl - 1) / cl * 4 > max_smem || cl > 8) {

@@ -49,6 +49,7 @@ _SIGS = {
     "gbk_status_string": ([ci], ctypes.c_char_p),
     "gbk_device_info": ([vp, vp, vp, vp], ci),
     "gbk_stream_check": ([vp], ci),
+    "gbk_fence_read": ([vp, vp, vp, i64], ci),
     "gbk_workspace_reserve": ([vp, i64], ci),
     "gbk_workspace_release_all": ([], ci),
     "gbk_set_wait_limit": ([i64], ci),

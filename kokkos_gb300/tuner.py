@@ -3,11 +3,14 @@
 * Exhaustive autotuner: for a workload (operation kind, element type, size,
   segment statistics, histogram bins and key entropy) every candidate launch
   configuration is timed through the C ABI (CUDA events, median of repeats).
-* Learned tuner: a 3-layer, 64-hidden FP32 MLP (features of the workload and
-  of a candidate configuration -> log time), trained with the library's own
-  CUDA kernels (gbk_mlp_forward / backward / mse / adam); for an unseen
-  workload it picks the candidate with the smallest predicted time.  The
-  exhaustive tuner stays the fallback and the judge of its regret.
+* Learned tuner: an ensemble of five 3-layer, 64-hidden FP32 MLPs (features
+  of the workload and of a candidate configuration -> log time relative to
+  the workload's mean), trained with the library's own CUDA kernels
+  (gbk_mlp_forward / backward / mse / adam); for an unseen workload it picks
+  the candidate with the smallest mean predicted time.  The exhaustive tuner
+  stays the fallback and the judge of its regret; the tuning table (the
+  exhaustive best per bucket, looked up at the nearest bucket) is the method
+  without the MLP that it is compared with.
 * The tuning table (text, loaded by gbk_tuner_load) maps (kind, op, dtype,
   log2 n, extra) to the chosen configuration; the entry points consult it
   when called without an explicit configuration.
@@ -25,20 +28,24 @@ import time
 
 import numpy as np
 
-KIND_REDUCE, KIND_SCAN, KIND_HIST, KIND_SEG = 0, 1, 2, 3
+KIND_REDUCE, KIND_SCAN, KIND_HIST, KIND_SEG, KIND_SEGSCAN = 0, 1, 2, 3, 4
 REDUCE_CFGS = [(b, u, c) for (b, u) in [(256, 2), (256, 4), (256, 8), (512, 2), (512, 4), (128, 8), (1024, 2)]
                for c in (1, 2, 4, 8)]
 SCAN_CFGS = [(9, 0), (7, 0), (3, 0), (9, 1)]  # (vectors per thread, CTAs per SM; 0 = all resident)
 # segmented reduce (variant, vectors per thread, CTAs per SM; 0 = all resident): variant 0 is the
 # contiguous-share kernel (its shape is fixed), variant 1 the tile pipeline
 SEG_CFGS = [(0, 7, 0), (1, 7, 0), (1, 3, 0), (1, 7, 1)]
-# histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit, no privatisation
+# segmented scan (the tile pipeline; vectors per thread, CTAs per SM)
+SEGSCAN_CFGS = [(7, 0), (3, 0), (7, 1), (3, 1)]
+# histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit with periodic drains (0x20)
+# or drain-free (0x80), no privatisation (0x40)
 HIST_CFGS_SMALL = [(0x01, 1), (0x01, 2), (0x11, 2), (0x20, 1), (0x30, 1), (0x40, 1)]
-HIST_CFGS_2E16 = [(0x02, 1), (0x12, 1), (0x04, 1), (0x20, 1), (0x30, 1), (0x40, 1)]
+HIST_CFGS_2E16 = [(0x02, 1), (0x12, 1), (0x04, 1), (0x20, 1), (0x30, 1), (0x80, 1), (0x40, 1)]
 SPLIT_CFGS = [(3, 0), (4, 0), (5, 0), (6, 0), (5, 2)]  # double Sum, variant 3: (vectors per thread, CTAs per SM)
-REDUCE_OPS = [("sum", 5), ("sum", 4), ("minloc", 4), ("maxloc", 4), ("sum", 0), ("sum", 1)]  # (op, dtype code)
-OPC = {"sum": 0, "minloc": 8, "maxloc": 9}
-NFEAT = 24
+# (op, dtype code); "mmls" is the fused MinMaxLoc+Sum reducer
+REDUCE_OPS = [("sum", 5), ("sum", 4), ("minloc", 4), ("maxloc", 4), ("mmls", 4), ("sum", 0), ("sum", 1)]
+OPC = {"sum": 0, "minloc": 8, "maxloc": 9, "mmls": 12}
+NFEAT = 34
 
 
 def candidates(w):
@@ -55,6 +62,8 @@ def candidates(w):
         return [{"block": 256, "ipt": u, "cps": c, "variant": 0} for (u, c) in SCAN_CFGS]
     if k == KIND_SEG:
         return [{"block": 256, "ipt": u, "cps": c, "variant": v} for (v, u, c) in SEG_CFGS]
+    if k == KIND_SEGSCAN:
+        return [{"block": 256, "ipt": u, "cps": c, "variant": 1} for (u, c) in SEGSCAN_CFGS]
     cf = HIST_CFGS_2E16 if w["nbins"] > 24576 else HIST_CFGS_SMALL
     return [{"block": 0, "ipt": 0, "cps": c, "variant": v} for (v, c) in cf]
 
@@ -62,9 +71,16 @@ def candidates(w):
 def features(w, c):
     """Workload + candidate features (NFEAT floats, roughly unit scale)."""
     f = np.zeros(NFEAT, dtype=np.float32)
-    f[w["kind"]] = 1.0                                   # 0..3 kind one-hot
+    k = w["kind"]
+    f[min(k, KIND_SEG)] = 1.0                            # 0..3 kind one-hot (both segmented kinds: 3)
+    f[24] = float(k == KIND_SEGSCAN)                     # segmented scan
     f[4 + w["dtype"]] = 1.0                              # 4..9 dtype one-hot
-    f[10] = {0: 0.0, 8: 1.0, 9: 1.0}.get(w.get("op", 0), 0.0)  # *Loc reducer
+    op = w.get("op", 0)
+    if k == KIND_REDUCE:
+        f[10] = float(op in (8, 9, 12))                  # *Loc reducer
+        f[25] = float(op == 12)                          # fused MinMaxLoc+Sum
+    elif k in (KIND_SCAN, KIND_SEGSCAN):
+        f[27] = float(op & 1)                            # inclusive
     f[11] = (math.log2(max(w["n"], 1)) - 22.0) / 6.0     # size
     f[12] = (w.get("seg_log2mean", 0.0) - 11.0) / 4.0    # segment-length mean (log2)
     f[13] = w.get("seg_sigma", 0.0) / 2.0                # segment-length spread (lognormal sigma)
@@ -75,17 +91,24 @@ def features(w, c):
     f[18] = (math.log2(max(c["ipt"], 1)) - 2.0) / 1.5
     f[19] = (math.log2(max(c["cps"], 1)) - 2.0) / 2.0
     v = c["variant"]
-    # histogram: cluster-split bins; reduce: the ring kernel (variant 2)
-    if w["kind"] == KIND_SEG:
-        f[20] = float(v == 1)                            # segmented: the tile pipeline
-    elif w["kind"] == KIND_REDUCE:
-        f[20] = float(v == 2)
-    else:
-        f[20] = float((v & 0xF) > 1) if v and not (v & 0x60) else 0.0
-    # histogram: warp aggregation; reduce: the FP64 / integer split kernel (variant 3)
-    f[21] = float(v == 3) if w["kind"] == KIND_REDUCE else float((v & 0x10) != 0)
-    f[22] = float((v & 0x20) != 0)                       # 16-bit bins
-    f[23] = float((v & 0x40) != 0)                       # no privatisation
+    if k == KIND_SEG:
+        f[20] = float(v == 1)                            # segmented reduce: the tile pipeline
+    elif k == KIND_REDUCE:
+        f[20] = float(v == 2)                            # reduce: the ring kernel
+        f[21] = float(v == 3)                            # reduce: the FP64 / integer split kernel
+    elif k == KIND_HIST:
+        f[20] = float((v & 0xF) > 1) if v and not (v & 0xE0) else 0.0  # cluster-split bins
+        f[21] = float((v & 0x10) != 0)                   # warp aggregation
+        f[22] = float((v & 0xA0) != 0)                   # 16-bit bins
+        f[23] = float((v & 0x40) != 0)                   # no privatisation
+        f[26] = float((v & 0x80) != 0)                   # 16-bit bins without drains
+    # size x candidate interactions: the best tile depth, block and CTAs per SM move with the size
+    f[28] = f[11] * f[18]
+    f[29] = f[11] * f[19]
+    f[30] = f[11] * f[17]
+    f[31] = f[11] * f[11]
+    f[32] = float(c["cps"] == 0)                         # all resident CTAs
+    f[33] = f[11] * f[20]
     return f
 
 
@@ -94,24 +117,28 @@ def sample_workloads(count, seed):
     out = []
     for _ in range(count):
         r = rng.random()
-        if r < 0.45:
+        if r < 0.40:
             op, dt = REDUCE_OPS[rng.integers(len(REDUCE_OPS))]
             n = int(2 ** rng.uniform(16, 27 if dt in (1, 5) else 28))
             out.append({"kind": KIND_REDUCE, "op": OPC[op], "opname": op, "dtype": dt, "n": n, "inner_extent": 1})
-        elif r < 0.65:
+        elif r < 0.55:
             n = int(2 ** rng.uniform(16, 28))
             out.append({"kind": KIND_SCAN, "op": int(rng.integers(2)), "dtype": 0, "n": n})
-        elif r < 0.82:
+        elif r < 0.72:
             nb = int(rng.choice([256, 4096, 65536]))
             out.append({"kind": KIND_HIST, "op": 0, "dtype": 0, "n": int(2 ** rng.uniform(16, 26)), "nbins": nb,
                         "pool": int(rng.integers(5))})
         else:
+            # batched segments (lognormal lengths): Sum of f32, or an int32 -> int64 scan
             nseg = int(2 ** rng.uniform(6, 13.3))
             l2m = float(rng.uniform(6, 13))
             sig = float(rng.uniform(0.3, 2.5))
             total = min(int(nseg * 2 ** l2m), 1 << 27)
-            out.append({"kind": KIND_SEG, "op": 0, "dtype": 4, "n": total, "nseg": nseg, "seg_log2mean": l2m,
-                        "seg_sigma": sig, "seed": int(rng.integers(1 << 30))})
+            w = {"kind": KIND_SEG, "op": 0, "dtype": 4, "n": total, "nseg": nseg, "seg_log2mean": l2m,
+                 "seg_sigma": sig, "seed": int(rng.integers(1 << 30))}
+            if r >= 0.86:
+                w.update(kind=KIND_SEGSCAN, op=int(rng.integers(2)), dtype=0)
+            out.append(w)
     return out
 
 
@@ -167,7 +194,7 @@ class Bench:
             w["entropy_bits"] = self.entropy(w["pool"], w["nbins"])
             w["keys"] = (self.pools[w["pool"]][: w["n"]] % w["nbins"]).contiguous() if w["nbins"] < 65536 \
                 else self.pools[w["pool"]][: w["n"]]
-        if w["kind"] == KIND_SEG:
+        if w["kind"] in (KIND_SEG, KIND_SEGSCAN):
             lens, _ = self.datagen.lognormal_lengths(w["nseg"], median=2 ** w["seg_log2mean"], max_len=1 << 24,
                                                      target_total=min(w["n"], self.max_n // 2), seed=w["seed"])
             lens = np.minimum(lens, max(1, (self.max_n // 2) // max(w["nseg"], 1)))
@@ -191,6 +218,10 @@ class Bench:
         if k == KIND_HIST:
             return lib.gbk_histogram_i32_i64(ctypes.c_void_p(w["keys"].data_ptr()), w["n"],
                                              ctypes.c_void_p(self.bins.data_ptr()), w["nbins"], sp, ctypes.byref(t))
+        if k == KIND_SEGSCAN:
+            return lib.gbk_segmented_scan(w["op"], 0, 1, ctypes.c_void_p(self.i32.data_ptr()),
+                                          ctypes.c_void_p(w["offsets"].data_ptr()), w["nseg"], w["n"],
+                                          ctypes.c_void_p(self.y64.data_ptr()), sp, ctypes.byref(t))
         return lib.gbk_segmented_reduce(0, 4, ctypes.c_void_p(self.f32.data_ptr()),
                                         ctypes.c_void_p(w["offsets"].data_ptr()), w["nseg"], w["n"],
                                         ctypes.c_void_p(w["segout"].data_ptr()), sp, ctypes.byref(t))
@@ -307,6 +338,29 @@ class MLP:
         return Y.cpu().numpy() * self.sd + self.mu
 
 
+class Ensemble:
+    """K MLPs from different initial weights, trained on the same samples;
+    the prediction is their mean (less variance in the pick)."""
+
+    def __init__(self, k=5, D=NFEAT):
+        self.models = [MLP(D=D, seed=s) for s in range(k)]
+
+    def train(self, X, T, epochs=300, **kw):
+        hist = []
+        for s, m in enumerate(self.models):
+            h = m.train(X, T, epochs=epochs, seed=s, **kw)
+            hist = h if not hist else [(a[0], a[1] + b[1]) for a, b in zip(hist, h)]
+        return [(e, l / len(self.models)) for e, l in hist]
+
+    def predict(self, X):
+        return np.mean([m.predict(X) for m in self.models], axis=0)
+
+    @property
+    def params(self):
+        import torch
+        return torch.stack([m.params for m in self.models])
+
+
 def default_cfg_index(w, cs):
     """The configuration the library uses without tuning."""
     k = w["kind"]
@@ -322,30 +376,79 @@ def default_cfg_index(w, cs):
                 return i
         if k == KIND_SCAN and (c["ipt"], c["cps"]) == (9, 0):
             return i
+        # segmented reduce: 7 vectors; segmented int32 -> int64 scan (widening): 3
         if k == KIND_SEG and (c["ipt"], c["cps"]) == (7, 0):
             return i
+        if k == KIND_SEGSCAN and (c["ipt"], c["cps"]) == (3, 0):
+            return i
         if k == KIND_HIST:
-            want = 0x20 if w["nbins"] > 24576 else 0x01
-            if c["variant"] == want:
+            # 65536 bins: the drain-free 16-bit kernel; up to 24576: 32-bit
+            # privatised bins, two CTAs per SM
+            want = (0x80, 1) if w["nbins"] > 24576 else (0x01, 2)
+            if (c["variant"], c["cps"]) == want:
                 return i
     return 0
 
 
+def _ceil_log2(v):
+    v = max(int(v), 1)
+    return (v - 1).bit_length()
+
+
+def lookup_key(w):
+    """(kind, op, dtype, n, extra): the key under which the entry point for
+    this workload looks its configuration up in the tuning table."""
+    k = w["kind"]
+    if k == KIND_REDUCE:
+        return 0, w["op"], w["dtype"], w["n"], 0
+    if k == KIND_SCAN:
+        return 1, w["op"], 0 * 8 + 1, w["n"], 0
+    if k == KIND_HIST:
+        return 2, 0, 0, w["n"], _ceil_log2(w["nbins"]) * 8
+    extra = _ceil_log2(w["n"] // max(w["nseg"], 1))
+    if k == KIND_SEG:
+        return 3, 0, 4, w["n"], extra
+    return 3, 16 + w["op"], 0 * 8 + 1, w["n"], extra
+
+
+def table_pick(w, cs):
+    """Index of the candidate the loaded tuning table gives this workload (the
+    nearest log2 n of its bucket, as the entry points do), or the default's
+    when the table has no entry for it.  This is the method without the MLP."""
+    from kokkos_gb300 import gbk
+    t = gbk.Tuning()
+    if gbk.lib.gbk_tuner_lookup(*lookup_key(w), ctypes.byref(t)) == 0:
+        for i, c in enumerate(cs):
+            if (c["block"], c["ipt"], c["cps"], c["variant"]) == (t.block, t.items_per_thread, t.ctas_per_sm,
+                                                                  t.variant):
+                return i
+    return default_cfg_index(w, cs)
+
+
 def dataset(rows):
+    """Training set: one sample per (workload, candidate).  The target is the
+    candidate's log time minus the mean log time of its workload's
+    candidates: only the order within a workload matters for the pick, and
+    the centred target leaves the model's capacity to that order."""
     X, T, grp = [], [], []
     for gi, (w, cs, ts) in enumerate(rows):
+        lt = [math.log(t) for t in ts if math.isfinite(t) and t > 0]
+        if not lt:
+            continue
+        mu = float(np.mean(lt))
         for c, t in zip(cs, ts):
             if math.isfinite(t) and t > 0:
                 X.append(features(w, c))
-                T.append(math.log(t))
+                T.append(math.log(t) - mu)
                 grp.append(gi)
     return np.array(X, dtype=np.float32), np.array(T, dtype=np.float64), np.array(grp)
 
 
-def evaluate(model, rows):
-    """Throughput of the predicted-best and of the default configuration
-    relative to the exhaustive best, per held-out workload."""
-    pred_ratio, def_ratio = [], []
+def evaluate(model, rows, table=False):
+    """Throughput of the MLP's predicted-best, of the untuned default and (with
+    table=True, for the tuning table loaded in the library) of the table's
+    configuration, each relative to the exhaustive best, per held-out workload."""
+    ratios = {"mlp": [], "default": [], "table": []}
     per_kind = {}
     for (w, cs, ts) in rows:
         ts = np.array(ts)
@@ -356,20 +459,25 @@ def evaluate(model, rows):
         X = np.stack([features(w, c) for c in cs])
         p = model.predict(X)
         p[~ok] = np.inf
-        pr = best / ts[int(np.argmin(p))]
-        dr = best / ts[default_cfg_index(w, cs)]
-        pred_ratio.append(pr)
-        def_ratio.append(dr)
-        per_kind.setdefault(w["kind"], []).append((pr, dr))
-    return {
-        "workloads": len(pred_ratio),
-        "mlp_mean_throughput_vs_best": float(np.mean(pred_ratio)),
-        "mlp_geomean_throughput_vs_best": float(np.exp(np.mean(np.log(pred_ratio)))),
-        "default_mean_throughput_vs_best": float(np.mean(def_ratio)),
-        "mlp_frac_within_5pct": float(np.mean(np.array(pred_ratio) >= 0.95)),
-        "per_kind": {str(k): {"n": len(v), "mlp": float(np.mean([a for a, _ in v])),
-                              "default": float(np.mean([b for _, b in v]))} for k, v in per_kind.items()},
-    }
+        r = {"mlp": best / ts[int(np.argmin(p))], "default": best / ts[default_cfg_index(w, cs)]}
+        if table:
+            r["table"] = best / ts[table_pick(w, cs)]
+        for key, v in r.items():
+            ratios[key].append(float(v))
+        per_kind.setdefault(w["kind"], []).append(r)
+    rep = {"workloads": len(ratios["mlp"])}
+    for key, v in ratios.items():
+        if not v:
+            continue
+        a = np.array(v)
+        rep[f"{key}_mean_throughput_vs_best"] = float(a.mean())
+        rep[f"{key}_geomean_throughput_vs_best"] = float(np.exp(np.log(a).mean()))
+        rep[f"{key}_frac_within_5pct"] = float((a >= 0.95).mean())
+    rep["per_kind"] = {str(k): dict({"n": len(v)}, **{key: float(np.mean([r[key] for r in v])) for key in v[0]},
+                                    **{key + "_within_5pct": float(np.mean([r[key] >= 0.95 for r in v]))
+                                       for key in v[0]})
+                       for k, v in per_kind.items()}
+    return rep
 
 
 def grid_workloads():
@@ -386,16 +494,21 @@ def grid_workloads():
         if l2 <= 26:
             for nb in (256, 4096, 65536):
                 out.append({"kind": KIND_HIST, "op": 0, "dtype": 0, "n": 1 << l2, "nbins": nb, "pool": 3})
+    # batched segments: total size x mean segment length (lognormal sigma 1.5)
+    for l2 in (20, 22, 24, 26):
+        for l2m in (6, 8, 10, 12):
+            base = {"kind": KIND_SEG, "op": 0, "dtype": 4, "n": 1 << l2, "nseg": 1 << (l2 - l2m),
+                    "seg_log2mean": float(l2m), "seg_sigma": 1.5, "seed": 7}
+            out.append(dict(base))
+            for inc in (0, 1):
+                out.append(dict(base, kind=KIND_SEGSCAN, op=inc, dtype=0))
     return out
 
 
 def table_line(w, c):
-    l2 = int(round(math.log2(w["n"])))
-    if w["kind"] == KIND_REDUCE:
-        return f"0 {w['op']} {w['dtype']} {l2} 0 {c['block']} {c['ipt']} {c['cps']} {c['variant']}"
-    if w["kind"] == KIND_SCAN:
-        return f"1 {w['op']} {0 * 8 + 1} {l2} 0 {c['block']} {c['ipt']} {c['cps']} 0"
-    return f"2 0 0 {l2} {int(math.log2(w['nbins'])) * 8} 0 0 {c['cps']} {c['variant']}"
+    k, op, dt, n, extra = lookup_key(w)
+    l2 = int(round(math.log2(max(n, 1))))
+    return f"{k} {op} {dt} {l2} {extra} {c['block']} {c['ipt']} {c['cps']} {c['variant']}"
 
 
 HEADER = "# kind op dtype log2n extra block items_per_thread ctas_per_sm variant"
@@ -448,20 +561,29 @@ def main():
     eval_rows = collect(eval_w, bench)
     t_collect = time.time() - t0
     X, T, _ = dataset(train_rows)
-    model = MLP(seed=0)
+    model = Ensemble(k=5)
     t1 = time.time()
     hist = model.train(X, T, epochs=args.epochs)
     t_train = time.time() - t1
-    rep = evaluate(model, eval_rows)
+    grid_rows = collect(grid_workloads(), bench, log_every=0)
+    table = table_exhaustive(grid_rows, os.path.join(args.out, "tuning_table.txt"))
+    from kokkos_gb300 import gbk
+    gbk.check(gbk.lib.gbk_tuner_load(table.encode()), "tuner_load")
+    try:
+        rep = evaluate(model, eval_rows, table=True)
+    finally:
+        gbk.lib.gbk_tuner_clear()
     rep.update({"train_timings": int(X.shape[0]), "eval_timings": int(sum(len(r[2]) for r in eval_rows)),
                 "collect_s": round(t_collect, 1), "train_s": round(t_train, 1), "loss_history": hist[::4] + hist[-1:]})
-    grid_rows = collect(grid_workloads(), bench, log_every=0)
-    table_exhaustive(grid_rows, os.path.join(args.out, "tuning_table.txt"))
     rep["grid_buckets"] = len(grid_rows)
     rep["mlp_grid_throughput_vs_best"] = table_from_model(model, grid_rows, os.path.join(args.out, "mlp_table.txt"))
     np.save(os.path.join(args.out, "mlp_params.npy"), model.params.cpu().numpy())
     with open(os.path.join(args.out, "tuner_eval.json"), "w") as f:
         json.dump(rep, f, indent=1)
+    # every timing, for re-analysis without the GPU
+    with open(os.path.join(args.out, "timings.json"), "w") as f:
+        json.dump({name: [[w, cs, [t if math.isfinite(t) else None for t in ts]] for (w, cs, ts) in rows]
+                   for name, rows in (("train", train_rows), ("eval", eval_rows), ("grid", grid_rows))}, f)
     print(json.dumps({k: v for k, v in rep.items() if k != "loss_history"}, indent=1))
 
 

@@ -35,7 +35,7 @@ def test_golden_histograms(env):
         np.testing.assert_array_equal(bins.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 4, 8, 0x11, 0x12, 0x14, 0x18, 0x20, 0x30, 0x40, 0x80])
+@pytest.mark.parametrize("variant", [0, 1, 2, 4, 8, 0x11, 0x12, 0x14, 0x18, 0x20, 0x30, 0x40, 0x80, 0x100])
 @pytest.mark.parametrize("nbins", [16, 1000, 4096, 1 << 16])
 def test_histogram_variants(env, variant, nbins):
     """Every privatisation variant (cluster size 1/2/4/8, with/without warp
@@ -56,7 +56,7 @@ def test_histogram_variants(env, variant, nbins):
     np.testing.assert_array_equal(bins.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("variant", [0x20, 0x30, 0, 0x80])
+@pytest.mark.parametrize("variant", [0x20, 0x30, 0, 0x80, 0x100])
 def test_hist16_saturating_bins(env, variant):
     """16-bit privatised counters: one bin taking every key, and two bins
     sharing one 32-bit word both taking millions of keys, stay exact."""
@@ -71,7 +71,7 @@ def test_hist16_saturating_bins(env, variant):
         np.testing.assert_array_equal(bins.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("variant", [0x20, 0x30, 0x80])
+@pytest.mark.parametrize("variant", [0x20, 0x30, 0x80, 0x100])
 def test_hist16_saturating_ragged_words(env, variant):
     """16-bit counters when the word count is not a multiple of four (4,099
     bins: 2,050 words): the hot bins sit in the last words, which the drain
@@ -85,7 +85,7 @@ def test_hist16_saturating_ragged_words(env, variant):
     np.testing.assert_array_equal(bins.cpu().numpy(), np.bincount(keys, minlength=nb))
 
 
-@pytest.mark.parametrize("variant", [0, 0x20, 0x80])
+@pytest.mark.parametrize("variant", [0, 0x20, 0x80, 0x100])
 @pytest.mark.parametrize("offset", [1, 2, 3])
 def test_hist16_unaligned_keys(env, variant, offset):
     """Keys that start off the 16-byte boundary (a ragged head and tail go
@@ -131,7 +131,7 @@ def test_out_of_range_keys_flagged(env):
     gbk.stream_check()  # the flag was cleared
 
 
-@pytest.mark.parametrize("variant", [0x20, 0x30, 0x80])
+@pytest.mark.parametrize("variant", [0x20, 0x30, 0x80, 0x100])
 def test_hist16_out_of_range_keys(env, variant):
     """16-bit counters: keys below 0 or at and above nbins (odd nbins, so
     the last word's high half is not a bin) are left out of every bin and

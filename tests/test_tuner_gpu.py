@@ -52,3 +52,39 @@ def test_small_pipeline_and_table():
     finally:
         gbk.lib.gbk_tuner_enable(0)
         gbk.lib.gbk_tuner_clear()
+
+
+def test_mlp_gains_over_the_methods_without_it():
+    """On held-out workloads (sizes, segment statistics and key distributions
+    the training set never held) the learned tuner's choice (an ensemble of
+    five MLPs trained by the library's kernels) is compared with the
+    exhaustive best, with the library's untuned default, and with the tuning
+    table the exhaustive autotuner writes for its buckets (the method without
+    the MLP: nearest bucket by ceil(log2 n), as the entry points look it up).
+    Margins (mean throughput relative to the best, and the fraction of
+    workloads within 5 % of the best):
+      MLP >= default + 0.02;  MLP >= table + 0.005;
+      MLP within 5 % on >= 0.88 of the workloads and on more of them than the table."""
+    from kokkos_gb300 import gbk, tuner
+    GAIN_DEFAULT, GAIN_TABLE, WITHIN_5PCT = 0.02, 0.005, 0.88
+    bench = tuner.Bench(max_n=1 << 26)
+    train = tuner.collect(tuner.sample_workloads(500, seed=21), bench, log_every=0)
+    held = tuner.collect(tuner.sample_workloads(250, seed=22), bench, log_every=0)
+    grid = tuner.collect(tuner.grid_workloads(), bench, log_every=0)
+    X, T, _ = tuner.dataset(train)
+    m = tuner.Ensemble(k=5)
+    m.train(X, T, epochs=300)
+    with tempfile.TemporaryDirectory() as d:
+        path = tuner.table_exhaustive(grid, os.path.join(d, "t.txt"))
+        assert gbk.lib.gbk_tuner_load(path.encode()) == 0
+        try:
+            rep = tuner.evaluate(m, held, table=True)
+        finally:
+            gbk.lib.gbk_tuner_clear()
+    print({k: (round(v, 4) if isinstance(v, float) else v) for k, v in rep.items() if k != "per_kind"})
+    assert rep["workloads"] == 250
+    mlp, dflt, table = (rep[f"{k}_mean_throughput_vs_best"] for k in ("mlp", "default", "table"))
+    assert mlp >= dflt + GAIN_DEFAULT, rep
+    assert mlp >= table + GAIN_TABLE, rep
+    assert rep["mlp_frac_within_5pct"] >= WITHIN_5PCT, rep
+    assert rep["mlp_frac_within_5pct"] > rep["table_frac_within_5pct"], rep
