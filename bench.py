@@ -54,12 +54,31 @@ STEP_BYTES = 3 * RED_BYTES + HIST_BYTES
 # The dominant kernel and its DRAM traffic per launch (dram__bytes_read.sum +
 # dram__bytes_write.sum from one ncu capture of the same launch, as recorded
 # in profiles/).
-ROOF_KERNEL = ("flat reduce of the box, MinLoc/MaxLoc/Sum f32 (with the autotuner table: k_reduce_flat load-pipelined "
-               "512 x 4, 2 CTAs/SM, for MinLoc and MaxLoc; k_reduce_tma shared-memory ring, 2 CTAs/SM, for Sum)")
-ROOF_TRAFFIC = 271620000  # MinLoc f32 over the box, load-pipelined kernel: 268.69 MB read + 2.93 MB written (ncu, MB precision)
+ROOF_KERNEL = "flat reduce of the box, MinLoc/MaxLoc/Sum f32"
+ROOF_TRAFFIC = 272140000  # MinLoc f32 over the box, ring kernel: 268.48 MB read + 3.66 MB written (ncu, MB precision)
 METRIC = "HBM GB/s (algorithmic bytes / step time) of MDRange reduce + ScatterView histogram"
 WORKLOAD = ("MDRange<Rank<3>> MinLoc+MaxLoc+Sum over LayoutLeft View<float***> 512x512x256 N(0,1) "
             "+ ScatterView histogram 2^26 int32 Zipf(1.1) keys -> 2^16 int64 bins")
+
+
+def launch_shapes(gbk, tuned):
+    """The kernel each operation of the step runs with (from the tuning table
+    when it is in use, else the library defaults)."""
+    import ctypes
+    out = {}
+    for name, op in (("MinLoc", 8), ("MaxLoc", 9), ("Sum", 0)):
+        t = gbk.Tuning()
+        if tuned and gbk.lib.gbk_tuner_lookup(0, op, 4, NX, 0, ctypes.byref(t)) == 0:
+            cps = f"{t.ctas_per_sm} CTAs/SM" if t.ctas_per_sm else "all resident CTAs"
+            out[name] = (f"k_reduce_flat load-pipelined {t.block} x {t.items_per_thread}, {cps}" if t.variant == 1
+                         else f"k_reduce_tma shared-memory ring, {cps}")
+        else:
+            out[name] = "k_reduce_tma shared-memory ring, all resident CTAs (default)"
+    t = gbk.Tuning()
+    hv = t.variant if tuned and gbk.lib.gbk_tuner_lookup(2, 0, 0, NKEYS, 16 * 8, ctypes.byref(t)) == 0 else 0
+    out["histogram"] = {0: "default (16-bit drain-free, multiply form)", 0x20: "k_hist16 with drains",
+                        0x80: "k_hist16 drain-free", 0x100: "k_hist16 drain-free, multiply form"}.get(hv, hex(hv))
+    return out
 
 
 def peaks():
@@ -764,7 +783,8 @@ def main():
         "config": {"workload": WORKLOAD, "step_bytes": STEP_BYTES, "l2": ("inputs 268 MB each > 129 MB L2, no flush in the step; MaxLoc and Sum re-read the view MinLoc "
                           "just read, so part of it can still be in L2 (ops_cold_l2: each op after a 256 MiB read)"),
                    "parallelism": f"replicas x{world}",
-                   "launch_config": "autotuner table" if tuned else "library defaults"},
+                   "launch_config": "autotuner table" if tuned else "library defaults",
+                   "kernels": launch_shapes(gbk, tuned)},
         "roofline": {"bound": "hbm", "kernel": ROOF_KERNEL,
                      "achieved": round(red_gbs, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(red_gbs / hbm, 4), "peak_kind": peak_kind + " hbm_gbs (burst copy)",

@@ -4,7 +4,8 @@
 // tile and a grid of at most the block size in CTAs).
 //
 // Here the box [lower, upper) of rank 1..6 is walked as one flat index space
-// on the skeleton kernels of Kokkos_GB300_Skeletons.hpp: the policy's inner
+// on the skeleton kernels of Kokkos_GB300_Skeletons.hpp (through their walk
+// protocol: each thread keeps its multi-index and steps it): the policy's inner
 // iteration direction is the fastest-varying dimension across consecutive
 // threads (Iterate::Left, the default on this space as on the CUDA space:
 // dimension 0 fastest, which coalesces LayoutLeft views; Iterate::Right:
@@ -48,58 +49,75 @@ inline TileSizeProperties get_tile_size_properties<Kokkos::Experimental::GB300>(
   return p;
 }
 
-// The box of an MDRangePolicy as the kernels see it: extents in walk order
-// (walk dimension 0 fastest) and, per walk dimension, the policy dimension it
-// stands for.
-template <int R, class Index>
+// The box of an MDRangePolicy as the kernels see it: lower bounds in policy
+// order, extents in walk order (walk dimension 0 fastest), and the CTA width
+// (kBlock) written in the mixed radix of the extents.  A thread turns its
+// first flat index into walk digits once (divisions), then steps by kBlock
+// with a mixed-radix add (an add, a compare and a conditional subtract per
+// dimension) instead of dividing for every element.
+template <int R>
 struct GB300Box {
-  Index lo[R];
-  Index ext[R];
-  int dim[R];  // walk order -> policy dimension
-  bool fits32;
+  int64_t lo[R];
+  int64_t ext[R];
+  int64_t step[R];
+  bool fits32;  // every flat index (and the walk's overshoot) below 2^31
+};
 
-  // index of the element at flat position f, in policy dimension order
-  __device__ __forceinline__ void point(int64_t f, Index (&i)[R]) const {
-    if (fits32) {
-      uint32_t r = (uint32_t)f;
+// Walk digits; LEFT: walk dimension d is policy dimension d, else R - 1 - d.
+template <int R, bool LEFT, class IT>
+struct GB300Walk {
+  IT d[R];
+  __device__ __forceinline__ void start(const GB300Box<R>& b, int64_t flat) {
+    IT r = (IT)flat;
 #pragma unroll
-      for (int d = 0; d < R - 1; ++d) {
-        const uint32_t e = (uint32_t)ext[d];
-        i[dim[d]] = lo[dim[d]] + (Index)(r % e);
-        r /= e;
-      }
-      i[dim[R - 1]] = lo[dim[R - 1]] + (Index)r;
-    } else {
-      int64_t r = f;
-#pragma unroll
-      for (int d = 0; d < R - 1; ++d) {
-        const int64_t e = (int64_t)ext[d];
-        i[dim[d]] = lo[dim[d]] + (Index)(r % e);
-        r /= e;
-      }
-      i[dim[R - 1]] = lo[dim[R - 1]] + (Index)r;
+    for (int k = 0; k < R - 1; ++k) {
+      const IT e = (IT)b.ext[k];
+      d[k] = r % e;
+      r /= e;
     }
+    d[R - 1] = r;
+  }
+  __device__ __forceinline__ void next(const GB300Box<R>& b) {
+    IT carry = 0;
+#pragma unroll
+    for (int k = 0; k < R - 1; ++k) {
+      const IT v = d[k] + (IT)b.step[k] + carry;
+      const IT e = (IT)b.ext[k];
+      carry = v >= e ? IT(1) : IT(0);
+      d[k] = carry ? v - e : v;
+    }
+    d[R - 1] += (IT)b.step[R - 1] + carry;
+  }
+  template <class Index>
+  __device__ __forceinline__ void point(const GB300Box<R>& b, Index (&i)[R]) const {
+#pragma unroll
+    for (int p = 0; p < R; ++p) i[p] = (Index)(b.lo[p] + (int64_t)d[LEFT ? p : R - 1 - p]);
   }
 };
 
 template <class MDPolicy, int R = MDPolicy::rank>
-GB300Box<R, typename MDPolicy::index_type> gb300_box(const MDPolicy& p, int64_t* total) {
-  using Index = typename MDPolicy::index_type;
-  GB300Box<R, Index> b{};
+GB300Box<R> gb300_box(const MDPolicy& p, int64_t* total) {
   // Left: dimension 0 fastest; Right: dimension R-1 fastest.  The outer
   // direction of the reference orders tiles, which a flat walk does not have;
   // the inner direction alone sets the element order here.
-  const bool left = MDPolicy::inner_direction == Iterate::Left;
+  constexpr bool left = MDPolicy::inner_direction == Iterate::Left;
+  GB300Box<R> b{};
   int64_t n = 1;
   for (int d = 0; d < R; ++d) {
     const int pd = left ? d : R - 1 - d;
-    b.dim[d] = pd;
-    b.lo[pd] = (Index)p.m_lower[pd];
+    b.lo[d] = (int64_t)p.m_lower[d];
     const int64_t e = (int64_t)p.m_upper[pd] - (int64_t)p.m_lower[pd];
-    b.ext[d] = (Index)(e > 0 ? e : 0);
+    b.ext[d] = e > 0 ? e : 0;
     n *= (e > 0 ? e : 0);
   }
-  b.fits32 = n < (int64_t(1) << 31);
+  int64_t r = gbk_skel::kBlock;
+  for (int d = 0; d < R - 1; ++d) {
+    const int64_t e = b.ext[d] > 0 ? b.ext[d] : 1;
+    b.step[d] = r % e;
+    r /= e;
+  }
+  b.step[R - 1] = r;
+  b.fits32 = n + 2 * gbk_skel::kUnroll * gbk_skel::kBlock < (int64_t(1) << 31);
   *total = n;
   return b;
 }
@@ -129,12 +147,17 @@ class ParallelFor<FunctorType, Kokkos::MDRangePolicy<Traits...>, Kokkos::Experim
   const Policy m_policy;
 
  public:
+  static constexpr bool kLeft = Policy::inner_direction == Iterate::Left;
+  template <class IT>
   struct Closure {
     FunctorType f;
-    GB300Box<R, Index> box;
-    __device__ void exec(int64_t flat) const {
+    GB300Box<R> box;
+    using walk_state = GB300Walk<R, kLeft, IT>;
+    __device__ void walk_start(walk_state& w, int64_t flat) const { w.start(box, flat); }
+    __device__ void walk_next(walk_state& w) const { w.next(box); }
+    __device__ void walk_exec(const walk_state& w) const {
       Index i[R];
-      box.point(flat, i);
+      w.point(box, i);
       gb300_md_call<WorkTag, R>(f, i);
     }
   };
@@ -155,8 +178,12 @@ class ParallelFor<FunctorType, Kokkos::MDRangePolicy<Traits...>, Kokkos::Experim
     const auto& exec = m_policy.space();
     const int64_t g = gb300_grid(exec, n);
     int* err = gb300_scratch(exec, 0).err;
-    gbk_skel::k_for<Closure><<<(unsigned)g, gbk_skel::kBlock, 0, exec.stream()>>>(Closure{m_functor, box}, 0, n,
-                                                                                   err);
+    if (box.fits32)
+      gbk_skel::k_for<Closure<int32_t>>
+          <<<(unsigned)g, gbk_skel::kBlock, 0, exec.stream()>>>(Closure<int32_t>{m_functor, box}, 0, n, err);
+    else
+      gbk_skel::k_for<Closure<int64_t>>
+          <<<(unsigned)g, gbk_skel::kBlock, 0, exec.stream()>>>(Closure<int64_t>{m_functor, box}, 0, n, err);
     gb300_launched("parallel_for(MDRangePolicy)");
   }
 };
@@ -183,12 +210,17 @@ class ParallelReduce<CombinedFunctorReducerType, Kokkos::MDRangePolicy<Traits...
   const bool m_result_ptr_device_accessible;
 
  public:
+  static constexpr bool kLeft = Policy::inner_direction == Iterate::Left;
+  template <class IT>
   struct Closure : GB300ValueOps<ReducerType> {
     FunctorType f;
-    GB300Box<R, Index> box;
-    __device__ void exec(int64_t flat, void* v) const {
+    GB300Box<R> box;
+    using walk_state = GB300Walk<R, kLeft, IT>;
+    __device__ void walk_start(walk_state& w, int64_t flat) const { w.start(box, flat); }
+    __device__ void walk_next(walk_state& w) const { w.next(box); }
+    __device__ void walk_exec(const walk_state& w, void* v) const {
       Index i[R];
-      box.point(flat, i);
+      w.point(box, i);
       gb300_md_call<WorkTag, R>(f, i, this->r.reference(static_cast<pointer_type>(v)));
     }
   };
@@ -215,11 +247,21 @@ class ParallelReduce<CombinedFunctorReducerType, Kokkos::MDRangePolicy<Traits...
     const auto box = gb300_box<Policy>(m_policy, &n);
     const auto& exec = m_policy.space();
     const int64_t g = gb300_grid(exec, n > 0 ? n : 1);
-    Closure c{{m_functor_reducer.get_reducer()}, m_functor_reducer.get_functor(), box};
     gb300_run_reduce<VB>(exec, m_functor_reducer.get_reducer(), g, m_result_ptr, m_result_ptr_device_accessible,
                          [&](gbk_skel::Val<VB>* part, unsigned* ctr, gbk_skel::Val<VB>* out, int* err) {
-                           gbk_skel::k_reduce<VB, Closure><<<(unsigned)g, gbk_skel::kBlock, 0, exec.stream()>>>(
-                               c, 0, n > 0 ? n : 0, part, ctr, out, err);
+                           if (box.fits32) {
+                             Closure<int32_t> c{{m_functor_reducer.get_reducer()}, m_functor_reducer.get_functor(),
+                                                box};
+                             gbk_skel::k_reduce<VB, Closure<int32_t>>
+                                 <<<(unsigned)g, gbk_skel::kBlock, 0, exec.stream()>>>(c, 0, n > 0 ? n : 0, part,
+                                                                                       ctr, out, err);
+                           } else {
+                             Closure<int64_t> c{{m_functor_reducer.get_reducer()}, m_functor_reducer.get_functor(),
+                                                box};
+                             gbk_skel::k_reduce<VB, Closure<int64_t>>
+                                 <<<(unsigned)g, gbk_skel::kBlock, 0, exec.stream()>>>(c, 0, n > 0 ? n : 0, part,
+                                                                                       ctr, out, err);
+                           }
                          });
   }
 };

@@ -465,10 +465,21 @@ struct ThreadVectorRangeBoundariesStruct<iType, GB300TeamMember> {
       : start(b), end(e) {}
 };
 
-// Team-strided walk of [start, end): thread r takes start + r, + team_size, ...
+// Team-strided walk of [start, end): thread r takes start + r, + team_size,
+// ..., eight of them per loop trip so that eight loads of the closure are in
+// flight (calls stay in increasing index order per thread).
 template <class B, class F>
 __device__ __forceinline__ void gb300_team_walk(const B& b, const F& f) {
-  for (auto i = b.start + (decltype(b.start))threadIdx.x; i < b.end; i += (decltype(b.start))blockDim.x) f(i);
+  using I = std::remove_cv_t<decltype(b.start)>;
+  constexpr int U = 8;
+  const I step = (I)blockDim.x;
+  I i = b.start + (I)threadIdx.x;
+  if (i >= b.end) return;
+  for (; (b.end - i) > (I)(U - 1) * step; i += (I)U * step) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) f(i + (I)u * step);
+  }
+  for (; i < b.end; i += step) f(i);
 }
 
 }  // namespace Impl

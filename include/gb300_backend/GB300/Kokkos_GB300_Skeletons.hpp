@@ -42,6 +42,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
+#include <type_traits>
 
 #include "../../gbk.h"
 
@@ -210,16 +211,44 @@ __device__ Val<VB> cta_reduce_any(const C& c, Val<VB> v) {
 }
 
 // ---- parallel_for ---------------------------------------------------------
+// A closure may walk its index space itself: with a nested walk_state type it
+// provides walk_start(state, flat), walk_exec(state[, value]) and
+// walk_next(state), the last stepping by kBlock flat indices; the loops
+// below then use those instead of exec(flat) (the MDRange closures keep
+// their multi-index instead of dividing for every element).
+template <class C, class = void>
+struct has_walk : std::false_type {};
+template <class C>
+struct has_walk<C, std::void_t<typename C::walk_state>> : std::true_type {};
+
 template <class C>
 __global__ void __launch_bounds__(kBlock) k_for(const C c, int64_t begin, int64_t n, int* err) {
   int64_t c0, c1;
   cta_share(n, &c0, &c1);
   int64_t i = c0 + threadIdx.x;
-  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+  if constexpr (has_walk<C>::value) {
+    if (i < c1) {
+      typename C::walk_state w;
+      c.walk_start(w, begin + i);
+      for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) c.exec(begin + i + u * kBlock);
+        for (int u = 0; u < kUnroll; ++u) {
+          c.walk_exec(w);
+          c.walk_next(w);
+        }
+      }
+      for (; i < c1; i += kBlock) {
+        c.walk_exec(w);
+        c.walk_next(w);
+      }
+    }
+  } else {
+    for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) c.exec(begin + i + u * kBlock);
+    }
+    for (; i < c1; i += kBlock) c.exec(begin + i);
   }
-  for (; i < c1; i += kBlock) c.exec(begin + i);
   report_abort(err);
 }
 
@@ -234,11 +263,29 @@ __global__ void __launch_bounds__(kBlock)
   int64_t c0, c1;
   cta_share(n, &c0, &c1);
   int64_t i = c0 + threadIdx.x;
-  for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+  if constexpr (has_walk<C>::value) {
+    if (i < c1) {
+      typename C::walk_state w;
+      c.walk_start(w, begin + i);
+      for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) c.exec(begin + i + u * kBlock, &v);
+        for (int u = 0; u < kUnroll; ++u) {
+          c.walk_exec(w, &v);
+          c.walk_next(w);
+        }
+      }
+      for (; i < c1; i += kBlock) {
+        c.walk_exec(w, &v);
+        c.walk_next(w);
+      }
+    }
+  } else {
+    for (; i + (kUnroll - 1) * kBlock < c1; i += kUnroll * kBlock) {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) c.exec(begin + i + u * kBlock, &v);
+    }
+    for (; i < c1; i += kBlock) c.exec(begin + i, &v);
   }
-  for (; i < c1; i += kBlock) c.exec(begin + i, &v);
   v = cta_reduce<VB>(c, v);
   report_abort(err);
   __shared__ unsigned s_ticket;

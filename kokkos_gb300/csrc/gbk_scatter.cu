@@ -114,26 +114,36 @@ __global__ void __launch_bounds__(BLOCK)
 // word, 2^16 bins in 128 KiB).  Word i holds bins i (low half) and
 // i + nwords (high half): bins next to each other land in different words,
 // so the few hot bins of a skewed key distribution (Zipf: bins 0, 1, 2, ...)
-// do not also collide on one word with their neighbours.  The CTA walks its contiguous share of the
-// keys in rounds of BLOCK*8 keys; after every DRAIN rounds (at most 32768
-// keys, so no half-word can pass 0xFFFF from below 0x8000) all threads sync
-// and every half-word that reached 0x8000 gives 0x8000 to the global bin.
-// Overflow is therefore impossible and no carry ever reaches the
-// neighbouring bin.  Keys for the next round are loaded before the current
-// round is counted, so two rounds of loads are in flight.
+// do not also collide on one word with their neighbours.  The CTA walks its
+// contiguous share of the keys in rounds of BLOCK*8 keys; keys for the next
+// round are loaded before the current round is counted, so two rounds of
+// loads are in flight.  Overflow handling, by MODE:
 //
-// NODRAIN: no periodic drains.  Each increment reads the counter's old value
-// (the shared atomic returns it); the one increment that takes a 16-bit
-// counter from 0x7FFF to 0x8000 moves 0x8000 to the global bin itself (a
-// shared atomic subtract and a global red.add).  Until that subtract lands,
-// other increments can raise the counter by less than the 0x7FFF headroom
-// left (far fewer increments are in flight in one CTA), so no carry reaches
-// the neighbouring bin.
+// MODE 0 (drains): after every DRAIN rounds (at most 32768 keys, so no
+// half-word can pass 0xFFFF from below 0x8000) all threads sync and every
+// half-word that reached 0x8000 gives 0x8000 to the global bin.  Overflow is
+// therefore impossible and no carry ever reaches the neighbouring bin.
+//
+// MODE 1 (drain-free): each increment reads the counter's old value (the
+// shared atomic returns it); the one increment that takes a 16-bit counter
+// from 0x7FFF to 0x8000 moves 0x8000 to the global bin itself (a shared
+// atomic subtract and a global red.add).  Until that subtract lands, other
+// increments can raise the counter by less than the 0x7FFF headroom left
+// (far fewer increments are in flight in one CTA), so no carry reaches the
+// neighbouring bin.
+//
+// MODE 2 (drain-free, power-of-two bin counts): MODE 1 with the per-key
+// arithmetic as multiplies (see the loop).  Measured on GB300 with ncu, the
+// general form is bound by the ALU pipe (math-pipe-throttle stalls, about 27
+// warp instructions per 32 keys, shared-memory wavefronts at half their
+// peak); moving the work to the multiply pipe took 2^26 keys into 2^16 bins
+// from 66.5 to 61.4 us (Zipf 1.1) and from 70.1 to 64.7 us (uniform).
 template <int BLOCK, bool AGG, int MODE>
 __global__ void __launch_bounds__(BLOCK, 1)
-    k_hist16(const int32_t* __restrict__ keys, int64_t nvec, int64_t nbins, unsigned long long* bins, int* err) {
+    k_hist16(const int32_t* __restrict__ keys, int64_t nvec, int64_t nbins, unsigned long long* bins, int* err,
+             unsigned mulw, unsigned cffff, unsigned c7fff) {
   extern __shared__ __align__(16) unsigned sh[];
-  constexpr int VPT = 2;                       // vectors (4 keys each) per thread per round
+  constexpr int VPT = MODE == 3 ? 4 : 2;       // vectors (4 keys each) per thread per round
   constexpr int ROUND = BLOCK * VPT;           // vectors per round
   constexpr int DRAIN = 32768 / (ROUND * 4);   // rounds between drains
   static_assert(DRAIN >= 1, "round too large for 16-bit counters");
@@ -216,35 +226,37 @@ __global__ void __launch_bounds__(BLOCK, 1)
       const int64_t q = vn + (int64_t)j * BLOCK + threadIdx.x;
       nxt[j].u = q < v1 ? ld_stream16(keys + 4 * q) : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
     }
-    if constexpr (MODE == 2 && !AGG) {
-      // All 4 x VPT shared atomics of the round are issued before any of
-      // their old values is tested, so they are in flight together; the one
-      // thread whose increment took a half from 0x7FFF to 0x8000 moves 0x8000
-      // to the global bin afterwards (others may have counted past 0x8000 in
-      // between: the half has 0x8000 of headroom).  Vectors past the share
-      // add 0 to the spare word.
-      unsigned o[VPT][4], wd[VPT][4], hs[VPT][4];
+    if constexpr ((MODE == 2 || MODE == 3) && !AGG) {
+      // Power-of-two bins: the word, the half and the increment come from
+      // multiplies (hi = key >> log2(nwords) as a high multiply by mulw; word
+      // = key - hi * nwords; increment 1 or 0x10000 = 1 + hi * 0xFFFF) and the
+      // crossing test is one masked compare, so a key costs few ALU-pipe
+      // instructions (the ALU pipe bounds the general form).  The constants
+      // arrive as kernel arguments so that they stay multiplies.  A vector
+      // with any key outside the bins takes the general path.
 #pragma unroll
       for (int j = 0; j < VPT; ++j) {
-        const bool in = v + (int64_t)j * BLOCK + threadIdx.x < v1;
+        const int64_t q = v + (int64_t)j * BLOCK + threadIdx.x;
+        if (q < v1) {
+          const unsigned k0 = (unsigned)cur[j].v[0], k1 = (unsigned)cur[j].v[1];
+          const unsigned k2 = (unsigned)cur[j].v[2], k3 = (unsigned)cur[j].v[3];
+          const unsigned mx = max(__vimax3_u32(k0, k1, k2), k3);
+          if (mx < nb32) {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const unsigned uk = (unsigned)cur[j].v[e];
-          const bool ok = uk < nb32;
-          bad = bad || (in && !ok);
-          const unsigned hi = uk >= nw32 ? 16u : 0u;
-          wd[j][e] = ok ? uk - (hi ? nw32 : 0u) : nw32;
-          hs[j][e] = (ok && in) ? hi : 32u;  // 32: nothing counted, nothing to test
-          o[j][e] = atomicAdd(sh + wd[j][e], (ok && in) ? 1u << hi : 0u);
-        }
-      }
+            for (int e = 0; e < 4; ++e) {
+              const unsigned uk = (unsigned)cur[j].v[e];
+              const unsigned hi = __umulhi(uk, mulw);
+              const unsigned word = uk - hi * nw32;
+              const unsigned inc = 1u + hi * cffff;
+              const unsigned old = atomicAdd(sh + word, inc);
+              if (((old & (inc * cffff)) ^ (inc * c7fff)) == 0u) {
+                atomicSub(sh + word, inc << 15);
+                red_add_u64(bins + word + hi * nw32, 0x8000ull);
+              }
+            }
+          } else {
 #pragma unroll
-      for (int j = 0; j < VPT; ++j) {
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          if (hs[j][e] < 32u && ((o[j][e] >> hs[j][e]) & 0xFFFFu) == 0x7FFFu) {
-            atomicSub(sh + wd[j][e], 0x8000u << hs[j][e]);
-            red_add_u64(bins + (hs[j][e] ? nw32 + wd[j][e] : wd[j][e]), 0x8000ull);
+            for (int e = 0; e < 4; ++e) count(cur[j].v[e]);
           }
         }
       }
@@ -307,8 +319,10 @@ int launch_hist16(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, 
     int64_t grid = sm_count();
     const int64_t need = (nvec + BLOCK * 2 - 1) / (BLOCK * 2);
     if (grid > need) grid = need;
+    // MODE 2 needs a power-of-two bin count of at least 4 (mulw = 2^32 / nwords)
+    const unsigned mulw = MODE >= 2 ? (unsigned)((1ull << 32) / (uint64_t)((nbins + 1) >> 1)) : 0u;
     GBK_CUDA_TRY(launch_pdl(kfn, dim3((unsigned)grid), dim3(BLOCK), smem, w->stream, keys + head, nvec, nbins,
-                            (unsigned long long*)bins, w->err));
+                            (unsigned long long*)bins, w->err, mulw, 0xFFFFu, 0x7FFFu));
     note_launch();
   }
   return cuda_status(cudaGetLastError());
@@ -372,7 +386,7 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   // variant bits: 0x0F cluster size of the 32-bit privatised kernel (1, 2,
   // 4, 8); 0x10 warp aggregation; 0x20 the 16-bit one-CTA-per-SM kernel;
   // 0x40 no privatisation; 0x80 the 16-bit kernel without drains; 0x100
-  // the same with each round's atomics issued before their tests.
+  // the same in its multiply form for power-of-two bin counts.
   // 0 = automatic choice.
   const int var = t ? t->variant : 0;
   int cl = var & 0xF;
@@ -383,10 +397,17 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   const bool force_global = (var & 0x40) != 0;
   if (var == 0) {
     if (nbins * 4 <= 96 * 1024) cl = 1;
-    else if ((nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, 1>(keys, n, nbins, bins, w);
+    else if ((nbins + 1) / 2 * 4 <= max_smem) {
+      const bool pow2 = (nbins & (nbins - 1)) == 0;  // nbins > 24576 here
+      return pow2 ? launch_hist16<false, 2>(keys, n, nbins, bins, w) : launch_hist16<false, 1>(keys, n, nbins, bins, w);
+    }
     else { cl = 2; while (cl <= 8 && (nbins + cl - 1) / cl * 4 > max_smem) cl *= 2; }
   }
-  if ((var & 0x100) && (nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, 2>(keys, n, nbins, bins, w);
+  if ((var & 0x100) && (nbins + 1) / 2 * 4 <= max_smem) {
+    const bool pow2 = nbins >= 4 && (nbins & (nbins - 1)) == 0;
+    if (pow2 && (var & 0x200)) return launch_hist16<false, 3>(keys, n, nbins, bins, w);
+    return pow2 ? launch_hist16<false, 2>(keys, n, nbins, bins, w) : launch_hist16<false, 1>(keys, n, nbins, bins, w);
+  }
   if ((var & 0x80) && (nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, 1>(keys, n, nbins, bins, w);
   if (use16 && !force_global && (nbins + 1) / 2 * 4 <= max_smem) {
     return agg ? launch_hist16<true, 0>(keys, n, nbins, bins, w) : launch_hist16<false, 0>(keys, n, nbins, bins, w);

@@ -1,0 +1,156 @@
+// Throughput of the reference's own Kokkos API on the GB300 execution space
+// (the backend in include/gb300_backend, built by tests/backend/Makefile):
+// plain Kokkos user code, timed with CUDA events on the instance's stream
+// after 3 warm-up calls, inputs alternating over two copies of at least
+// 128 MiB each (a call starts with most of its input out of the 129 MB L2).
+// Prints one JSON line.
+//   range_sum_f64:   parallel_reduce(RangePolicy<GB300>(0, 2^24), x(i) summed)
+//                    into a host double and into a device View
+//   mdrange_sum_f32: parallel_reduce(MDRangePolicy<GB300, Rank<3>> over a
+//                    LayoutLeft 512x512x256 float View, Sum into a View)
+//   team_sum_f32:    TeamPolicy<GB300>(segments, 256), TeamThreadRange reduce
+//                    per league rank over the lognormal segments whose int64
+//                    offsets are in argv[1], single(PerTeam) store
+//   scatter_hist:    ScatterView (defaults: non-duplicated, atomic) histogram
+//                    of 2^26 int32 keys (x * 2654435761 mod 2^16) into 2^16
+//                    int64 bins, contribute
+//   sort_u64:        Kokkos::sort of 2^27 uint64 keys (refilled each call)
+//   backend_bench <offsets.bin> <nseg> <reps>
+#include <Kokkos_Core.hpp>
+#include <Kokkos_ScatterView.hpp>
+#include <Kokkos_Sort.hpp>
+
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+using ES = Kokkos::Experimental::GB300;
+using MS = Kokkos::Experimental::GB300Space;
+
+template <class F>
+static double time_us(const ES& ex, int reps, F&& f) {
+  for (int r = 0; r < 3; ++r) f(r);
+  ex.fence();
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, ex.stream());
+  for (int r = 0; r < reps; ++r) f(r);
+  cudaEventRecord(b, ex.stream());
+  cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return 1000.0 * ms / reps;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 4) return 1;
+  const int64_t nseg = std::atoll(argv[2]);
+  const int reps = std::atoi(argv[3]);
+  std::vector<int64_t> offs(nseg + 1);
+  FILE* fo = std::fopen(argv[1], "rb");
+  if (!fo || std::fread(offs.data(), 8, offs.size(), fo) != offs.size()) return 2;
+  std::fclose(fo);
+  Kokkos::initialize(argc, argv);
+  {
+    ES ex;
+    auto gbs = [](double bytes, double us) { return bytes / (us * 1e-6) / 1e9; };
+    // ---- RangePolicy Sum over 2^24 doubles -------------------------------
+    const int64_t n = 1 << 24;
+    Kokkos::View<double*, MS> x0("x0", n), x1("x1", n);
+    Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, n), KOKKOS_LAMBDA(int64_t i) {
+      x0(i) = (double)((i * 2654435761u) % 1000) * 1e-3;
+      x1(i) = (double)((i * 40503u) % 1000) * 1e-3;
+    });
+    double hsum = 0;
+    const double t_range_host = time_us(ex, reps, [&](int r) {
+      auto x = (r & 1) ? x1 : x0;
+      Kokkos::parallel_reduce(Kokkos::RangePolicy<ES>(ex, 0, n), KOKKOS_LAMBDA(int64_t i, double& u) { u += x(i); },
+                              hsum);
+    });
+    Kokkos::View<double, MS> dsum("dsum");
+    const double t_range_dev = time_us(ex, reps, [&](int r) {
+      auto x = (r & 1) ? x1 : x0;
+      Kokkos::parallel_reduce(Kokkos::RangePolicy<ES>(ex, 0, n), KOKKOS_LAMBDA(int64_t i, double& u) { u += x(i); },
+                              dsum);
+    });
+    // ---- MDRange Sum over a 512x512x256 float box --------------------------
+    const int64_t n0 = 512, n1 = 512, n2 = 256;
+    Kokkos::View<float***, Kokkos::LayoutLeft, MS> b0("b0", n0, n1, n2), b1("b1", n0, n1, n2);
+    using MD = Kokkos::MDRangePolicy<ES, Kokkos::Rank<3>>;
+    Kokkos::parallel_for(MD(ex, {0, 0, 0}, {n0, n1, n2}), KOKKOS_LAMBDA(int64_t i, int64_t j, int64_t k) {
+      b0(i, j, k) = (float)((i + j + k) % 7);
+      b1(i, j, k) = (float)((i * 3 + j + k) % 5);
+    });
+    Kokkos::View<float, MS> fsum("fsum");
+    const double t_md = time_us(ex, reps, [&](int r) {
+      auto b = (r & 1) ? b1 : b0;
+      Kokkos::parallel_reduce(MD(ex, {0, 0, 0}, {n0, n1, n2}),
+                              KOKKOS_LAMBDA(int64_t i, int64_t j, int64_t k, float& u) { u += b(i, j, k); }, fsum);
+    });
+    // ---- TeamPolicy league reduce over lognormal segments ------------------
+    const int64_t ns = offs[nseg];
+    Kokkos::View<int64_t*, MS> doff("doff", nseg + 1);
+    Kokkos::View<int64_t*, Kokkos::HostSpace> hoff(offs.data(), nseg + 1);
+    Kokkos::deep_copy(ex, doff, hoff);
+    Kokkos::View<float*, MS> v("v", ns), segs("segs", nseg);
+    Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, ns), KOKKOS_LAMBDA(int64_t i) { v(i) = (float)(i % 11); });
+    using TP = Kokkos::TeamPolicy<ES>;
+    const double t_team = time_us(ex, reps, [&](int) {
+      Kokkos::parallel_for(TP(ex, (int)nseg, 256), KOKKOS_LAMBDA(const TP::member_type& t) {
+        const int64_t sg = t.league_rank();
+        float u = 0;
+        Kokkos::parallel_reduce(Kokkos::TeamThreadRange(t, doff(sg), doff(sg + 1)),
+                                [&](int64_t i, float& w) { w += v(i); }, u);
+        Kokkos::single(Kokkos::PerTeam(t), [&]() { segs(sg) = u; });
+      });
+    });
+    // ---- ScatterView histogram -------------------------------------------
+    const int64_t nk = 1 << 26, nb = 1 << 16;
+    Kokkos::View<int32_t*, MS> keys("keys", nk);
+    Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, nk), KOKKOS_LAMBDA(int64_t i) {
+      keys(i) = (int32_t)(((uint64_t)i * 2654435761ull) & (uint64_t)(nb - 1));
+    });
+    Kokkos::View<int64_t*, MS> bins("bins", nb);
+    const double t_hist = time_us(ex, reps, [&](int) {
+      auto sv = Kokkos::Experimental::create_scatter_view(bins);
+      Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, nk), KOKKOS_LAMBDA(int64_t i) {
+        auto a = sv.access();
+        a(keys(i)) += 1;
+      });
+      Kokkos::Experimental::contribute(bins, sv);
+    });
+    // ---- Kokkos::sort of 2^27 uint64 keys -----------------------------------
+    const int64_t nsort = 1 << 27;
+    Kokkos::View<uint64_t*, MS> sk("sk", nsort);
+    auto fill = [&](int r) {
+      Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, nsort), KOKKOS_LAMBDA(int64_t i) {
+        uint64_t z = (uint64_t)i + 0x9E3779B97F4A7C15ull * (uint64_t)(r + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        sk(i) = z ^ (z >> 31);
+      });
+    };
+    const double t_fill = time_us(ex, 3, fill);
+    const double t_sort_fill = time_us(ex, 3, [&](int r) {
+      fill(r);
+      Kokkos::sort(ex, sk);
+    });
+    ex.fence();
+    const double rb = (double)n * 8, mb = (double)n0 * n1 * n2 * 4, tb = (double)ns * 4 + (nseg + 1) * 8.0 + nseg * 4.0;
+    const double hb = (double)nk * 4 + nb * 8.0;
+    std::printf(
+        "{\"range_sum_f64_2^24\": {\"host_result_us\": %.2f, \"view_result_us\": %.2f, \"GB/s\": %.1f}, "
+        "\"mdrange_sum_f32_512x512x256\": {\"us\": %.2f, \"GB/s\": %.1f}, "
+        "\"team_sum_f32_lognormal_segments\": {\"segments\": %lld, \"elements\": %lld, \"us\": %.2f, \"GB/s\": %.1f}, "
+        "\"scatterview_hist_2^26_keys_2^16_bins\": {\"us\": %.2f, \"GB/s\": %.1f}, "
+        "\"sort_u64_2^27\": {\"ms\": %.3f, \"Gkeys_per_s\": %.2f}}\n",
+        t_range_host, t_range_dev, gbs(rb, t_range_dev), t_md, gbs(mb, t_md), (long long)nseg, (long long)ns, t_team,
+        gbs(tb, t_team), t_hist, gbs(hb, t_hist), (t_sort_fill - t_fill) / 1000.0,
+        (double)nsort / ((t_sort_fill - t_fill) * 1e-6) / 1e9);
+  }
+  Kokkos::finalize();
+  return 0;
+}

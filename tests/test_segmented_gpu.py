@@ -193,13 +193,24 @@ def test_c3_batched_full_size(env):
 
 def test_graph_chain_of_dependent_nodes(env):
     """A CUDA graph of 8 dependent reduce/scan nodes (each node reads the
-    previous node's output) replays to the same results as the stream
-    launches, several times, interleaved with uncaptured scans."""
+    previous node's output) replays to the results of the oracle (the
+    reference's OpenMP scan and reduce restated, int64 arithmetic wrapping
+    as two's complement in both) and of the same chain as stream launches,
+    several times, interleaved with uncaptured scans."""
     gbk, torch = env
+    import oracle
     from kokkos_gb300 import datagen
     s = torch.cuda.Stream()
     n = 1 << 20
-    x = _dev(torch, datagen.uniform_i32(n, 0, 15, seed=1))
+    xh = datagen.uniform_i32(n, 0, 15, seed=1)
+    x = _dev(torch, xh)
+    o0 = oracle.scan(xh, np.int64, inclusive=False, init=0, nthreads=4)
+    o1 = oracle.scan(o0, np.int64, inclusive=True, nthreads=4)
+    o2 = oracle.scan(o1, np.int64, inclusive=False, init=3, nthreads=4)
+    o3 = oracle.scan(o2, np.int64, inclusive=True, nthreads=4)
+    want_oracle = b"".join(np.asarray(r).tobytes() for r in (
+        oracle.reduce("max", o0, 4), oracle.reduce("sum", o1, 4), oracle.reduce("minloc", o2[1:], 4),
+        oracle.reduce("maxloc", o3, 4)))
     bufs = [torch.empty(n, dtype=torch.int64, device="cuda") for _ in range(4)]
     res = torch.zeros(64, dtype=torch.uint8, device="cuda")
     gbk.lib.gbk_workspace_reserve(__import__("ctypes").c_void_p(s.cuda_stream), 64 << 20)
@@ -218,6 +229,8 @@ def test_graph_chain_of_dependent_nodes(env):
         chain()
     s.synchronize()
     want = (res.cpu().numpy().copy(), bufs[3].cpu().numpy().copy())
+    assert want[0][:48].tobytes() == want_oracle
+    np.testing.assert_array_equal(want[1], o3)
     g = gbk.Graph(s)
     with g:
         chain()

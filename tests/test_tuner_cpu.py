@@ -46,9 +46,11 @@ def test_new_candidate_families():
     h = {"kind": tuner.KIND_HIST, "dtype": 0, "n": 1 << 24, "nbins": 65536}
     cs = tuner.candidates(h)
     c = cs[tuner.default_cfg_index(h, cs)]
-    assert (c["variant"], c["cps"]) == (0x80, 1)  # 65536 bins: the drain-free 16-bit kernel
+    assert (c["variant"], c["cps"]) == (0x100, 1)  # 65536 bins: the drain-free 16-bit kernel, multiply form
     f = tuner.features(h, c)
-    assert f[22] == 1 and f[26] == 1
+    assert f[22] == 1 and f[26] == 2
+    f80 = tuner.features(h, next(x for x in cs if x["variant"] == 0x80))
+    assert f80[22] == 1 and f80[26] == 1
     f20 = tuner.features(h, next(x for x in cs if x["variant"] == 0x20))
     assert f20[22] == 1 and f20[26] == 0
     small = {"kind": tuner.KIND_HIST, "dtype": 0, "n": 1 << 24, "nbins": 4096}
