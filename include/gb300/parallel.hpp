@@ -562,16 +562,23 @@ void parallel_reduce(const std::string& label, N n, const F& f, A0&& a0, A1&& a1
 // (host-device because they are called from KOKKOS_LAMBDA bodies; they only
 // do work in device code)
 // A team thread takes indices team_rank, team_rank + team_size, ... of the
-// range, kTeamUnroll of them per loop trip so that as many loads of the
-// functor are in flight (calls stay in increasing index order per thread).
-constexpr int kTeamUnroll = 8;
+// range, 32 of them per loop trip while that many remain, then 8, then one
+// at a time, so that up to 32 loads of the functor are in flight (calls
+// stay in increasing index order per thread).  One team per league rank
+// makes the longest range the league's tail: one CTA streams it alone, and
+// its rate is the bytes it keeps in flight.
+template <int U, class F, class... A>
+__device__ __forceinline__ void team_range_steps(int64_t& i, int64_t e, int64_t step, const F& f, A&... a) {
+  for (; i + (U - 1) * step < e; i += U * step) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) f(i + u * step, a...);
+  }
+}
 template <class F, class... A>
 __device__ __forceinline__ void team_range_walk(int64_t b, int64_t e, int64_t step, const F& f, A&... a) {
   int64_t i = b;
-  for (; i + (kTeamUnroll - 1) * step < e; i += kTeamUnroll * step) {
-#pragma unroll
-    for (int u = 0; u < kTeamUnroll; ++u) f(i + u * step, a...);
-  }
+  team_range_steps<32>(i, e, step, f, a...);
+  team_range_steps<8>(i, e, step, f, a...);
   for (; i < e; i += step) f(i, a...);
 }
 template <class F>

@@ -466,19 +466,25 @@ struct ThreadVectorRangeBoundariesStruct<iType, GB300TeamMember> {
 };
 
 // Team-strided walk of [start, end): thread r takes start + r, + team_size,
-// ..., eight of them per loop trip so that eight loads of the closure are in
-// flight (calls stay in increasing index order per thread).
-template <class B, class F>
-__device__ __forceinline__ void gb300_team_walk(const B& b, const F& f) {
-  using I = std::remove_cv_t<decltype(b.start)>;
-  constexpr int U = 8;
-  const I step = (I)blockDim.x;
-  I i = b.start + (I)threadIdx.x;
-  if (i >= b.end) return;
-  for (; (b.end - i) > (I)(U - 1) * step; i += (I)U * step) {
+// ..., 32 of them per loop trip while that many remain, then 8, then one at
+// a time, so that up to 32 loads of the closure are in flight (calls stay in
+// increasing index order per thread).  With one team per league rank the
+// longest range is the league's tail, streamed by one CTA at the rate of
+// the bytes it keeps in flight.
+template <int U, class I, class F>
+__device__ __forceinline__ void gb300_team_steps(I& i, I end, I step, const F& f) {
+  for (; i < end && (end - i) > (I)(U - 1) * step; i += (I)U * step) {
 #pragma unroll
     for (int u = 0; u < U; ++u) f(i + (I)u * step);
   }
+}
+template <class B, class F>
+__device__ __forceinline__ void gb300_team_walk(const B& b, const F& f) {
+  using I = std::remove_cv_t<decltype(b.start)>;
+  const I step = (I)blockDim.x;
+  I i = b.start + (I)threadIdx.x;
+  gb300_team_steps<32>(i, (I)b.end, step, f);
+  gb300_team_steps<8>(i, (I)b.end, step, f);
   for (; i < b.end; i += step) f(i);
 }
 

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(BLOCK, 1)
     k_hist16(const int32_t* __restrict__ keys, int64_t nvec, int64_t nbins, unsigned long long* bins, int* err,
              unsigned mulw, unsigned cffff, unsigned c7fff) {
   extern __shared__ __align__(16) unsigned sh[];
-  constexpr int VPT = MODE == 3 ? 4 : 2;       // vectors (4 keys each) per thread per round
+  constexpr int VPT = 2;                       // vectors (4 keys each) per thread per round (4: slower)
   constexpr int ROUND = BLOCK * VPT;           // vectors per round
   constexpr int DRAIN = 32768 / (ROUND * 4);   // rounds between drains
   static_assert(DRAIN >= 1, "round too large for 16-bit counters");
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(BLOCK, 1)
       const int64_t q = vn + (int64_t)j * BLOCK + threadIdx.x;
       nxt[j].u = q < v1 ? ld_stream16(keys + 4 * q) : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
     }
-    if constexpr ((MODE == 2 || MODE == 3) && !AGG) {
+    if constexpr (MODE == 2 && !AGG) {
       // Power-of-two bins: the word, the half and the increment come from
       // multiplies (hi = key >> log2(nwords) as a high multiply by mulw; word
       // = key - hi * nwords; increment 1 or 0x10000 = 1 + hi * 0xFFFF) and the
@@ -320,7 +320,7 @@ int launch_hist16(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, 
     const int64_t need = (nvec + BLOCK * 2 - 1) / (BLOCK * 2);
     if (grid > need) grid = need;
     // MODE 2 needs a power-of-two bin count of at least 4 (mulw = 2^32 / nwords)
-    const unsigned mulw = MODE >= 2 ? (unsigned)((1ull << 32) / (uint64_t)((nbins + 1) >> 1)) : 0u;
+    const unsigned mulw = MODE == 2 ? (unsigned)((1ull << 32) / (uint64_t)((nbins + 1) >> 1)) : 0u;
     GBK_CUDA_TRY(launch_pdl(kfn, dim3((unsigned)grid), dim3(BLOCK), smem, w->stream, keys + head, nvec, nbins,
                             (unsigned long long*)bins, w->err, mulw, 0xFFFFu, 0x7FFFu));
     note_launch();
@@ -405,7 +405,6 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   }
   if ((var & 0x100) && (nbins + 1) / 2 * 4 <= max_smem) {
     const bool pow2 = nbins >= 4 && (nbins & (nbins - 1)) == 0;
-    if (pow2 && (var & 0x200)) return launch_hist16<false, 3>(keys, n, nbins, bins, w);
     return pow2 ? launch_hist16<false, 2>(keys, n, nbins, bins, w) : launch_hist16<false, 1>(keys, n, nbins, bins, w);
   }
   if ((var & 0x80) && (nbins + 1) / 2 * 4 <= max_smem) return launch_hist16<false, 1>(keys, n, nbins, bins, w);

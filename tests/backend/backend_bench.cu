@@ -13,7 +13,8 @@
 //                    offsets are in argv[1], single(PerTeam) store
 //   scatter_hist:    ScatterView (defaults: non-duplicated, atomic) histogram
 //                    of 2^26 int32 keys (x * 2654435761 mod 2^16) into 2^16
-//                    int64 bins, contribute
+//                    int64 bins, contribute; and the same with log-uniform keys
+//                    (exp2(16 u) - 1: a few bins take most of them)
 //   sort_u64:        Kokkos::sort of 2^27 uint64 keys (refilled each call)
 //   backend_bench <offsets.bin> <nseg> <reps>
 #include <Kokkos_Core.hpp>
@@ -122,6 +123,21 @@ int main(int argc, char** argv) {
       });
       Kokkos::Experimental::contribute(bins, sv);
     });
+    // skewed keys: log-uniform over the bins (a few bins take most keys)
+    Kokkos::View<int32_t*, MS> skeys("skeys", nk);
+    Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, nk), KOKKOS_LAMBDA(int64_t i) {
+      const double u = (double)(((uint64_t)i * 0x9E3779B97F4A7C15ull) >> 11) * (1.0 / 9007199254740992.0);
+      const int64_t k = (int64_t)exp2(u * 16.0) - 1;
+      skeys(i) = (int32_t)(k < nb ? k : nb - 1);
+    });
+    const double t_hist_skew = time_us(ex, reps, [&](int) {
+      auto sv = Kokkos::Experimental::create_scatter_view(bins);
+      Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, nk), KOKKOS_LAMBDA(int64_t i) {
+        auto a = sv.access();
+        a(skeys(i)) += 1;
+      });
+      Kokkos::Experimental::contribute(bins, sv);
+    });
     // ---- Kokkos::sort of 2^27 uint64 keys -----------------------------------
     const int64_t nsort = 1 << 27;
     Kokkos::View<uint64_t*, MS> sk("sk", nsort);
@@ -145,10 +161,10 @@ int main(int argc, char** argv) {
         "{\"range_sum_f64_2^24\": {\"host_result_us\": %.2f, \"view_result_us\": %.2f, \"GB/s\": %.1f}, "
         "\"mdrange_sum_f32_512x512x256\": {\"us\": %.2f, \"GB/s\": %.1f}, "
         "\"team_sum_f32_lognormal_segments\": {\"segments\": %lld, \"elements\": %lld, \"us\": %.2f, \"GB/s\": %.1f}, "
-        "\"scatterview_hist_2^26_keys_2^16_bins\": {\"us\": %.2f, \"GB/s\": %.1f}, "
+        "\"scatterview_hist_2^26_keys_2^16_bins\": {\"us\": %.2f, \"GB/s\": %.1f, \"log_uniform_keys_us\": %.2f}, "
         "\"sort_u64_2^27\": {\"ms\": %.3f, \"Gkeys_per_s\": %.2f}}\n",
         t_range_host, t_range_dev, gbs(rb, t_range_dev), t_md, gbs(mb, t_md), (long long)nseg, (long long)ns, t_team,
-        gbs(tb, t_team), t_hist, gbs(hb, t_hist), (t_sort_fill - t_fill) / 1000.0,
+        gbs(tb, t_team), t_hist, gbs(hb, t_hist), t_hist_skew, (t_sort_fill - t_fill) / 1000.0,
         (double)nsort / ((t_sort_fill - t_fill) * 1e-6) / 1e9);
   }
   Kokkos::finalize();
