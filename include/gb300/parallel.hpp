@@ -253,6 +253,8 @@ MDArgs md_args(const P& p, int64_t* total) {
 }
 
 // ---- TeamPolicy: one CTA per team, league ranks strided over the grid ----------
+constexpr int64_t kTeamGridMax = int64_t(1) << 20;
+constexpr int64_t kTeamReduceGridMax = int64_t(1) << 16;
 template <class F>
 __global__ void k_team_for(F f, int64_t league) {
   for (int64_t lr = blockIdx.x; lr < league; lr += gridDim.x) {
@@ -339,9 +341,11 @@ template <class E, class... R, class F>
 void parallel_for(const TeamPolicy<E, R...>& p, const F& f) {
   Tools::Impl::Region<F> tool_region(Tools::Impl::kFor, p.space().stream());
   if (p.league_size() <= 0) return;
+  // One CTA per league rank (up to 2^20 CTAs, then each strides): the block
+  // scheduler hands the next team to whichever SM frees up first, so a long
+  // team does not hold back the teams that would have followed it on its CTA.
   int64_t g = p.league_size();
-  const int64_t cap = (int64_t)Impl::num_sms() * (2048 / p.team_size());
-  if (g > cap) g = cap;
+  if (g > Impl::kTeamGridMax) g = Impl::kTeamGridMax;
   Impl::k_team_for<<<(unsigned)g, p.team_size(), 0, p.space().stream()>>>(f, p.league_size());
   Impl::launched(cudaGetLastError(), "parallel_for(TeamPolicy)");
 }
@@ -390,9 +394,9 @@ template <class E, class... R, class F, class Red, std::enable_if_t<Impl::is_red
 void parallel_reduce(const TeamPolicy<E, R...>& p, const F& f, const Red& red) {
   Tools::Impl::Region<F> tool_region(Tools::Impl::kReduce, p.space().stream());
   using V = typename Red::value_type;
+  // one CTA per league rank, as parallel_for; at most 2^16 per-CTA partials
   int64_t g = p.league_size();
-  const int64_t cap = (int64_t)Impl::num_sms() * (2048 / p.team_size());
-  if (g > cap) g = cap;
+  if (g > Impl::kTeamReduceGridMax) g = Impl::kTeamReduceGridMax;
   if (g < 1) g = 1;
   cudaStream_t s = p.space().stream();
   const int64_t league = p.league_size();

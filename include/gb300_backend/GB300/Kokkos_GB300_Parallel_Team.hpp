@@ -323,15 +323,17 @@ class TeamPolicyInternal<Kokkos::Experimental::GB300, Properties...> : public Po
 
 // Grid and dynamic shared memory of a team launch.
 template <class Policy>
-void gb300_team_shape(const Policy& p, const void* kernel, int64_t* grid, int* shmem) {
+// One CTA per league rank, up to max_grid CTAs (then each strides): the block
+// scheduler hands the next team to whichever SM frees up first, so a long
+// team does not hold back the teams that would have followed it on its CTA.
+void gb300_team_shape(const Policy& p, const void* kernel, int64_t max_grid, int64_t* grid, int* shmem) {
   const int ts = p.team_size();
   *shmem = (int)p.scratch_size(0, ts);
   if (*shmem > 48 * 1024)
     gb300_check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, *shmem),
                      "TeamPolicy scratch");
   int64_t g = p.league_size();
-  const int64_t cap = (int64_t)p.space().sm_count() * (2048 / (ts > 0 ? ts : 1));
-  if (g > cap) g = cap;
+  if (g > max_grid) g = max_grid;
   *grid = g < 1 ? 1 : g;
 }
 
@@ -365,7 +367,7 @@ class ParallelFor<FunctorType, Kokkos::TeamPolicy<Properties...>, Kokkos::Experi
     const auto& exec = m_policy.space();
     int64_t g = 1;
     int shmem = 0;
-    gb300_team_shape(m_policy, (const void*)gbk_skel::k_team_for<Closure>, &g, &shmem);
+    gb300_team_shape(m_policy, (const void*)gbk_skel::k_team_for<Closure>, int64_t(1) << 20, &g, &shmem);
     int* err = gb300_scratch(exec, 0).err;
     gbk_skel::k_team_for<Closure><<<(unsigned)g, m_policy.team_size(), shmem, exec.stream()>>>(
         Closure{m_functor, shmem}, m_policy.league_size(), err);
@@ -419,7 +421,7 @@ class ParallelReduce<CombinedFunctorReducerType, Kokkos::TeamPolicy<Properties..
     const auto& exec = m_policy.space();
     int64_t g = 1;
     int shmem = 0;
-    gb300_team_shape(m_policy, (const void*)gbk_skel::k_team_reduce<VB, Closure>, &g, &shmem);
+    gb300_team_shape(m_policy, (const void*)gbk_skel::k_team_reduce<VB, Closure>, int64_t(1) << 16, &g, &shmem);
     const int64_t league = m_policy.league_size() > 0 ? m_policy.league_size() : 0;
     Closure c{{m_functor_reducer.get_reducer()}, m_functor_reducer.get_functor(), shmem};
     const int ts = m_policy.team_size();

@@ -144,6 +144,7 @@ namespace {
 // the value (its size divides 16, so every aligned vector holds whole
 // values in phase); grid-stride over the vectors.
 __global__ void k_fill16(uint4* __restrict__ d, int64_t nvec, uint4 pat) {
+  pdl_entry();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nvec; i += stride) __stcs(d + i, pat);
 }
@@ -394,9 +395,8 @@ int gbk_fill(void* dst, const void* value, int elem_bytes, int64_t n, gbk_stream
     int64_t grid = (nvec + 255) / 256;
     const int64_t cap = (int64_t)sm_count() * 8;
     if (grid > cap) grid = cap;
-    k_fill16<<<(unsigned)grid, 256, 0, s>>>(reinterpret_cast<uint4*>(body), nvec, pat);
+    GBK_CUDA_TRY(launch_pdl(k_fill16, dim3((unsigned)grid), dim3(256), 0, s, reinterpret_cast<uint4*>(body), nvec, pat));
     note_launch();
-    GBK_CUDA_TRY(cudaGetLastError());
   }
   if (nhead + ntail > 0) {
     k_fill_edges<<<(unsigned)((nhead + ntail + 255) / 256), 256, 0, s>>>(d, nhead, body + nvec * 16, ntail,

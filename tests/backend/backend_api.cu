@@ -14,6 +14,7 @@
 #include <Kokkos_ScatterView.hpp>
 #include <Kokkos_Sort.hpp>
 #include <Kokkos_StdAlgorithms.hpp>
+#include <Kokkos_Graph.hpp>
 
 #include <algorithm>
 #include <cmath>
@@ -376,6 +377,49 @@ static void scatter_sort_checks() {
   report(ok, "sort");
 }
 
+// Experimental::Graph on the GB300 space (Kokkos' generic graph
+// implementation, nodes run on the space's instance at submit): a chain of
+// two parallel_for and a parallel_reduce into a device View, submitted three
+// times.
+// (functors, not lambdas: nvcc takes no extended lambda inside the generic
+// lambda that builds the graph)
+struct GraphFill {
+  Kokkos::View<int64_t*, MS> a;
+  KOKKOS_INLINE_FUNCTION void operator()(int i) const { a(i) = i % 7; }
+};
+struct GraphMap {
+  Kokkos::View<int64_t*, MS> a, b;
+  KOKKOS_INLINE_FUNCTION void operator()(int i) const { b(i) = 2 * a(i) + 1; }
+};
+struct GraphSum {
+  Kokkos::View<int64_t*, MS> b;
+  KOKKOS_INLINE_FUNCTION void operator()(int i, int64_t& u) const { u += b(i); }
+};
+static void graph_checks() {
+  const int n = 1 << 20;
+  ES ex;
+  Kokkos::View<int64_t*, MS> a("a", n), b("b", n);
+  Kokkos::View<int64_t, MS> s("s");
+  auto graph = Kokkos::Experimental::create_graph(ex, [&](auto root) {
+    auto f1 = root.then_parallel_for(Kokkos::RangePolicy<ES>(0, n), GraphFill{a});
+    auto f2 = f1.then_parallel_for(Kokkos::RangePolicy<ES>(0, n), GraphMap{a, b});
+    f2.then_parallel_reduce(Kokkos::RangePolicy<ES>(0, n), GraphSum{b}, s);
+  });
+  int64_t want = 0;
+  for (int i = 0; i < n; ++i) want += 2 * (i % 7) + 1;
+  bool ok = true;
+  for (int rep = 0; rep < 3; ++rep) {
+    Kokkos::deep_copy(ex, s, int64_t(0));
+    Kokkos::deep_copy(ex, b, int64_t(0));
+    graph.submit();
+    int64_t got = -1;
+    Kokkos::deep_copy(ex, got, s);
+    ex.fence();
+    ok = ok && got == want;
+  }
+  report(ok, "graph_chain_submit_three_times");
+}
+
 static void copy_checks() {
   const int n = 1000003;
   std::vector<double> h(n);
@@ -415,6 +459,7 @@ int main(int argc, char** argv) {
     mdrange_checks();
     team_checks();
     scatter_sort_checks();
+    graph_checks();
     copy_checks();
     ES().fence();
   }
