@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK, 2)
     }
   };
 
+  pdl_entry();  // nothing of the previous launch is read or written before this
   if (threadIdx.x == 0) {
     s_bad = 0;
 #pragma unroll
@@ -352,12 +353,26 @@ int launch_k_scan(const TI* x, TO* y, int64_t n, TO init, const LbState& S, TO* 
   cfg.blockDim = dim3(SCAN_BLOCK);
   cfg.dynamicSmemBytes = dyn;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
+  // Cooperative, and scheduled while the previous launch on the stream runs
+  // (programmatic dependent launch: the kernel waits for it on the device
+  // before its first access).  A driver that refuses the pair for a
+  // cooperative grid gets the plain cooperative launch from then on.
+  static bool pdl_ok = true;
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cuda_status(cudaLaunchKernelEx(&cfg, kfn, x, y, n, init, S, total));
+  cfg.numAttrs = pdl_ok && pdl_enabled() ? 2 : 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kfn, x, y, n, init, S, total);
+  if (e != cudaSuccess && cfg.numAttrs == 2) {
+    (void)cudaGetLastError();
+    pdl_ok = false;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kfn, x, y, n, init, S, total);
+  }
+  return cuda_status(e);
 }
 
 template <class TI, class TO, bool INCL>

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(BLOCK, 1)
   constexpr int ROUND = BLOCK * VPT;           // vectors per round
   constexpr int DRAIN = 32768 / (ROUND * 4);   // rounds between drains
   static_assert(DRAIN >= 1, "round too large for 16-bit counters");
-  constexpr bool NODRAIN = MODE != 0;
+  constexpr bool NODRAIN = MODE == 1 || MODE == 2;
   const int nwords = (int)((nbins + 1) >> 1);
   for (int i = threadIdx.x; i <= nwords; i += BLOCK) sh[i] = 0u;  // the counters and the spare word
   pdl_entry();
