@@ -391,6 +391,43 @@ static void test_team() {
     if (t.team_rank() == 0) u += ts;
   }, lsum);
   report(lsum == tot, "team_league_reduce");
+  // A league longer than one CTA per rank allows (2^20 CTAs; the rest stride
+  // over them) and long TeamThreadRange ranges (the 32-, 8- and 1-call steps).
+  {
+    const int64_t big = (int64_t(1) << 20) + 37;
+    Kokkos::View<int64_t*> marks("marks", big);
+    Kokkos::parallel_for(TP(big, 32), KOKKOS_LAMBDA(const TP::member_type& t) {
+      Kokkos::single(Kokkos::PerTeam(t), [&]() { marks(t.league_rank()) = t.league_rank() * 3 + 1; });
+    });
+    int64_t msum = 0;
+    Kokkos::parallel_reduce(TP(big, 64), KOKKOS_LAMBDA(const TP::member_type& t, int64_t& u) {
+      if (t.team_rank() == 0) u += marks(t.league_rank());
+    }, msum);
+    const int64_t want = 3 * (big * (big - 1) / 2) + big;
+    auto hm = to_host(marks);
+    bool okm = msum == want;
+    for (int64_t r = 0; r < big; r += 4093) okm = okm && hm[r] == r * 3 + 1;
+    okm = okm && hm[big - 1] == (big - 1) * 3 + 1;
+    report(okm, "team_league_beyond_grid");
+    const int64_t len = 1000003;
+    Kokkos::View<int64_t*> lv("lv", len);
+    Kokkos::parallel_for(Kokkos::RangePolicy<>(0, len), KOKKOS_LAMBDA(int64_t i) { lv(i) = i % 1013; });
+    Kokkos::View<int64_t*> ls("ls", 3);
+    Kokkos::parallel_for(TP(3, 256), KOKKOS_LAMBDA(const TP::member_type& t) {
+      const int64_t b = t.league_rank() * 7, e = len - t.league_rank() * 5;
+      int64_t acc = 0;
+      Kokkos::parallel_reduce(Kokkos::TeamThreadRange(t, b, e), [&](int64_t i, int64_t& w) { w += lv(i); }, acc);
+      Kokkos::single(Kokkos::PerTeam(t), [&]() { ls(t.league_rank()) = acc; });
+    });
+    auto hl = to_host(ls);
+    bool okl = true;
+    for (int64_t r = 0; r < 3; ++r) {
+      int64_t e = 0;
+      for (int64_t i = r * 7; i < len - r * 5; ++i) e += i % 1013;
+      okl = okl && hl[r] == e;
+    }
+    report(okl, "team_thread_range_long");
+  }
   int64_t lsum2 = 0, lcnt = 0;
   Kokkos::parallel_reduce(TP(league, 128), KOKKOS_LAMBDA(const TP::member_type& t, int64_t& u, int64_t& c) {
     const int64_t s = t.league_rank();

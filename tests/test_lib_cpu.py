@@ -48,6 +48,10 @@ def test_argument_errors_without_device(gbk):
     assert gbk.lib.gbk_scan(0, 0, 1, None, 5, None, None, None, None, None) == 1  # null buffers
     assert gbk.lib.gbk_histogram_i32_i64(None, 10, None, 0, None, None) == 1
     assert gbk.lib.gbk_set_wait_limit(0) == 1
+    buf = ctypes.create_string_buffer(512)
+    assert gbk.lib.gbk_fence_read(None, ctypes.c_void_p(8), buf, 257) == 1  # more than the 256-byte slot
+    assert gbk.lib.gbk_fence_read(None, None, buf, 8) == 1                  # no source
+    assert gbk.lib.gbk_fence_read(None, ctypes.c_void_p(8), buf, -1) == 1
 
 
 def test_datagen_deterministic_and_blocked():

@@ -192,6 +192,42 @@ def test_host_buffer_entry(env):
         assert r[nm] == w[nm]
 
 
+def test_fence_read_returns_result_and_status(env):
+    """gbk_fence_read: the reduce's device result comes back into host memory
+    behind the same synchronisation as the stream's status (the host-scalar
+    parallel_reduce path), on the default and on a created stream, twice in a
+    row (the pinned slot is reused); a device-side status raised earlier on the
+    stream comes back with it and is cleared."""
+    import ctypes
+
+    import oracle
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    x = datagen.uniform_i32((1 << 20) + 7, -50, 50, seed=3)
+    dx = _dev(torch, x)
+    want = int(oracle.reduce("sum", x, 4))
+    for st in (None, torch.cuda.Stream()):
+        sp = ctypes.c_void_p(st.cuda_stream) if st is not None else None
+        d = torch.zeros(8, dtype=torch.int64, device="cuda")
+        for _ in range(2):
+            d.zero_()
+            torch.cuda.synchronize()
+            assert gbk.lib.gbk_reduce(0, 0, ctypes.c_void_p(dx.data_ptr()), x.size,
+                                      ctypes.c_void_p(d.data_ptr()), sp, None) == 0
+            h = ctypes.c_int64(-1)
+            assert gbk.lib.gbk_fence_read(sp, ctypes.c_void_p(d.data_ptr()), ctypes.byref(h), 8) == 0
+            assert h.value == want
+    # a key outside the bins raises the stream's status; fence_read reports it once
+    keys = torch.tensor([1, 2, 70000], dtype=torch.int32, device="cuda")
+    bins = torch.zeros(16, dtype=torch.int64, device="cuda")
+    assert gbk.lib.gbk_histogram_i32_i64(ctypes.c_void_p(keys.data_ptr()), 3, ctypes.c_void_p(bins.data_ptr()),
+                                         16, None, None) == 0
+    h = ctypes.c_int64(-1)
+    assert gbk.lib.gbk_fence_read(None, ctypes.c_void_p(bins.data_ptr() + 8), ctypes.byref(h), 8) == 6
+    assert h.value == 1
+    assert gbk.lib.gbk_stream_check(None) == 0
+
+
 def test_tuning_configs_agree(env):
     """Every compiled launch configuration gives a correct (in-tolerance,
     exact for integers) result."""
