@@ -723,6 +723,32 @@ def main():
     red_cold_ms = np.mean([cold[n]["ms"] for n in ("mdrange_minloc_f32", "mdrange_maxloc_f32", "mdrange_sum_f32")])
     red_cold_gbs = RED_BYTES / (red_cold_ms / 1e3) / 1e9
 
+    # Each reduce launched 20 times back to back between two events, the view
+    # and a copy of it taking turns (268 MB each, twice the L2, so every launch
+    # reads its input from HBM): the kernel's own duration, its launch latency
+    # hidden as in the step.  This is the roofline's `achieved`.
+    dx2 = dx.clone()
+    X2 = ctypes.c_void_p(dx2.data_ptr())
+    b2b = {}
+    with torch.cuda.stream(stream):
+        for name, code, outp in (("mdrange_minloc_f32", 8, R0), ("mdrange_maxloc_f32", 9, R1), ("mdrange_sum_f32", 0, R2)):
+            def call(i, code=code, outp=outp, name=name):
+                gbk.check(lib.gbk_mdrange_reduce(code, 4, X if i % 2 == 0 else X2, rk, lo, up, st, outp, sp, None), name)
+            for i in range(4):
+                call(i)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for i in range(20):
+                call(i)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            gbk.stream_check(stream)
+            b_ms = e0.elapsed_time(e1) / 20
+            gbs = RED_BYTES / (b_ms / 1e3) / 1e9
+            b2b[name] = {"ms": round(b_ms, 5), "GB/s": round(gbs, 1), "frac_of_" + peak_kind + "_hbm": round(gbs / hbm, 4)}
+    del dx2
+    red_b2b_gbs = RED_BYTES / (np.mean([v["ms"] for v in b2b.values()]) / 1e3) / 1e9
+
     # The same three results from one pass: MinMaxLoc and Sum as two reducers
     # of one parallel_reduce over the box (reported beside the step, not in it).
     R3 = ctypes.c_void_p(dres.data_ptr() + 192)
@@ -799,10 +825,14 @@ def main():
                    "launch_config": "autotuner table" if tuned else "library defaults",
                    "kernels": launch_shapes(gbk, tuned)},
         "roofline": {"bound": "hbm", "kernel": ROOF_KERNEL,
-                     "achieved": round(red_gbs, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(red_gbs / hbm, 4), "peak_kind": peak_kind + " hbm_gbs (burst copy)",
+                     "achieved": round(red_b2b_gbs, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(red_b2b_gbs / hbm, 4), "peak_kind": peak_kind + " hbm_gbs (burst copy)",
                      "traffic": ROOF_TRAFFIC,
+                     "achieved_how": "20 back-to-back launches per reducer, two copies of the view taking turns "
+                                     "(each twice the L2), CUDA events around the 20",
+                     "achieved_in_step": round(red_gbs, 1), "frac_in_step": round(red_gbs / hbm, 4),
                      "achieved_cold_l2": round(red_cold_gbs, 1), "frac_cold_l2": round(red_cold_gbs / hbm, 4)},
+        "ops_back_to_back": b2b,
         "ops": per_op,
         "ops_cold_l2": cold,
         "e2e": {"value": round(e2e_val, 1), "unit": "GB/s", "ms_per_step": round(e_ms, 3),

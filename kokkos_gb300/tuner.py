@@ -2,7 +2,10 @@
 
 * Exhaustive autotuner: for a workload (operation kind, element type, size,
   segment statistics, histogram bins and key entropy) every candidate launch
-  configuration is timed through the C ABI (CUDA events, median of repeats).
+  configuration is timed through the C ABI with CUDA events: inputs of at
+  least twice the L2 as consecutive calls (two copies taking turns where the
+  buffer has room; launch latency hidden, as in a stream of kernels), smaller
+  ones one call at a time after a read that empties L2 of them (median of 3).
 * Learned tuner: an ensemble of five 3-layer, 64-hidden FP32 MLPs (features
   of the workload and of a candidate configuration -> log time relative to
   the workload's mean), trained with the library's own CUDA kernels
@@ -46,6 +49,11 @@ SPLIT_CFGS = [(3, 0), (4, 0), (5, 0), (6, 0), (5, 2)]  # double Sum, variant 3: 
 REDUCE_OPS = [("sum", 5), ("sum", 4), ("minloc", 4), ("maxloc", 4), ("mmls", 4), ("sum", 0), ("sum", 1)]
 OPC = {"sum": 0, "minloc": 8, "maxloc": 9, "mmls": 12}
 NFEAT = 34
+# Timing regime: inputs of at least twice the 129 MB L2 are timed as BACK_TO_BACK
+# consecutive calls (launch latency hidden, as in a stream of kernels); smaller
+# ones one call at a time after a 256 MiB read that empties L2 of them.
+BACK_TO_BACK_BYTES = 2 * 129 * 1000 * 1000
+BACK_TO_BACK = 6
 
 
 def candidates(w):
@@ -203,28 +211,41 @@ class Bench:
             w["offsets"] = self.torch.from_numpy(offs).cuda()
             w["segout"] = self.torch.empty(w["nseg"], dtype=self.torch.float32, device="cuda")
 
-    def call(self, w, c):
+    def _half(self, buf, n, alt):
+        """Address of the workload's input: the buffer's start, or (alt) its
+        second half when the input fits there (a second copy of the same
+        distribution)."""
+        off = buf.numel() // 2 if alt and n <= buf.numel() // 2 else 0
+        return ctypes.c_void_p(buf.data_ptr() + off * buf.element_size())
+
+    def call(self, w, c, alt=False):
         gbk, lib, sp = self.gbk, self.gbk.lib, self.sp
         t = gbk.Tuning(c["block"], c["ipt"], c["cps"], c["variant"])
         k = w["kind"]
         if k == KIND_REDUCE:
             buf = {5: self.f64, 4: self.f32, 0: self.i32, 1: self.i64}[w["dtype"]]
-            return lib.gbk_reduce(w["op"], w["dtype"], ctypes.c_void_p(buf.data_ptr()), w["n"],
+            return lib.gbk_reduce(w["op"], w["dtype"], self._half(buf, w["n"], alt), w["n"],
                                   ctypes.c_void_p(self.res.data_ptr()), sp, ctypes.byref(t))
         if k == KIND_SCAN:
             iv = ctypes.c_int64(0)
-            return lib.gbk_scan(w["op"], 0, 1, ctypes.c_void_p(self.i32.data_ptr()), w["n"], ctypes.byref(iv),
+            return lib.gbk_scan(w["op"], 0, 1, self._half(self.i32, w["n"], alt), w["n"], ctypes.byref(iv),
                                 ctypes.c_void_p(self.y64.data_ptr()), None, sp, ctypes.byref(t))
         if k == KIND_HIST:
             return lib.gbk_histogram_i32_i64(ctypes.c_void_p(w["keys"].data_ptr()), w["n"],
                                              ctypes.c_void_p(self.bins.data_ptr()), w["nbins"], sp, ctypes.byref(t))
         if k == KIND_SEGSCAN:
-            return lib.gbk_segmented_scan(w["op"], 0, 1, ctypes.c_void_p(self.i32.data_ptr()),
+            return lib.gbk_segmented_scan(w["op"], 0, 1, self._half(self.i32, w["n"], alt),
                                           ctypes.c_void_p(w["offsets"].data_ptr()), w["nseg"], w["n"],
                                           ctypes.c_void_p(self.y64.data_ptr()), sp, ctypes.byref(t))
-        return lib.gbk_segmented_reduce(0, 4, ctypes.c_void_p(self.f32.data_ptr()),
+        return lib.gbk_segmented_reduce(0, 4, self._half(self.f32, w["n"], alt),
                                         ctypes.c_void_p(w["offsets"].data_ptr()), w["nseg"], w["n"],
                                         ctypes.c_void_p(w["segout"].data_ptr()), sp, ctypes.byref(t))
+
+    @staticmethod
+    def input_bytes(w):
+        if w["kind"] == KIND_REDUCE:
+            return w["n"] * (8 if w["dtype"] in (1, 3, 5) else 4)
+        return w["n"] * 4  # int32 keys, int32 scan input, float / int32 segment values
 
     def time(self, w, c, reps=3):
         torch = self.torch
@@ -232,6 +253,19 @@ class Bench:
         st = self.call(w, c)  # warm-up
         if st:
             return float("inf")
+        if self.input_bytes(w) >= BACK_TO_BACK_BYTES:
+            # Inputs of at least twice the L2: BACK_TO_BACK calls between two
+            # events, alternating between two copies where the buffer has room
+            # (every call reads from HBM), so the launch latency is hidden as
+            # in a sequence of kernels on a stream.
+            self.call(w, c, alt=True)
+            e0, e1 = e[0], e[1]
+            e0.record(self.s)
+            for i in range(BACK_TO_BACK):
+                self.call(w, c, alt=bool(i & 1))
+            e1.record(self.s)
+            e1.synchronize()
+            return e0.elapsed_time(e1) / BACK_TO_BACK * 1e3  # us
         for r in range(reps):
             with torch.cuda.stream(self.s):
                 self.flush_sink.copy_(self.flush.sum(dtype=torch.int64))
