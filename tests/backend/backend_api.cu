@@ -15,6 +15,7 @@
 #include <Kokkos_Sort.hpp>
 #include <Kokkos_StdAlgorithms.hpp>
 #include <Kokkos_Graph.hpp>
+#include <GB300/Kokkos_GB300_Graph_Impl.hpp>
 
 #include <algorithm>
 #include <cmath>
@@ -377,10 +378,11 @@ static void scatter_sort_checks() {
   report(ok, "sort");
 }
 
-// Experimental::Graph on the GB300 space (Kokkos' generic graph
-// implementation, nodes run on the space's instance at submit): a chain of
-// two parallel_for and a parallel_reduce into a device View, submitted three
-// times.
+// Experimental::Graph on the GB300 space (GraphImpl<GB300>: the nodes are
+// captured into one CUDA graph at instantiate): a chain of two parallel_for
+// and a parallel_reduce into a device View, submitted three times; then a
+// diamond through when_all (an aggregate node) submitted twice, once on
+// another instance.
 // (functors, not lambdas: nvcc takes no extended lambda inside the generic
 // lambda that builds the graph)
 struct GraphFill {
@@ -394,6 +396,14 @@ struct GraphMap {
 struct GraphSum {
   Kokkos::View<int64_t*, MS> b;
   KOKKOS_INLINE_FUNCTION void operator()(int i, int64_t& u) const { u += b(i); }
+};
+struct GraphShift {
+  Kokkos::View<int64_t*, MS> a, c;
+  KOKKOS_INLINE_FUNCTION void operator()(int i) const { c(i) = a(i) + 5; }
+};
+struct GraphSum2 {
+  Kokkos::View<int64_t*, MS> b, c;
+  KOKKOS_INLINE_FUNCTION void operator()(int i, int64_t& u) const { u += b(i) + c(i); }
 };
 static void graph_checks() {
   const int n = 1 << 20;
@@ -418,6 +428,35 @@ static void graph_checks() {
     ok = ok && got == want;
   }
   report(ok, "graph_chain_submit_three_times");
+  // diamond: fill a; b = 2a + 1 and c = a + 5 both after it; sum of b + c after both
+  Kokkos::View<int64_t*, MS> c("c", n);
+  Kokkos::View<int64_t, MS> s2("s2");
+  auto diamond = Kokkos::Experimental::create_graph(ex, [&](auto root) {
+    auto f1 = root.then_parallel_for(Kokkos::RangePolicy<ES>(0, n), GraphFill{a});
+    auto fb = f1.then_parallel_for(Kokkos::RangePolicy<ES>(0, n), GraphMap{a, b});
+    auto fc = f1.then_parallel_for(Kokkos::RangePolicy<ES>(0, n), GraphShift{a, c});
+    Kokkos::Experimental::when_all(fb, fc).then_parallel_reduce(Kokkos::RangePolicy<ES>(0, n), GraphSum2{b, c}, s2);
+  });
+  int64_t want2 = want;
+  for (int i = 0; i < n; ++i) want2 += i % 7 + 5;
+  cudaStream_t other_stream = nullptr;
+  cudaStreamCreateWithFlags(&other_stream, cudaStreamNonBlocking);
+  ES other(other_stream);
+  bool ok2 = true;
+  for (int rep = 0; rep < 2; ++rep) {
+    const ES& on = rep ? other : ex;
+    Kokkos::deep_copy(on, s2, int64_t(0));
+    Kokkos::deep_copy(on, b, int64_t(0));
+    Kokkos::deep_copy(on, c, int64_t(0));
+    diamond.submit(on);
+    int64_t got = -1;
+    Kokkos::deep_copy(on, got, s2);
+    on.fence();
+    ok2 = ok2 && got == want2;
+  }
+  report(ok2, "graph_diamond_when_all");
+  other.fence();
+  cudaStreamDestroy(other_stream);
 }
 
 static void copy_checks() {

@@ -16,10 +16,15 @@
 //                    int64 bins, contribute; and the same with log-uniform keys
 //                    (exp2(16 u) - 1: a few bins take most of them)
 //   sort_u64:        Kokkos::sort of 2^27 uint64 keys (refilled each call)
+//   graph:           Experimental::Graph of 8 dependent parallel_for nodes over
+//                    2^16 int64 (y = x + 1) submitted, against the same 8
+//                    parallel_for launched directly
 //   backend_bench <offsets.bin> <nseg> <reps>
 #include <Kokkos_Core.hpp>
 #include <Kokkos_ScatterView.hpp>
 #include <Kokkos_Sort.hpp>
+#include <Kokkos_Graph.hpp>
+#include <GB300/Kokkos_GB300_Graph_Impl.hpp>
 
 #include <cstdio>
 #include <cstdlib>
@@ -27,6 +32,13 @@
 
 using ES = Kokkos::Experimental::GB300;
 using MS = Kokkos::Experimental::GB300Space;
+
+// graph nodes: y = x + 1, chained (functors: no extended lambda inside the
+// generic lambda that builds the graph)
+struct AddOne {
+  Kokkos::View<int64_t*, MS> x, y;
+  KOKKOS_INLINE_FUNCTION void operator()(int64_t i) const { y(i) = x(i) + 1; }
+};
 
 template <class F>
 static double time_us(const ES& ex, int reps, F&& f) {
@@ -154,6 +166,21 @@ int main(int argc, char** argv) {
       fill(r);
       Kokkos::sort(ex, sk);
     });
+    // ---- Graph of 8 dependent parallel_for nodes over 2^16 elements ----------
+    const int64_t gn = 1 << 16;
+    std::vector<Kokkos::View<int64_t*, MS>> gv;
+    for (int i = 0; i < 9; ++i) gv.emplace_back("gv", gn);
+    auto chain = [&]() {
+      for (int i = 0; i < 8; ++i) Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, gn), AddOne{gv[i], gv[i + 1]});
+    };
+    auto graph = Kokkos::Experimental::create_graph(ex, [&](auto root) {
+      // type-erased node handle, so that each link can be assigned to it
+      Kokkos::Experimental::GraphNodeRef<ES> node = root.then_parallel_for(Kokkos::RangePolicy<ES>(0, gn), AddOne{gv[0], gv[1]});
+      for (int i = 1; i < 8; ++i) node = node.then_parallel_for(Kokkos::RangePolicy<ES>(0, gn), AddOne{gv[i], gv[i + 1]});
+    });
+    graph.instantiate();
+    const double t_chain = time_us(ex, reps * 10, [&](int) { chain(); });
+    const double t_graph = time_us(ex, reps * 10, [&](int) { graph.submit(); });
     ex.fence();
     const double rb = (double)n * 8, mb = (double)n0 * n1 * n2 * 4, tb = (double)ns * 4 + (nseg + 1) * 8.0 + nseg * 4.0;
     const double hb = (double)nk * 4 + nb * 8.0;
@@ -162,10 +189,11 @@ int main(int argc, char** argv) {
         "\"mdrange_sum_f32_512x512x256\": {\"us\": %.2f, \"GB/s\": %.1f}, "
         "\"team_sum_f32_lognormal_segments\": {\"segments\": %lld, \"elements\": %lld, \"us\": %.2f, \"GB/s\": %.1f}, "
         "\"scatterview_hist_2^26_keys_2^16_bins\": {\"us\": %.2f, \"GB/s\": %.1f, \"log_uniform_keys_us\": %.2f}, "
-        "\"sort_u64_2^27\": {\"ms\": %.3f, \"Gkeys_per_s\": %.2f}}\n",
+        "\"sort_u64_2^27\": {\"ms\": %.3f, \"Gkeys_per_s\": %.2f}, "
+        "\"graph_8_parallel_for_2^16\": {\"graph_us\": %.2f, \"launches_us\": %.2f}}\n",
         t_range_host, t_range_dev, gbs(rb, t_range_dev), t_md, gbs(mb, t_md), (long long)nseg, (long long)ns, t_team,
         gbs(tb, t_team), t_hist, gbs(hb, t_hist), t_hist_skew, (t_sort_fill - t_fill) / 1000.0,
-        (double)nsort / ((t_sort_fill - t_fill) * 1e-6) / 1e9);
+        (double)nsort / ((t_sort_fill - t_fill) * 1e-6) / 1e9, t_graph, t_chain);
   }
   Kokkos::finalize();
   return 0;
