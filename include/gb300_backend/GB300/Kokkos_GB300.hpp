@@ -247,7 +247,7 @@ struct DeepCopy<HostSpace, Kokkos::Experimental::GB300Space, ExecutionSpace,
 // (core/src/Kokkos_Core_fwd.hpp:230-256, View/Kokkos_ViewAccessPreconditionsCheck.hpp:
 // 70-77, View/Kokkos_ViewMapping.hpp:3480-3490).  Kokkos' list of default
 // spaces (Kokkos_Core_fwd.hpp:96-121) has no entry for a space added beside
-// the built-in ones, so in this build both are Serial, and the stock checks
+// the built-in ones, so with this backend both are Serial, and the stock checks
 // would reject every device access to GB300 memory.  These specialisations
 // state the real rule: GB300Space is accessible from device code and not
 // from host code; HostSpace is accessible from host code and not from

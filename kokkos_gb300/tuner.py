@@ -11,7 +11,7 @@
   the workload's mean), trained with the library's own CUDA kernels
   (gbk_mlp_forward / backward / mse / adam); for an unseen workload it picks
   the candidate with the smallest mean predicted time.  The exhaustive tuner
-  stays the fallback and the judge of its regret; the tuning table (the
+  stays the fallback and the yardstick of its regret; the tuning table (the
   exhaustive best per bucket, looked up at the nearest bucket) is the method
   without the MLP that it is compared with.
 * The tuning table (text, loaded by gbk_tuner_load) maps (kind, op, dtype,
