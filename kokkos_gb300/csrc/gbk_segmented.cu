@@ -868,17 +868,17 @@ int launch_k_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t 
   return GBK_OK;
 }
 
-// items_per_thread (16-byte vectors per thread per tile): 7 or 3.  Default:
-// 3 for scans that widen (output wider than input: the out tile doubles the
-// shared memory of a stage), 7 otherwise.  Measured on GB300, int32 -> int64
-// inclusive scans: 3 was the faster on 493 of 501 sampled workloads (2^16 to
-// 2^27 elements, 64 to 10,000 lognormal segments; 7 reached 0.72 of the best
-// on average), and 0.869 against 0.897 ms on 2^28 elements in 10,000
-// segments; int32 -> int32 on the latter: 7 takes 0.477 ms, 3 0.740 ms.
+// items_per_thread (16-byte vectors per thread per tile): 7, 5 or 3.  Scans
+// default to 5 with three staging stages (two CTAs per SM still fit), so
+// the compute warps have a second tile ahead while they wait for a carry;
+// reduces of unaligned input keep 7 with three stages.  Measured on GB300,
+// inclusive scans of 2^28 int32 in 10,000 lognormal segments: int32 ->
+// int64 0.638 ms with 5 x 3 stages against 0.896 (7 x 2) and 0.866 (3 x 2);
+// int32 -> int32 0.472 against 0.476 (7 x 2) and 0.739 (3 x 2).
 template <class TI, class TO, int OP, int MODE>
 int launch_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t nseg, Workspace* w,
                const gbk_tuning_t* t) {
-  constexpr int DEF = sizeof(TO) > sizeof(TI) && MODE != M_REDUCE ? 3 : 7;
+  constexpr int DEF = MODE != M_REDUCE ? 5 : 7;
   const int want = t && t->items_per_thread > 0 ? t->items_per_thread : DEF;
   const int cps = t ? t->ctas_per_sm : 0;
   const bool fast = (uintptr_t)x % 16 == 0 && (MODE == M_REDUCE || (uintptr_t)y % 16 == 0);
@@ -887,6 +887,8 @@ int launch_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t ns
   constexpr int STG = MODE == M_REDUCE ? 3 : 2;
   if (!fast) return launch_k_seg<TI, TO, OP, MODE, false, 7, STG>(x, y, n, offsets, nseg, w, cps);
   if (want <= 4) return launch_k_seg<TI, TO, OP, MODE, true, 3, STG>(x, y, n, offsets, nseg, w, cps);
+  // 5 vectors per thread: three stages still fit two CTAs per SM
+  if (want == 5 && MODE != M_REDUCE) return launch_k_seg<TI, TO, OP, MODE, true, 5, 3>(x, y, n, offsets, nseg, w, cps);
   return launch_k_seg<TI, TO, OP, MODE, true, 7, STG>(x, y, n, offsets, nseg, w, cps);
 }
 

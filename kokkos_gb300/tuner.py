@@ -38,8 +38,8 @@ SCAN_CFGS = [(9, 0), (7, 0), (3, 0), (9, 1)]  # (vectors per thread, CTAs per SM
 # segmented reduce (variant, vectors per thread, CTAs per SM; 0 = all resident): variant 0 is the
 # contiguous-share kernel (its shape is fixed), variant 1 the tile pipeline
 SEG_CFGS = [(0, 7, 0), (1, 7, 0), (1, 3, 0), (1, 7, 1)]
-# segmented scan (the tile pipeline; vectors per thread, CTAs per SM)
-SEGSCAN_CFGS = [(7, 0), (3, 0), (7, 1), (3, 1)]
+# segmented scan (the tile pipeline; vectors per thread, CTAs per SM; 5 runs three stages)
+SEGSCAN_CFGS = [(7, 0), (5, 0), (3, 0), (7, 1), (5, 1), (3, 1)]
 # histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit with periodic drains (0x20),
 # drain-free (0x80) and drain-free in the multiply form for power-of-two bins (0x100), no privatisation (0x40)
 HIST_CFGS_SMALL = [(0x01, 1), (0x01, 2), (0x11, 2), (0x20, 1), (0x30, 1), (0x40, 1)]
@@ -410,10 +410,10 @@ def default_cfg_index(w, cs):
                 return i
         if k == KIND_SCAN and (c["ipt"], c["cps"]) == (9, 0):
             return i
-        # segmented reduce: 7 vectors; segmented int32 -> int64 scan (widening): 3
+        # segmented reduce: 7 vectors; segmented scans: 5 vectors with three stages
         if k == KIND_SEG and (c["ipt"], c["cps"]) == (7, 0):
             return i
-        if k == KIND_SEGSCAN and (c["ipt"], c["cps"]) == (3, 0):
+        if k == KIND_SEGSCAN and (c["ipt"], c["cps"]) == (5, 0):
             return i
         if k == KIND_HIST:
             # 65536 bins: the drain-free 16-bit kernel in its multiply form; up to

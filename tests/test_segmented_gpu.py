@@ -80,17 +80,19 @@ def test_segmented_vs_oracle(env, case):
     np.testing.assert_array_equal(y64.cpu().numpy(), inc - xi.astype(np.int64))
 
 
-@pytest.mark.parametrize("ipt,cps", [(7, 0), (7, 1), (3, 0), (3, 2)])
+@pytest.mark.parametrize("ipt,cps", [(7, 0), (7, 1), (5, 0), (5, 1), (3, 0), (3, 2)])
 def test_segmented_shapes(env, ipt, cps):
-    """Every tile shape of the persistent kernel (7 or 3 vectors per thread,
-    all-resident or fewer CTAs), with segment boundaries on the tile edges of
-    both shapes (7168 / 3072 elements for 4-byte types, 3584 / 1536 for
-    8-byte), empty segments next to them, and an unaligned input view."""
+    """Every tile shape of the persistent kernel (7, 5 (scans: three stages)
+    or 3 vectors per thread, all-resident or fewer CTAs), with segment
+    boundaries on the tile edges of the shapes (7168 / 5120 / 3072 elements
+    for 4-byte types, 3584 / 2560 / 1536 for 8-byte), empty segments next to
+    them, and an unaligned input view."""
     gbk, torch = env
     import oracle
     from kokkos_gb300 import datagen
     rng = np.random.default_rng(ipt * 10 + cps)
-    lens = np.concatenate([[7168, 7168, 0, 1, 7167, 3584, 3584, 0, 0, 3072, 1536, 5, 14336, 6144],
+    lens = np.concatenate([[7168, 7168, 0, 1, 7167, 3584, 3584, 0, 0, 3072, 1536, 5, 14336, 6144, 5120, 0, 5120,
+                            2560, 10240, 2559, 1],
                            rng.integers(0, 40, 400), [100000], rng.integers(0, 9000, 60)]).astype(np.int64)
     offs = datagen.offsets_from_lengths(lens)
     n = int(offs[-1])

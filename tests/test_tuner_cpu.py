@@ -59,7 +59,7 @@ def test_new_candidate_families():
     s = {"kind": tuner.KIND_SEGSCAN, "op": 1, "dtype": 0, "n": 1 << 22, "nseg": 1024}
     cs = tuner.candidates(s)
     assert [(c["ipt"], c["cps"]) for c in cs] == list(tuner.SEGSCAN_CFGS)
-    assert (cs[tuner.default_cfg_index(s, cs)]["ipt"], cs[tuner.default_cfg_index(s, cs)]["cps"]) == (3, 0)
+    assert (cs[tuner.default_cfg_index(s, cs)]["ipt"], cs[tuner.default_cfg_index(s, cs)]["cps"]) == (5, 0)
     fs = tuner.features(s, cs[0])
     assert fs[3] == 1 and fs[24] == 1 and fs[27] == 1
     m = {"kind": tuner.KIND_REDUCE, "op": 12, "dtype": 4, "n": 1 << 22}
