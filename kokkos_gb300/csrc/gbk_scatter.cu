@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(BLOCK, 1)
   constexpr int ROUND = BLOCK * VPT;           // vectors per round
   constexpr int DRAIN = 32768 / (ROUND * 4);   // rounds between drains
   static_assert(DRAIN >= 1, "round too large for 16-bit counters");
-  constexpr bool NODRAIN = MODE == 1 || MODE == 2;
+  constexpr bool NODRAIN = MODE == 1 || MODE == 2 || MODE == 4;
   const int nwords = (int)((nbins + 1) >> 1);
   for (int i = threadIdx.x; i <= nwords; i += BLOCK) sh[i] = 0u;  // the counters and the spare word
   pdl_entry();
@@ -212,6 +212,94 @@ __global__ void __launch_bounds__(BLOCK, 1)
     __syncthreads();
   };
   int64_t v = v0;
+  if constexpr (MODE == 4) {
+    // MODE 2's arithmetic with the round's eight atomics issued back to
+    // back and one crossing test per round: t = (old ^ 0x7FFF<<half) &
+    // 0xFFFF<<half is zero only for the increment that took its counter
+    // from 0x7FFF to 0x8000, so the minimum of the eight t is zero when any
+    // crossing happened; that rare round then finds its crossings one by
+    // one.  The crossing thread subtracts once its round's eight atomics
+    // have returned (a few hundred cycles); passing the 0x7FFF headroom
+    // meanwhile would take 32,767 more increments of that one counter, which
+    // shared memory applies one at a time.
+    // Two register sets take turns (one is counted while the other loads),
+    // and only a CTA's last, partial round checks bounds per vector.
+    auto load = [&](Vec16<int32_t>* r, int64_t vb) {
+#pragma unroll
+      for (int j = 0; j < VPT; ++j) {
+        const int64_t q = vb + (int64_t)j * BLOCK + threadIdx.x;
+        r[j].u = q < v1 ? ld_stream16(keys + 4 * q) : make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+      }
+    };
+    auto count_round = [&](const Vec16<int32_t>* r, int64_t vb) {
+      if (vb + ROUND <= v1) {
+        unsigned mx = 0;
+#pragma unroll
+        for (int j = 0; j < VPT; ++j)
+          mx = max(mx, max(__vimax3_u32((unsigned)r[j].v[0], (unsigned)r[j].v[1], (unsigned)r[j].v[2]),
+                           (unsigned)r[j].v[3]));
+        if (mx < nb32) {
+          unsigned o[VPT * 4];
+#pragma unroll
+          for (int j = 0; j < VPT; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const unsigned uk = (unsigned)r[j].v[e];
+              const unsigned hi = __umulhi(uk, mulw);
+              o[j * 4 + e] = atomicAdd(sh + (uk - hi * nw32), 1u + hi * cffff);
+            }
+          unsigned t = 0xFFFFFFFFu;
+#pragma unroll
+          for (int j = 0; j < VPT; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const unsigned inc = 1u + __umulhi((unsigned)r[j].v[e], mulw) * cffff;
+              t = min(t, (o[j * 4 + e] ^ (inc * c7fff)) & (inc * cffff));
+            }
+          if (t == 0u) {
+#pragma unroll
+            for (int j = 0; j < VPT; ++j)
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const unsigned uk = (unsigned)r[j].v[e];
+                const unsigned hi = __umulhi(uk, mulw);
+                const unsigned word = uk - hi * nw32;
+                const unsigned inc = 1u + hi * cffff;
+                if (((o[j * 4 + e] ^ (inc * c7fff)) & (inc * cffff)) == 0u) {
+                  atomicSub(sh + word, inc << 15);
+                  red_add_u64(bins + word + hi * nw32, 0x8000ull);
+                }
+              }
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < VPT; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) count(r[j].v[e]);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < VPT; ++j) {
+          const int64_t q = vb + (int64_t)j * BLOCK + threadIdx.x;
+          if (q < v1) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) count(r[j].v[e]);
+          }
+        }
+      }
+    };
+    Vec16<int32_t> ra[VPT], rb[VPT];
+    load(ra, v);
+    while (v < v1) {
+      load(rb, v + ROUND);
+      count_round(ra, v);
+      v += ROUND;
+      if (v >= v1) break;
+      load(ra, v + ROUND);
+      count_round(rb, v);
+      v += ROUND;
+    }
+  } else {
   Vec16<int32_t> cur[VPT], nxt[VPT];
 #pragma unroll
   for (int j = 0; j < VPT; ++j) {
@@ -278,6 +366,7 @@ __global__ void __launch_bounds__(BLOCK, 1)
       drain();
     }
   }
+  }
   __syncthreads();
   for (int i = threadIdx.x; i < nwords; i += BLOCK) {
     const unsigned w = sh[i];
@@ -319,8 +408,8 @@ int launch_hist16(const int32_t* keys, int64_t n, int64_t nbins, int64_t* bins, 
     int64_t grid = sm_count();
     const int64_t need = (nvec + BLOCK * 2 - 1) / (BLOCK * 2);
     if (grid > need) grid = need;
-    // MODE 2 needs a power-of-two bin count of at least 4 (mulw = 2^32 / nwords)
-    const unsigned mulw = MODE == 2 ? (unsigned)((1ull << 32) / (uint64_t)((nbins + 1) >> 1)) : 0u;
+    // MODEs 2 and 4 need a power-of-two bin count of at least 4 (mulw = 2^32 / nwords)
+    const unsigned mulw = MODE == 2 || MODE == 4 ? (unsigned)((1ull << 32) / (uint64_t)((nbins + 1) >> 1)) : 0u;
     GBK_CUDA_TRY(launch_pdl(kfn, dim3((unsigned)grid), dim3(BLOCK), smem, w->stream, keys + head, nvec, nbins,
                             (unsigned long long*)bins, w->err, mulw, 0xFFFFu, 0x7FFFu));
     note_launch();
@@ -386,7 +475,8 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
   // variant bits: 0x0F cluster size of the 32-bit privatised kernel (1, 2,
   // 4, 8); 0x10 warp aggregation; 0x20 the 16-bit one-CTA-per-SM kernel;
   // 0x40 no privatisation; 0x80 the 16-bit kernel without drains; 0x100
-  // the same in its multiply form for power-of-two bin counts.
+  // the same in its multiply form for power-of-two bin counts; 0x200 the
+  // multiply form with one crossing test per round.
   // 0 = automatic choice.
   const int var = t ? t->variant : 0;
   int cl = var & 0xF;
@@ -402,6 +492,10 @@ int hist_launch(const int32_t* keys, int64_t n, int64_t* bins, int64_t nbins, Wo
       return pow2 ? launch_hist16<false, 2>(keys, n, nbins, bins, w) : launch_hist16<false, 1>(keys, n, nbins, bins, w);
     }
     else { cl = 2; while (cl <= 8 && (nbins + cl - 1) / cl * 4 > max_smem) cl *= 2; }
+  }
+  if ((var & 0x200) && (nbins + 1) / 2 * 4 <= max_smem) {
+    const bool pow2 = nbins >= 4 && (nbins & (nbins - 1)) == 0;
+    return pow2 ? launch_hist16<false, 4>(keys, n, nbins, bins, w) : launch_hist16<false, 1>(keys, n, nbins, bins, w);
   }
   if ((var & 0x100) && (nbins + 1) / 2 * 4 <= max_smem) {
     const bool pow2 = nbins >= 4 && (nbins & (nbins - 1)) == 0;

@@ -41,9 +41,11 @@ SEG_CFGS = [(0, 7, 0), (1, 7, 0), (1, 3, 0), (1, 7, 1)]
 # segmented scan (the tile pipeline; vectors per thread, CTAs per SM; 5 runs three stages)
 SEGSCAN_CFGS = [(7, 0), (5, 0), (3, 0), (7, 1), (5, 1), (3, 1)]
 # histogram (variant, ctas_per_sm): 32-bit privatised (cluster 1/2), 16-bit with periodic drains (0x20),
-# drain-free (0x80) and drain-free in the multiply form for power-of-two bins (0x100), no privatisation (0x40)
+# drain-free (0x80), drain-free in the multiply form for power-of-two bins (0x100) and the same with one
+# crossing test per round (0x200), no privatisation (0x40)
 HIST_CFGS_SMALL = [(0x01, 1), (0x01, 2), (0x11, 2), (0x20, 1), (0x30, 1), (0x40, 1)]
-HIST_CFGS_2E16 = [(0x02, 1), (0x12, 1), (0x04, 1), (0x20, 1), (0x30, 1), (0x80, 1), (0x100, 1), (0x40, 1)]
+HIST_CFGS_2E16 = [(0x02, 1), (0x12, 1), (0x04, 1), (0x20, 1), (0x30, 1), (0x80, 1), (0x100, 1), (0x200, 1),
+                  (0x40, 1)]
 SPLIT_CFGS = [(3, 0), (4, 0), (5, 0), (6, 0), (5, 2)]  # double Sum, variant 3: (vectors per thread, CTAs per SM)
 # (op, dtype code); "mmls" is the fused MinMaxLoc+Sum reducer
 REDUCE_OPS = [("sum", 5), ("sum", 4), ("minloc", 4), ("maxloc", 4), ("mmls", 4), ("sum", 0), ("sum", 1)]
@@ -105,11 +107,12 @@ def features(w, c):
         f[20] = float(v == 2)                            # reduce: the ring kernel
         f[21] = float(v == 3)                            # reduce: the FP64 / integer split kernel
     elif k == KIND_HIST:
-        f[20] = float((v & 0xF) > 1) if v and not (v & 0x1E0) else 0.0  # cluster-split bins
+        f[20] = float((v & 0xF) > 1) if v and not (v & 0x3E0) else 0.0  # cluster-split bins
         f[21] = float((v & 0x10) != 0)                   # warp aggregation
-        f[22] = float((v & 0x1A0) != 0)                  # 16-bit bins
+        f[22] = float((v & 0x3A0) != 0)                  # 16-bit bins
         f[23] = float((v & 0x40) != 0)                   # no privatisation
-        f[26] = float((v & 0x180) != 0) + float((v & 0x100) != 0)  # without drains (2: multiply form)
+        f[26] = float((v & 0x380) != 0) + float((v & 0x300) != 0)  # without drains (2: multiply form)
+        f[25] = float((v & 0x200) != 0)                  # one crossing test per round
     # size x candidate interactions: the best tile depth, block and CTAs per SM move with the size
     f[28] = f[11] * f[18]
     f[29] = f[11] * f[19]

@@ -35,7 +35,7 @@ def test_golden_histograms(env):
         np.testing.assert_array_equal(bins.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 4, 8, 0x11, 0x12, 0x14, 0x18, 0x20, 0x30, 0x40, 0x80, 0x100])
+@pytest.mark.parametrize("variant", [0, 1, 2, 4, 8, 0x11, 0x12, 0x14, 0x18, 0x20, 0x30, 0x40, 0x80, 0x100, 0x200])
 @pytest.mark.parametrize("nbins", [16, 1000, 4096, 1 << 16])
 def test_histogram_variants(env, variant, nbins):
     """Every privatisation variant (cluster size 1/2/4/8, with/without warp
@@ -56,14 +56,16 @@ def test_histogram_variants(env, variant, nbins):
     np.testing.assert_array_equal(bins.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("variant", [0x20, 0x30, 0, 0x80, 0x100])
+@pytest.mark.parametrize("variant", [0x20, 0x30, 0, 0x80, 0x100, 0x200])
 def test_hist16_saturating_bins(env, variant):
     """16-bit privatised counters: one bin taking every key, and two bins
-    sharing one 32-bit word both taking millions of keys, stay exact."""
+    sharing one 32-bit word both taking millions of keys (low halves, then
+    a low and a high half), stay exact."""
     gbk, torch = env
     nb = 1 << 16
     for keys in (np.full(3000001, 7, dtype=np.int32),
-                 np.tile(np.array([6, 7, 7, 6, 6, 9], dtype=np.int32), 1000003)):
+                 np.tile(np.array([6, 7, 7, 6, 6, 9], dtype=np.int32), 1000003),
+                 np.tile(np.array([7, 32775, 32775, 7, 65535, 32775], dtype=np.int32), 1000003)):
         bins = torch.zeros(nb, dtype=torch.int64, device="cuda")
         gbk.histogram(_dev(torch, keys), bins, tune=(0, 0, 0, variant))
         gbk.stream_check()
@@ -85,7 +87,7 @@ def test_hist16_saturating_ragged_words(env, variant):
     np.testing.assert_array_equal(bins.cpu().numpy(), np.bincount(keys, minlength=nb))
 
 
-@pytest.mark.parametrize("variant", [0, 0x20, 0x80, 0x100])
+@pytest.mark.parametrize("variant", [0, 0x20, 0x80, 0x100, 0x200])
 @pytest.mark.parametrize("offset", [1, 2, 3])
 def test_hist16_unaligned_keys(env, variant, offset):
     """Keys that start off the 16-byte boundary (a ragged head and tail go
@@ -131,7 +133,7 @@ def test_out_of_range_keys_flagged(env):
     gbk.stream_check()  # the flag was cleared
 
 
-@pytest.mark.parametrize("variant", [0x20, 0x30, 0x80, 0x100])
+@pytest.mark.parametrize("variant", [0x20, 0x30, 0x80, 0x100, 0x200])
 def test_hist16_out_of_range_keys(env, variant):
     """16-bit counters: keys below 0 or at and above nbins (odd nbins, so
     the last word's high half is not a bin) are left out of every bin and
@@ -148,6 +150,28 @@ def test_hist16_out_of_range_keys(env, variant):
     ok = keys[(keys >= 0) & (keys < nb)]
     np.testing.assert_array_equal(bins.cpu().numpy(), np.bincount(ok, minlength=nb))
     gbk.stream_check()
+
+
+@pytest.mark.parametrize("variant", [0x100, 0x200])
+def test_hist16_multiply_form_out_of_range_keys(env, variant):
+    """The multiply forms (power-of-two bins): rounds holding a key below 0 or
+    at and above nbins take the general path; those keys raise the key-range
+    status and the rest count exactly."""
+    gbk, torch = env
+    from kokkos_gb300 import datagen
+    nb = 1 << 15
+    for lo, hi, n in ((-3, nb + 3, 2000003), (0, nb - 1, 1999999)):
+        keys = datagen.uniform_i64(n, lo, hi, seed=5).astype(np.int32)
+        if lo == 0:
+            keys[::100003] = nb  # a few rounds with one bad key
+        bins = torch.zeros(nb, dtype=torch.int64, device="cuda")
+        gbk.histogram(_dev(torch, keys), bins, tune=(0, 0, 0, variant))
+        with pytest.raises(gbk.GbkError) as e:
+            gbk.stream_check()
+        assert e.value.status == 6
+        ok = keys[(keys >= 0) & (keys < nb)]
+        np.testing.assert_array_equal(bins.cpu().numpy(), np.bincount(ok, minlength=nb))
+        gbk.stream_check()
 
 
 @pytest.mark.parametrize("op", ["sum", "min", "max", "prod"])
