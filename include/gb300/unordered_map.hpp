@@ -177,9 +177,8 @@ class UnorderedMap {
         if (s == Impl::kSlotEmpty) {
           keys_.data()[i] = k;
           if (!is_set) values_.data()[i] = v;
-          __threadfence();
-          gbk::st_release_u32(state_.data() + i, Impl::kSlotValid);
-          atomicAdd(scalars_.data() + 0, 1u);
+          gbk::st_release_u32(state_.data() + i, Impl::kSlotValid);  // orders the key and value before it
+          count_size(1);
           return insert_result(i, insert_result::kSuccess, p);
         }
       }
@@ -237,7 +236,7 @@ class UnorderedMap {
     const uint32_t i = find(k);
     if (i == invalid_index) return false;
     if (atomicCAS(state_.data() + i, Impl::kSlotValid, Impl::kSlotErased) != Impl::kSlotValid) return false;
-    atomicSub(scalars_.data() + 0, 1u);
+    count_size(-1);
     return true;
 #else
     (void)k;
@@ -278,6 +277,14 @@ class UnorderedMap {
     check_cuda(cudaMemcpy(scalars_.data() + k, &v, 4, cudaMemcpyHostToDevice), "UnorderedMap");
   }
 #ifdef __CUDA_ARCH__
+  // size += d for every lane of the warp that reaches this call together:
+  // one atomic per group of lanes instead of one per entry, so inserts of
+  // distinct keys do not serialise on the one size word.
+  __device__ void count_size(int d) const {
+    const unsigned g = __activemask();
+    const int lead = __ffs(g) - 1;
+    if ((int)(threadIdx.x & 31) == lead) atomicAdd(scalars_.data() + 0, (uint32_t)(d * __popc(g)));
+  }
   // A slot being written by another insert: wait (bounded) until it is
   // published; on a wait that gives up, record it and report failure.
   __device__ bool wait_valid(uint32_t i, uint32_t* s) const {

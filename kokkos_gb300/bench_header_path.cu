@@ -11,12 +11,27 @@
 //                    reduce, single(PerTeam) store, over the lognormal
 //                    segments whose int64 offsets are in argv[1]; vs
 //                    gbk_segmented_reduce
+//   umap_insert_u32: UnorderedMap<uint32_t, uint32_t> AtomicAdd inserts of
+//                    2^24 keys drawn from 2^23 values (table of 2^24 slots,
+//                    emptied before each call), then a find of each key;
+//                    the size is checked against the distinct keys counted
+//                    on the host
+//   bitset_set:      Bitset of 2^27 bits, 2^24 set() calls at hashed bits
 //   bench_header_path <offsets.bin> <nseg> <reps>
 #include <Kokkos_GB300.hpp>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
+
+// keys of the UnorderedMap and Bitset runs (splitmix64 finaliser of i)
+__host__ __device__ inline uint32_t bench_key(uint64_t i, uint32_t mask) {
+  uint64_t z = i + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return (uint32_t)(z ^ (z >> 31)) & mask;
+}
 
 template <class F>
 static double time_us(int reps, F&& f) {
@@ -111,6 +126,58 @@ int main(int argc, char** argv) {
     const double t_team_lib = time_us(reps, [&](int) {
       gbk_segmented_reduce(GBK_SUM, GBK_F32, v.data(), doff.data(), nseg, ns, segs.data(), (gbk_stream_t)s, nullptr);
     });
+    // ---- UnorderedMap inserts and finds, Bitset sets ---------------------
+    const uint32_t nk = 1u << 24, nu = 1u << 23;
+    Kokkos::View<uint32_t*> ks("ks", nk), fidx("fidx", nk);
+    Kokkos::parallel_for(Kokkos::RangePolicy<>(0, (int64_t)nk),
+                         KOKKOS_LAMBDA(int64_t i) { ks(i) = bench_key((uint64_t)i, nu - 1); });
+    Kokkos::UnorderedMap<uint32_t, uint32_t> map(nu);
+    using AddOp = Kokkos::UnorderedMapInsertOpTypes<Kokkos::View<uint32_t*>, uint32_t>::AtomicAdd;
+    cudaEvent_t ea, eb;
+    cudaEventCreate(&ea);
+    cudaEventCreate(&eb);
+    double t_ins = 0;
+    for (int r = 0; r < 3 + reps; ++r) {
+      map.clear();
+      cudaDeviceSynchronize();
+      cudaEventRecord(ea, nullptr);
+      Kokkos::parallel_for(Kokkos::RangePolicy<>(0, (int64_t)nk),
+                           KOKKOS_LAMBDA(int64_t i) { map.insert(ks(i), 1u, AddOp()); });
+      cudaEventRecord(eb, nullptr);
+      cudaEventSynchronize(eb);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ea, eb);
+      if (r >= 3) t_ins += 1000.0 * ms / reps;
+    }
+    const double t_find = time_us(reps, [&](int) {
+      Kokkos::parallel_for(Kokkos::RangePolicy<>(0, (int64_t)nk), KOKKOS_LAMBDA(int64_t i) { fidx(i) = map.find(ks(i)); });
+    });
+    std::vector<uint32_t> hk(nk);
+    for (uint32_t i = 0; i < nk; ++i) hk[i] = bench_key(i, nu - 1);
+    std::sort(hk.begin(), hk.end());
+    const uint32_t distinct = (uint32_t)(std::unique(hk.begin(), hk.end()) - hk.begin());
+    int64_t missing = 0;
+    Kokkos::parallel_reduce(Kokkos::RangePolicy<>(0, (int64_t)nk), KOKKOS_LAMBDA(int64_t i, int64_t& u) {
+      u += (map.valid_at(fidx(i)) && map.key_at(fidx(i)) == ks(i)) ? 0 : 1;
+    }, missing);
+    const bool map_ok = map.size() == distinct && !map.failed_insert() && missing == 0;
+    const unsigned nbits = 1u << 27;
+    Kokkos::Bitset<> bits(nbits);
+    double t_bits = 0;
+    for (int r = 0; r < 3 + reps; ++r) {
+      bits.reset();
+      cudaDeviceSynchronize();
+      cudaEventRecord(ea, nullptr);
+      Kokkos::parallel_for(Kokkos::RangePolicy<>(0, (int64_t)nk),
+                           KOKKOS_LAMBDA(int64_t i) { bits.set(bench_key((uint64_t)i + 77, nbits - 1)); });
+      cudaEventRecord(eb, nullptr);
+      cudaEventSynchronize(eb);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ea, eb);
+      if (r >= 3) t_bits += 1000.0 * ms / reps;
+    }
+    cudaEventDestroy(ea);
+    cudaEventDestroy(eb);
     ex.fence();
     auto gbs = [](double bytes, double us) { return bytes / (us * 1e-6) / 1e9; };
     const double rb = (double)n * 8, mb = (double)n0 * n1 * n2 * 4, tb = (double)ns * 4 + (nseg + 1) * 8.0 + nseg * 4.0;
@@ -119,9 +186,14 @@ int main(int argc, char** argv) {
         "\"library_GB/s\": %.1f}, "
         "\"mdrange_sum_f32_512x512x256\": {\"us\": %.2f, \"GB/s\": %.1f, \"library_us\": %.2f, \"library_GB/s\": %.1f}, "
         "\"team_sum_f32_lognormal_segments\": {\"segments\": %lld, \"elements\": %lld, \"us\": %.2f, \"GB/s\": %.1f, "
-        "\"library_us\": %.2f, \"library_GB/s\": %.1f}}\n",
+        "\"library_us\": %.2f, \"library_GB/s\": %.1f}, "
+        "\"umap_insert_u32\": {\"inserts\": %u, \"distinct\": %u, \"capacity\": %u, \"insert_us\": %.2f, "
+        "\"G_inserts_per_s\": %.3f, \"find_us\": %.2f, \"G_finds_per_s\": %.3f, \"ok\": %s}, "
+        "\"bitset_set\": {\"bits\": %u, \"sets\": %u, \"us\": %.2f, \"G_sets_per_s\": %.3f}}\n",
         t_range, gbs(rb, t_range), t_range_dev, t_range_lib, gbs(rb, t_range_lib), t_md, gbs(mb, t_md), t_md_lib,
-        gbs(mb, t_md_lib), (long long)nseg, (long long)ns, t_team, gbs(tb, t_team), t_team_lib, gbs(tb, t_team_lib));
+        gbs(mb, t_md_lib), (long long)nseg, (long long)ns, t_team, gbs(tb, t_team), t_team_lib, gbs(tb, t_team_lib),
+        nk, distinct, map.capacity(), t_ins, nk / t_ins * 1e-3, t_find, nk / t_find * 1e-3, map_ok ? "true" : "false",
+        nbits, nk, t_bits, nk / t_bits * 1e-3);
   }
   Kokkos::finalize();
   return 0;

@@ -19,13 +19,20 @@
 //   graph:           Experimental::Graph of 8 dependent parallel_for nodes over
 //                    2^16 int64 (y = x + 1) submitted, against the same 8
 //                    parallel_for launched directly
+//   umap_insert_u32: Kokkos::UnorderedMap<uint32_t, uint32_t, GB300> AtomicAdd
+//                    inserts of 2^24 keys drawn from 2^23 values (the map
+//                    emptied before each call), then a find of each key; the
+//                    size is checked against the distinct keys counted on the
+//                    host
 //   backend_bench <offsets.bin> <nseg> <reps>
 #include <Kokkos_Core.hpp>
 #include <Kokkos_ScatterView.hpp>
 #include <Kokkos_Sort.hpp>
 #include <Kokkos_Graph.hpp>
+#include <Kokkos_UnorderedMap.hpp>
 #include <GB300/Kokkos_GB300_Graph_Impl.hpp>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -39,6 +46,14 @@ struct AddOne {
   Kokkos::View<int64_t*, MS> x, y;
   KOKKOS_INLINE_FUNCTION void operator()(int64_t i) const { y(i) = x(i) + 1; }
 };
+
+// keys of the UnorderedMap run (splitmix64 finaliser of i)
+KOKKOS_INLINE_FUNCTION uint32_t bench_key(uint64_t i, uint32_t mask) {
+  uint64_t z = i + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return (uint32_t)(z ^ (z >> 31)) & mask;
+}
 
 template <class F>
 static double time_us(const ES& ex, int reps, F&& f) {
@@ -181,6 +196,44 @@ int main(int argc, char** argv) {
     graph.instantiate();
     const double t_chain = time_us(ex, reps * 10, [&](int) { chain(); });
     const double t_graph = time_us(ex, reps * 10, [&](int) { graph.submit(); });
+    // ---- UnorderedMap: AtomicAdd inserts, then finds --------------------------
+    const uint32_t unk = 1u << 24, unu = 1u << 23;
+    Kokkos::View<uint32_t*, MS> uks("uks", unk), ufx("ufx", unk);
+    Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, unk),
+                         KOKKOS_LAMBDA(int64_t i) { uks(i) = bench_key((uint64_t)i, unu - 1); });
+    using UMap = Kokkos::UnorderedMap<uint32_t, uint32_t, ES>;
+    using UAdd =
+        Kokkos::UnorderedMapInsertOpTypes<Kokkos::View<uint32_t*, typename UMap::device_type>, uint32_t>::AtomicAdd;
+    UMap umap(unu);
+    cudaEvent_t ua, ub;
+    cudaEventCreate(&ua);
+    cudaEventCreate(&ub);
+    double t_uins = 0;
+    for (int r = 0; r < 3 + reps; ++r) {
+      umap.clear();
+      ex.fence();
+      cudaEventRecord(ua, ex.stream());
+      Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, unk), KOKKOS_LAMBDA(int64_t i) { umap.insert(uks(i), 1u, UAdd()); });
+      cudaEventRecord(ub, ex.stream());
+      cudaEventSynchronize(ub);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ua, ub);
+      if (r >= 3) t_uins += 1000.0 * ms / reps;
+    }
+    cudaEventDestroy(ua);
+    cudaEventDestroy(ub);
+    const double t_ufind = time_us(ex, reps, [&](int) {
+      Kokkos::parallel_for(Kokkos::RangePolicy<ES>(ex, 0, unk), KOKKOS_LAMBDA(int64_t i) { ufx(i) = umap.find(uks(i)); });
+    });
+    std::vector<uint32_t> hks(unk);
+    for (uint32_t i = 0; i < unk; ++i) hks[i] = bench_key(i, unu - 1);
+    std::sort(hks.begin(), hks.end());
+    const uint32_t udistinct = (uint32_t)(std::unique(hks.begin(), hks.end()) - hks.begin());
+    int64_t umissing = 0;
+    Kokkos::parallel_reduce(Kokkos::RangePolicy<ES>(ex, 0, unk), KOKKOS_LAMBDA(int64_t i, int64_t& u) {
+      u += (umap.valid_at(ufx(i)) && umap.key_at(ufx(i)) == uks(i)) ? 0 : 1;
+    }, umissing);
+    const bool umap_ok = umap.size() == udistinct && !umap.failed_insert() && umissing == 0;
     ex.fence();
     const double rb = (double)n * 8, mb = (double)n0 * n1 * n2 * 4, tb = (double)ns * 4 + (nseg + 1) * 8.0 + nseg * 4.0;
     const double hb = (double)nk * 4 + nb * 8.0;
@@ -190,10 +243,14 @@ int main(int argc, char** argv) {
         "\"team_sum_f32_lognormal_segments\": {\"segments\": %lld, \"elements\": %lld, \"us\": %.2f, \"GB/s\": %.1f}, "
         "\"scatterview_hist_2^26_keys_2^16_bins\": {\"us\": %.2f, \"GB/s\": %.1f, \"log_uniform_keys_us\": %.2f}, "
         "\"sort_u64_2^27\": {\"ms\": %.3f, \"Gkeys_per_s\": %.2f}, "
-        "\"graph_8_parallel_for_2^16\": {\"graph_us\": %.2f, \"launches_us\": %.2f}}\n",
+        "\"graph_8_parallel_for_2^16\": {\"graph_us\": %.2f, \"launches_us\": %.2f}, "
+        "\"umap_insert_u32\": {\"inserts\": %u, \"distinct\": %u, \"capacity\": %u, \"insert_us\": %.2f, "
+        "\"G_inserts_per_s\": %.3f, \"find_us\": %.2f, \"G_finds_per_s\": %.3f, \"ok\": %s}}\n",
         t_range_host, t_range_dev, gbs(rb, t_range_dev), t_md, gbs(mb, t_md), (long long)nseg, (long long)ns, t_team,
         gbs(tb, t_team), t_hist, gbs(hb, t_hist), t_hist_skew, (t_sort_fill - t_fill) / 1000.0,
-        (double)nsort / ((t_sort_fill - t_fill) * 1e-6) / 1e9, t_graph, t_chain);
+        (double)nsort / ((t_sort_fill - t_fill) * 1e-6) / 1e9, t_graph, t_chain, unk, udistinct,
+        (unsigned)umap.capacity(), t_uins, unk / t_uins * 1e-3, t_ufind, unk / t_ufind * 1e-3,
+        umap_ok ? "true" : "false");
   }
   Kokkos::finalize();
   return 0;
