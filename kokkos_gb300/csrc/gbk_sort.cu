@@ -99,8 +99,7 @@ __device__ __forceinline__ unsigned digit_peers(unsigned d, bool ok) {
 // the lanes below holding d.  The lowest lane of each digit group advances
 // cnt[d].
 template <bool ALL>
-__device__ __forceinline__ unsigned rank_row(unsigned short* cnt, unsigned d, bool ok, int lane) {
-  const unsigned m = digit_peers<ALL>(d, ok);
+__device__ __forceinline__ unsigned rank_peers(unsigned short* cnt, unsigned d, bool ok, int lane, unsigned m) {
   const int leader = __ffs(m) - 1;
   unsigned b = 0;
   if (ok && lane == leader) {
@@ -111,12 +110,23 @@ __device__ __forceinline__ unsigned rank_row(unsigned short* cnt, unsigned d, bo
   __syncwarp();
   return b + (unsigned)__popc(m & ((1u << lane) - 1u));
 }
+template <bool ALL>
+__device__ __forceinline__ unsigned rank_row(unsigned short* cnt, unsigned d, bool ok, int lane) {
+  return rank_peers<ALL>(cnt, d, ok, lane, digit_peers<ALL>(d, ok));
+}
+// The same with the peer set from one match.any over the digit.
+template <bool ALL>
+__device__ __forceinline__ unsigned rank_row_match(unsigned short* cnt, unsigned d, bool ok, int lane) {
+  unsigned m = __match_any_sync(0xffffffffu, d);
+  if (!ALL) m &= __ballot_sync(0xffffffffu, ok);
+  return rank_peers<ALL>(cnt, d, ok, lane, m);
+}
 
 // The same rank from a per-warp array of 256 lane masks in shared memory
 // (zero between rows): every lane ORs its bit into its digit's mask, reads
 // the mask back as its peer set, and the group's lowest lane advances the
 // count and clears the mask.  About a third of the instructions of the
-// eight ballots; lanes sharing a digit serialise on its word, so the host
+// eight ballots; lanes sharing a digit serialise on its word, so the plan
 // picks it only for passes where no digit value holds a large share of the
 // keys.
 template <bool ALL>
@@ -151,7 +161,7 @@ struct SortPlan {
   int active[8];   // the pass's digit differs between keys
   int src[8];      // 0: the pass reads the caller's buffers, 1: the temporaries
   int first[8];    // the first active pass (its per-chunk counts come from k_digit_hist)
-  int rank_or[8];  // rank with the shared lane masks: no digit value holds over 1/32 of the keys
+  int rank[8];     // ranking of the pass's scatter: 0 ballots, 1 lane masks, 2 match.any (see k_sort_plan)
   int final_tmp;   // after the last active pass the data is in the temporaries
   int pad[3];
 };
@@ -318,6 +328,15 @@ template <int KB, int VB, int VAR> struct ScShape {
   static_assert(KPT * 32 <= 65535 && TILE <= 65535, "16-bit tile offsets");
 };
 
+// Passes whose rows of 32 keys are expected to hold at most this many
+// distinct digits rank with match.any.  Measured on 2^27 u64 keys + u32
+// values: keys with 2 distinct digits per pass (8 random bits) sort in
+// 4.24 ms with match.any, 5.53 with ballots and 6.03 with lane masks; uniform
+// keys (30 distinct digits per row) in 11.47 / 9.79 / 9.68 ms; on 2^26 keys
+// with 16-40 random bits (passes of 2 to 25 distinct digits per row) the
+// crossing between match.any and the masks lies near 15.
+constexpr float kMatchDistinct = 16.0f;
+
 // One CTA of 256 threads (one per digit): digit starts of every pass and the
 // plan.  A histogram whose counts do not add up to n (keys changed under the
 // sort) marks every pass inactive and raises the bad-state status.
@@ -328,6 +347,7 @@ __global__ void __launch_bounds__(256)
   __shared__ unsigned long long s_w[8];
   __shared__ int s_const[KB], s_hot[KB];
   __shared__ unsigned long long s_tot[KB];
+  __shared__ float s_e[8], s_dist[KB];
   const int d = threadIdx.x, lane = d & 31, warp = d >> 5;
   for (int p = 0; p < KB; ++p) {
     const unsigned long long v = hist[p * 256 + d];
@@ -346,12 +366,24 @@ __global__ void __launch_bounds__(256)
       tot += s_w[w];
     }
     off[p * 256 + d] = (int64_t)(pre + inc - v);
+    // expected number of distinct digits among 32 keys: sum over d of
+    // 1 - (1 - share_d)^32
+    float q = 1.0f - (float)v / (float)(n > 0 ? n : 1);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q *= q;
+    float e = 1.0f - q;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if (lane == 0) s_e[warp] = e;
     const int c = __syncthreads_or((int64_t)v == n);
-    const int hot = __syncthreads_or((int64_t)v * 32 > n);
+    const int hot = __syncthreads_or((int64_t)v * 8 > n);
     if (d == 0) {
       s_const[p] = c;
       s_hot[p] = hot;
       s_tot[p] = tot;
+      float de = 0.0f;
+      for (int w = 0; w < 8; ++w) de += s_e[w];
+      s_dist[p] = de;
     }
     __syncthreads();
   }
@@ -365,7 +397,11 @@ __global__ void __launch_bounds__(256)
       plan->active[p] = act;
       plan->src[p] = done & 1;
       plan->first[p] = act && done == 0;
-      plan->rank_or[p] = p < KB && !s_hot[p];
+      // A row of 32 keys with few distinct digits is ranked fastest by
+      // match.any (its cost grows with the distinct values); with many, by
+      // the lane masks, unless one digit holds over 1/8 of the keys (its
+      // word then serialises the masks): the eight ballots.
+      plan->rank[p] = p >= KB ? 0 : s_dist[p] <= kMatchDistinct ? 2 : !s_hot[p] ? 1 : 0;
       done += act;
     }
     plan->final_tmp = done & 1;
@@ -404,7 +440,8 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
   const V* __restrict__ vin = from_tmp ? vt : vu;
   V* __restrict__ vout = from_tmp ? vu : vt;
   const unsigned* counts = plan->first[A.pass] ? A.first_counts : A.counts;
-  const int rank_or = A.rank_mode == 1 ? 1 : A.rank_mode == 2 ? 0 : plan->rank_or[A.pass];
+  // 1: lane masks, 2: match.any, 0: ballots
+  const int rank_by = A.rank_mode == 1 ? 1 : A.rank_mode == 2 ? 0 : A.rank_mode == 3 ? 2 : plan->rank[A.pass];
   using Sh = ScShape<(int)sizeof(K), VB, VAR>;
   constexpr int BLOCK = Sh::BLOCK, KPT = Sh::KPT, TILE = Sh::TILE, STAGES = Sh::STAGES, WARPS = Sh::WARPS;
   extern __shared__ __align__(128) unsigned char ring[];
@@ -491,9 +528,12 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
         if (VB) val[k] = s_vals[slot];
         dig[k] = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
       }
-      if (rank_or) {
+      if (rank_by == 1) {
 #pragma unroll
         for (int k = 0; k < KPT; ++k) rk[k] = rank_row_or<true>(s_cnt[warp], s_rk + warp * 256, dig[k], true, lane);
+      } else if (rank_by == 2) {
+#pragma unroll
+        for (int k = 0; k < KPT; ++k) rk[k] = rank_row_match<true>(s_cnt[warp], dig[k], true, lane);
       } else {
 #pragma unroll
         for (int k = 0; k < KPT; ++k) rk[k] = rank_row<true>(s_cnt[warp], dig[k], true, lane);
@@ -507,10 +547,13 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
         if (VB) val[k] = slot < cv ? s_vals[slot] : (ok ? vin[base + slot] : V(0));
         dig[k] = (unsigned)(Radix<DT>::img(key[k]) >> A.shift) & 255u;
       }
-      if (rank_or) {
+      if (rank_by == 1) {
 #pragma unroll
         for (int k = 0; k < KPT; ++k)
           rk[k] = rank_row_or<false>(s_cnt[warp], s_rk + warp * 256, dig[k], wb + k * 32 + lane < cnt, lane);
+      } else if (rank_by == 2) {
+#pragma unroll
+        for (int k = 0; k < KPT; ++k) rk[k] = rank_row_match<false>(s_cnt[warp], dig[k], wb + k * 32 + lane < cnt, lane);
       } else {
 #pragma unroll
         for (int k = 0; k < KPT; ++k) rk[k] = rank_row<false>(s_cnt[warp], dig[k], wb + k * 32 + lane < cnt, lane);
@@ -573,7 +616,7 @@ __global__ void __launch_bounds__(ScVar<VAR>::BLOCK, ScVar<VAR>::MINB)
       }
     }
     __syncthreads();
-    if (rank_or) {  // s_off is dead: clear the lane masks for the next tile (visible after the loop's barrier)
+    if (rank_by == 1) {  // s_off is dead: clear the lane masks for the next tile (visible after the loop's barrier)
       uint4* z = reinterpret_cast<uint4*>(s_rk);
       for (int i = threadIdx.x; i < WARPS * 256 / 4; i += BLOCK) z[i] = make_uint4(0u, 0u, 0u, 0u);
     }
@@ -650,14 +693,14 @@ __global__ void k_sort_copy_back(const SortPlan* __restrict__ plan, const K* __r
   }
 }
 
-// Ranking of the scatter passes: GBK_SORT_RANK=masks or =ballot in the
-// environment forces one method for every pass; otherwise the plan chooses
-// per pass from the digit histogram.
+// Ranking of the scatter passes: GBK_SORT_RANK=masks, =ballot or =match in
+// the environment forces one method for every pass; otherwise the plan
+// chooses per pass from the digit histogram.
 int sort_rank_mode() {
   static int mode = -1;
   if (mode < 0) {
     const char* e = getenv("GBK_SORT_RANK");
-    mode = (e && !strcmp(e, "masks")) ? 1 : (e && !strcmp(e, "ballot")) ? 2 : 0;
+    mode = (e && !strcmp(e, "masks")) ? 1 : (e && !strcmp(e, "ballot")) ? 2 : (e && !strcmp(e, "match")) ? 3 : 0;
   }
   return mode;
 }
