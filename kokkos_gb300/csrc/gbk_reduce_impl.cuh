@@ -288,14 +288,14 @@ int launch_tma(const T* x, int64_t n, int64_t loc0, void* out, Workspace* w, int
   const int64_t nvec = (n - head) / VEC;
   auto kfn = k_reduce_tma<R, T, BLOCK, CV, STAGES>;
   constexpr size_t dyn = (size_t)STAGES * CV * 16;
-  static int resident = 0;  // CTAs per SM, per instantiation
+  static std::atomic<int> resident{0};  // CTAs per SM, per instantiation (set once, any host thread)
   if (!resident) {
     GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     int r = 0;
     GBK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kfn, BLOCK, dyn));
     resident = r > 0 ? r : 1;
   }
-  const int per_sm = cps > 0 && cps < resident ? cps : resident;
+  const int per_sm = cps > 0 && cps < resident ? cps : resident.load();
   int64_t grid = (int64_t)sm_count() * per_sm;
   const int64_t chunks = (nvec + CV - 1) / CV;
   if (grid > chunks) grid = chunks;

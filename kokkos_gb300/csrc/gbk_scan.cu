@@ -337,7 +337,7 @@ int launch_k_scan(const TI* x, TO* y, int64_t n, TO init, const LbState& S, TO* 
   constexpr size_t in_bytes = (size_t)SCAN_COMPUTE * IPT * 16;
   // stages + out tile
   const size_t dyn = FAST ? STAGES * in_bytes + in_bytes * (sizeof(TO) / sizeof(TI)) / ROUNDS : 0;
-  static int resident = 0;  // CTAs per SM, per instantiation
+  static std::atomic<int> resident{0};  // CTAs per SM, per instantiation (set once, any host thread)
   if (!resident) {
     // Static + dynamic shared memory above 48 KiB needs the opt-in.
     if (dyn) GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
@@ -346,7 +346,7 @@ int launch_k_scan(const TI* x, TO* y, int64_t n, TO init, const LbState& S, TO* 
     if (r < 1) return GBK_ERR_UNSUPPORTED;
     resident = r;
   }
-  const int per_sm = cps > 0 && cps < resident ? cps : resident;
+  const int per_sm = cps > 0 && cps < resident ? cps : resident.load();
   const int64_t grid = std::min<int64_t>(S.ntiles, (int64_t)per_sm * sm_count());
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
@@ -357,7 +357,7 @@ int launch_k_scan(const TI* x, TO* y, int64_t n, TO init, const LbState& S, TO* 
   // (programmatic dependent launch: the kernel waits for it on the device
   // before its first access).  A driver that refuses the pair for a
   // cooperative grid gets the plain cooperative launch from then on.
-  static bool pdl_ok = true;
+  static std::atomic<bool> pdl_ok{true};
   cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;

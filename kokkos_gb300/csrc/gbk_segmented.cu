@@ -782,7 +782,7 @@ int launch_segred(const T* x, T* out, int64_t n, const int64_t* offsets, int64_t
   const int64_t chunks = (nvec + SR_CV - 1) / SR_CV;
   auto kfn = k_segred<R, T>;
   constexpr size_t dyn = (size_t)SR_STAGES * SR_CV * 16;
-  static int resident = 0;  // CTAs per SM, per instantiation
+  static std::atomic<int> resident{0};  // CTAs per SM, per instantiation (set once, any host thread)
   if (!resident) {
     GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     int r = 0;
@@ -843,7 +843,7 @@ int launch_k_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t 
   A.arrive = w->counters + SLOT_SEG;
   A.depart = w->counters + SLOT_SEG + 1;
   auto kfn = k_seg<TI, TO, OP, MODE, FAST, IPT, STG>;
-  static int resident = 0;  // CTAs per SM, per instantiation
+  static std::atomic<int> resident{0};  // CTAs per SM, per instantiation (set once, any host thread)
   if (!resident) {
     GBK_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     int r = 0;
@@ -851,7 +851,7 @@ int launch_k_seg(const TI* x, TO* y, int64_t n, const int64_t* offsets, int64_t 
     if (r < 1) return GBK_ERR_UNSUPPORTED;
     resident = r;
   }
-  const int per_sm = cps > 0 && cps < resident ? cps : resident;
+  const int per_sm = cps > 0 && cps < resident ? cps : resident.load();
   const int64_t grid = std::min<int64_t>(ntiles, (int64_t)per_sm * sm_count());
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);

@@ -659,7 +659,7 @@ int launch_pass(typename Radix<DT>::K* ku, typename Radix<DT>::K* kt, typename V
   cudaStream_t s = w->stream;
   auto cfn = k_chunk_count<DT, TMA>;
   constexpr size_t cdyn = TMA ? (size_t)CNT_STAGES * CNT_STAGE_BYTES : 0;
-  static bool cset = false;
+  static std::atomic<bool> cset{false};
   if (!cset && cdyn) {
     GBK_CUDA_TRY(cudaFuncSetAttribute(cfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cdyn));
     cset = true;
@@ -671,7 +671,7 @@ int launch_pass(typename Radix<DT>::K* ku, typename Radix<DT>::K* kt, typename V
   GBK_CUDA_TRY(cudaGetLastError());
   auto sfn = k_chunk_scatter<DT, VB, TMA, VAR>;
   constexpr size_t sdyn = (size_t)(TMA ? Sh::STAGES : 1) * Sh::STAGE_BYTES;
-  static bool sset = false;
+  static std::atomic<bool> sset{false};
   if (!sset) {
     GBK_CUDA_TRY(cudaFuncSetAttribute(sfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sdyn));
     sset = true;
@@ -697,7 +697,7 @@ __global__ void k_sort_copy_back(const SortPlan* __restrict__ plan, const K* __r
 // the environment forces one method for every pass; otherwise the plan
 // chooses per pass from the digit histogram.
 int sort_rank_mode() {
-  static int mode = -1;
+  static std::atomic<int> mode{-1};
   if (mode < 0) {
     const char* e = getenv("GBK_SORT_RANK");
     mode = (e && !strcmp(e, "masks")) ? 1 : (e && !strcmp(e, "ballot")) ? 2 : (e && !strcmp(e, "match")) ? 3 : 0;

@@ -92,13 +92,13 @@ template <int UNROLL, int FPV>
 int launch_split(const double* x, int64_t n, double* out, Workspace* w, int ctas_per_sm) {
   constexpr int BLOCK = 256;
   auto kfn = k_sum_f64_split<BLOCK, UNROLL, FPV>;
-  static int resident = 0;  // CTAs per SM, per instantiation
+  static std::atomic<int> resident{0};  // CTAs per SM, per instantiation (set once, any host thread)
   if (!resident) {
     int r = 0;
     GBK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kfn, BLOCK, 0));
     resident = r > 0 ? r : 1;
   }
-  const int per_sm = ctas_per_sm > 0 && ctas_per_sm < resident ? ctas_per_sm : resident;
+  const int per_sm = ctas_per_sm > 0 && ctas_per_sm < resident ? ctas_per_sm : resident.load();
   const uintptr_t a = (uintptr_t)x;
   int64_t head = (int64_t)(((16 - (a & 15)) & 15) / sizeof(double));
   if (head > n) head = n;
