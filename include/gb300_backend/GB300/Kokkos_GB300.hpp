@@ -126,6 +126,16 @@ class GB300 {
   void impl_fence_read(const std::string& name, const void* device_src, void* host_dst, size_t bytes) const;
 
   int concurrency() const;  // SMs x 2048 resident threads
+  // An index in [0, concurrency()) for the calling device thread: its SM's
+  // id x 2048 plus its place among the CTAs of its size that fit on one SM
+  // (threads resident on one SM at once can share an index); 0 on the host.
+  KOKKOS_INLINE_FUNCTION static int impl_hardware_thread_id() noexcept {
+    KOKKOS_IF_ON_DEVICE((unsigned sm; asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+                         const unsigned per = 2048u / blockDim.x;
+                         return (int)(sm * 2048u + (blockIdx.x % per) * blockDim.x + threadIdx.x);))
+    KOKKOS_IF_ON_HOST((return 0;))
+  }
+  int impl_max_hardware_threads() const { return concurrency(); }
   void print_configuration(std::ostream& os, bool verbose = false) const;
 
   static void impl_initialize(InitializationSettings const&);

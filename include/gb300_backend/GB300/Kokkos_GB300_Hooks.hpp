@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <string>
 #include <type_traits>
 #include <vector>
 
@@ -145,6 +146,43 @@ constexpr int gb300_sort_dtype() {
   else return -1;
 }
 
+// A strided (non-contiguous) View is sorted in a contiguous copy; values of
+// a size the library does not move (not 4 or 8 bytes) follow the keys through
+// a sorted index permutation and one gather.  The copies are small kernels of
+// their own (this header is read before Kokkos' deep_copy and parallel_for).
+template <class T>
+using GB300SortTemp = Kokkos::View<T*, Kokkos::Experimental::GB300Space>;
+template <class T>
+GB300SortTemp<T> gb300_sort_temp(const Kokkos::Experimental::GB300& exec, const char* label, int64_t n) {
+  return GB300SortTemp<T>(Kokkos::view_alloc(exec, Kokkos::WithoutInitializing, std::string(label)), n);
+}
+template <class Dst, class Src>
+__global__ void k_gb300_copy_view(Dst dst, Src src, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst(i) = src(i);
+}
+template <class P>
+__global__ void k_gb300_iota(P* p, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = (P)i;
+}
+template <class Dst, class Src, class P>
+__global__ void k_gb300_gather(Dst dst, Src src, const P* perm, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst(i) = src(perm[i]);
+}
+inline unsigned gb300_copy_grid(const Kokkos::Experimental::GB300& exec, int64_t n) {
+  int64_t g = (n + 255) / 256;
+  const int64_t cap = (int64_t)exec.sm_count() * 8;
+  return (unsigned)(g < 1 ? 1 : g > cap ? cap : g);
+}
+template <class Dst, class Src>
+void gb300_copy_view(const Kokkos::Experimental::GB300& exec, const Dst& dst, const Src& src, int64_t n) {
+  k_gb300_copy_view<<<gb300_copy_grid(exec, n), 256, 0, exec.stream()>>>(dst, src, n);
+  gb300_check_cuda(cudaGetLastError(), "Kokkos::sort on GB300: copy");
+  gbk_note_launches(1);
+}
+
 template <class DataType, class... Properties>
 void sort_device_view_without_comparator(const Kokkos::Experimental::GB300& exec,
                                          const Kokkos::View<DataType, Properties...>& view) {
@@ -153,10 +191,16 @@ void sort_device_view_without_comparator(const Kokkos::Experimental::GB300& exec
   static_assert(ViewType::rank == 1, "Kokkos::sort: currently only supports rank-1 Views.");
   constexpr int dt = gb300_sort_dtype<T>();
   static_assert(dt >= 0, "Kokkos::sort on GB300: keys must be 4- or 8-byte integers or floating point");
-  if (view.extent(0) <= 1) return;
-  if (!view.span_is_contiguous()) Kokkos::abort("Kokkos::sort on GB300: the View must be contiguous");
-  gb300_check(gbk_sort((gbk_dtype_t)dt, (void*)view.data(), (int64_t)view.extent(0), (gbk_stream_t)exec.stream()),
-              "sort");
+  const int64_t n = (int64_t)view.extent(0);
+  if (n <= 1) return;
+  if (view.span_is_contiguous()) {
+    gb300_check(gbk_sort((gbk_dtype_t)dt, (void*)view.data(), n, (gbk_stream_t)exec.stream()), "sort");
+    return;
+  }
+  auto kt = gb300_sort_temp<T>(exec, "Kokkos::sort keys", n);
+  gb300_copy_view(exec, kt, view, n);
+  gb300_check(gbk_sort((gbk_dtype_t)dt, (void*)kt.data(), n, (gbk_stream_t)exec.stream()), "sort");
+  gb300_copy_view(exec, view, kt, n);
 }
 
 template <class KeysDataType, class... KeysProperties, class ValuesDataType, class... ValuesProperties>
@@ -167,12 +211,41 @@ void sort_by_key_device_view_without_comparator(const Kokkos::Experimental::GB30
   using V = typename Kokkos::View<ValuesDataType, ValuesProperties...>::non_const_value_type;
   constexpr int dt = gb300_sort_dtype<K>();
   static_assert(dt >= 0, "Kokkos::sort_by_key on GB300: keys must be 4- or 8-byte integers or floating point");
-  static_assert(sizeof(V) == 4 || sizeof(V) == 8, "Kokkos::sort_by_key on GB300: values of 4 or 8 bytes");
-  if (!keys.span_is_contiguous() || !values.span_is_contiguous())
-    Kokkos::abort("Kokkos::sort_by_key on GB300: the Views must be contiguous");
-  gb300_check(gbk_sort_by_key((gbk_dtype_t)dt, (void*)keys.data(), (int)sizeof(V), (void*)values.data(),
-                              (int64_t)keys.extent(0), (gbk_stream_t)exec.stream()),
-              "sort_by_key");
+  constexpr bool MOVED = sizeof(V) == 4 || sizeof(V) == 8;  // values the library moves with the keys
+  const int64_t n = (int64_t)keys.extent(0);
+  if (n <= 1) return;
+  const gbk_stream_t s = (gbk_stream_t)exec.stream();
+  if constexpr (MOVED) {
+    if (keys.span_is_contiguous() && values.span_is_contiguous()) {
+      gb300_check(gbk_sort_by_key((gbk_dtype_t)dt, (void*)keys.data(), (int)sizeof(V), (void*)values.data(), n, s),
+                  "sort_by_key");
+      return;
+    }
+  }
+  auto kt = gb300_sort_temp<K>(exec, "Kokkos::sort_by_key keys", n);
+  gb300_copy_view(exec, kt, keys, n);
+  if constexpr (MOVED) {
+    auto vt = gb300_sort_temp<V>(exec, "Kokkos::sort_by_key values", n);
+    gb300_copy_view(exec, vt, values, n);
+    gb300_check(gbk_sort_by_key((gbk_dtype_t)dt, (void*)kt.data(), (int)sizeof(V), (void*)vt.data(), n, s),
+                "sort_by_key");
+    gb300_copy_view(exec, values, vt, n);
+  } else {
+    // the stable permutation, then the values gathered through it
+    using P = uint64_t;
+    auto perm = gb300_sort_temp<P>(exec, "Kokkos::sort_by_key permutation", n);
+    k_gb300_iota<P><<<gb300_copy_grid(exec, n), 256, 0, exec.stream()>>>(perm.data(), n);
+    gb300_check_cuda(cudaGetLastError(), "Kokkos::sort_by_key on GB300: permutation");
+    gbk_note_launches(1);
+    gb300_check(gbk_sort_by_key((gbk_dtype_t)dt, (void*)kt.data(), (int)sizeof(P), (void*)perm.data(), n, s),
+                "sort_by_key");
+    auto vt = gb300_sort_temp<V>(exec, "Kokkos::sort_by_key values", n);
+    k_gb300_gather<<<gb300_copy_grid(exec, n), 256, 0, exec.stream()>>>(vt, values, perm.data(), n);
+    gb300_check_cuda(cudaGetLastError(), "Kokkos::sort_by_key on GB300: gather");
+    gbk_note_launches(1);
+    gb300_copy_view(exec, values, vt, n);
+  }
+  gb300_copy_view(exec, keys, kt, n);
 }
 
 }  // namespace Impl

@@ -79,17 +79,24 @@ constexpr int gb300_value_bytes() {
 // Runs a reduce skeleton and delivers the value: to a device-accessible
 // result in place, to a host result by a copy and a fence (the reference's
 // rule, Kokkos_Cuda_Parallel_Range.hpp:343-367).
+// `extra` bytes of the workspace after the partials (256-byte aligned) go to
+// a launch that takes them as a fifth argument.
 template <int VB, class ReducerType, class Launch>
 void gb300_run_reduce(const Kokkos::Experimental::GB300& exec, const ReducerType& reducer, int64_t grid,
-                      typename ReducerType::pointer_type result, bool result_on_device, Launch&& launch) {
+                      typename ReducerType::pointer_type result, bool result_on_device, Launch&& launch,
+                      size_t extra = 0) {
   using V = gbk_skel::Val<VB>;
   const size_t vsize = reducer.value_size();
   if (vsize > (size_t)VB)
     gb300_check(GBK_ERR_UNSUPPORTED, "parallel_reduce on GB300: reduction value larger than 256 bytes");
-  GB300Scratch sc = gb300_scratch(exec, 256 + (size_t)(grid + 1) * sizeof(V));
+  const size_t head = (256 + (size_t)(grid + 1) * sizeof(V) + 255) / 256 * 256;
+  GB300Scratch sc = gb300_scratch(exec, head + extra);
   V* dev_out = reinterpret_cast<V*>(sc.base + 256);
   V* partials = dev_out + 1;
-  launch(partials, sc.counters + gbk_skel::kSlotReduce, dev_out, sc.err);
+  if constexpr (std::is_invocable_v<Launch, V*, unsigned*, V*, int*, char*>)
+    launch(partials, sc.counters + gbk_skel::kSlotReduce, dev_out, sc.err, sc.base + head);
+  else
+    launch(partials, sc.counters + gbk_skel::kSlotReduce, dev_out, sc.err);
   gb300_launched("parallel_reduce");
   if (!result) return;
   if (result_on_device) {

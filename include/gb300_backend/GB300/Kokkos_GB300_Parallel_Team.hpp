@@ -10,8 +10,10 @@
 // at most SMs x (2048 / team_size) CTAs; level-0 team scratch (and per-thread
 // scratch x team size) is the CTA's dynamic shared memory.  Team sizes need
 // not be a multiple of 32: every team-wide join handles a partial last warp.
-// Level-1 scratch is not provided (a request for it is rejected when the
-// policy is built).
+// Level-1 scratch is global memory: each CTA owns one slice of the stream's
+// workspace (the launch's grid x the policy's level-1 bytes, 256-byte
+// aligned slices) and hands it to each team it runs, as a team's scratch
+// lives only as long as the team.
 #ifndef KOKKOS_GB300_PARALLEL_TEAM_HPP_
 #define KOKKOS_GB300_PARALLEL_TEAM_HPP_
 
@@ -37,6 +39,15 @@ struct GB300ReducerOps {
   using V = typename ReducerType::value_type;
   __device__ void init(void* v) const { r.init(*static_cast<V*>(v)); }
   __device__ void join(void* d, const void* s) const { r.join(*static_cast<V*>(d), *static_cast<const V*>(s)); }
+};
+// A reducer wrapped by FunctorAnalysis (pointer interface: init / join /
+// final on value_type*), as the nested reductions use it.
+template <class WR>
+struct GB300WrappedOps {
+  const WR& r;
+  using V = typename WR::value_type;
+  __device__ void init(void* v) const { r.init(static_cast<V*>(v)); }
+  __device__ void join(void* d, const void* s) const { r.join(static_cast<V*>(d), static_cast<const V*>(s)); }
 };
 template <class V>
 struct GB300PlusOps {
@@ -72,8 +83,9 @@ class GB300TeamMember {
   }
 
  public:
-  KOKKOS_INLINE_FUNCTION GB300TeamMember(void* shmem, int shmem_size, int league_rank, int league_size)
-      : m_team_shared(shmem, shmem_size), m_league_rank(league_rank), m_league_size(league_size) {}
+  KOKKOS_INLINE_FUNCTION GB300TeamMember(void* shmem, int shmem_size, int league_rank, int league_size,
+                                         void* l1 = nullptr, size_t l1_size = 0)
+      : m_team_shared(shmem, (size_t)shmem_size, l1, l1_size), m_league_rank(league_rank), m_league_size(league_size) {}
 
   KOKKOS_INLINE_FUNCTION int league_rank() const { return m_league_rank; }
   KOKKOS_INLINE_FUNCTION int league_size() const { return m_league_size; }
@@ -123,6 +135,15 @@ class GB300TeamMember {
     (void)reducer;
     (void)value;
     KOKKOS_IF_ON_DEVICE((reducer.reference() = allreduce(GB300ReducerOps<ReducerType>{reducer}, value);))
+  }
+
+  // value joined over the team with a FunctorAnalysis-wrapped reducer (the
+  // nested reductions: a reducer, or a closure with its own join / init).
+  template <class WR>
+  KOKKOS_INLINE_FUNCTION void impl_team_reduce_wrapped(const WR& wr, typename WR::value_type& value) const {
+    (void)wr;
+    (void)value;
+    KOKKOS_IF_ON_DEVICE((value = allreduce(GB300WrappedOps<WR>{wr}, value);))
   }
 
   // Exclusive prefix (team_rank order) of value; the team's total is added
@@ -208,8 +229,6 @@ class TeamPolicyInternal<Kokkos::Experimental::GB300, Properties...> : public Po
 
   void check() const {
     if (m_team_size > 1024) Kokkos::abort("Kokkos::TeamPolicy<GB300>: team size above 1024");
-    if (m_team_scratch_size[1] || m_thread_scratch_size[1])
-      Kokkos::abort("Kokkos::TeamPolicy<GB300>: level-1 scratch is not provided on this space");
   }
 
  public:
@@ -290,7 +309,8 @@ class TeamPolicyInternal<Kokkos::Experimental::GB300, Properties...> : public Po
   bool impl_auto_vector_length() const { return false; }
   void impl_set_team_size(size_t t) { m_team_size = (int)t; }
   void impl_set_vector_length(size_t) {}
-  static int scratch_size_max(int level) { return level == 0 ? 160 * 1024 : 0; }
+  // level 1: as the CUDA space, 20 MiB per team
+  static int scratch_size_max(int level) { return level == 0 ? 160 * 1024 : 20 * 1024 * 1024; }
   size_t scratch_size(const int& level, int team_size_ = -1) const {
     if (team_size_ < 0) team_size_ = m_team_size;
     return m_team_scratch_size[level] + (size_t)team_size_ * m_thread_scratch_size[level];
@@ -326,12 +346,26 @@ template <class Policy>
 // One CTA per league rank, up to max_grid CTAs (then each strides): the block
 // scheduler hands the next team to whichever SM frees up first, so a long
 // team does not hold back the teams that would have followed it on its CTA.
-void gb300_team_shape(const Policy& p, const void* kernel, int64_t max_grid, int64_t* grid, int* shmem) {
+// With level-1 scratch the grid is the resident CTAs at most (each holds a
+// slice of global memory): *l1 is the size a team sees (what the policy asked
+// for, exactly) and *l1_stride the slice's 256-byte-aligned stride.
+// extra_l0: the functor's own team_shmem_size(team_size), added to the
+// policy's level-0 bytes as the reference does.
+void gb300_team_shape(const Policy& p, const void* kernel, int64_t max_grid, int64_t* grid, int* shmem,
+                      size_t* l1 = nullptr, size_t* l1_stride = nullptr, size_t extra_l0 = 0) {
   const int ts = p.team_size();
-  *shmem = (int)p.scratch_size(0, ts);
+  *shmem = (int)(p.scratch_size(0, ts) + extra_l0);
   if (*shmem > 48 * 1024)
     gb300_check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, *shmem),
                      "TeamPolicy scratch");
+  const size_t l1req = p.scratch_size(1, ts);
+  const size_t l1b = (l1req + 255) / 256 * 256;
+  if (l1) *l1 = l1req;
+  if (l1_stride) *l1_stride = l1b;
+  if (l1b) {
+    const int64_t resident = (int64_t)p.space().sm_count() * (2048 / (ts > 0 ? ts : 1));
+    if (max_grid > resident) max_grid = resident;
+  }
   int64_t g = p.league_size();
   if (g > max_grid) g = max_grid;
   *grid = g < 1 ? 1 : g;
@@ -353,8 +387,12 @@ class ParallelFor<FunctorType, Kokkos::TeamPolicy<Properties...>, Kokkos::Experi
   struct Closure {
     FunctorType f;
     int shmem;
+    char* l1;          // level-1 slices, one per CTA
+    size_t l1_size;    // a team's level-1 bytes
+    size_t l1_stride;  // slice stride
     __device__ void exec_team(int64_t lr, int64_t league, unsigned char* sm) const {
-      gb300_call<WorkTag>(f, GB300TeamMember(sm, shmem, (int)lr, (int)league));
+      gb300_call<WorkTag>(f, GB300TeamMember(sm, shmem, (int)lr, (int)league,
+                                             l1 ? l1 + (size_t)blockIdx.x * l1_stride : nullptr, l1_size));
     }
   };
 
@@ -367,10 +405,12 @@ class ParallelFor<FunctorType, Kokkos::TeamPolicy<Properties...>, Kokkos::Experi
     const auto& exec = m_policy.space();
     int64_t g = 1;
     int shmem = 0;
-    gb300_team_shape(m_policy, (const void*)gbk_skel::k_team_for<Closure>, int64_t(1) << 20, &g, &shmem);
-    int* err = gb300_scratch(exec, 0).err;
+    size_t l1 = 0, l1s = 0;
+    gb300_team_shape(m_policy, (const void*)gbk_skel::k_team_for<Closure>, int64_t(1) << 20, &g, &shmem, &l1,
+                     &l1s, FunctorTeamShmemSize<FunctorType>::value(m_functor, m_policy.team_size()));
+    GB300Scratch sc = gb300_scratch(exec, (size_t)g * l1s);
     gbk_skel::k_team_for<Closure><<<(unsigned)g, m_policy.team_size(), shmem, exec.stream()>>>(
-        Closure{m_functor, shmem}, m_policy.league_size(), err);
+        Closure{m_functor, shmem, l1s ? sc.base : nullptr, l1, l1s}, m_policy.league_size(), sc.err);
     gb300_launched("parallel_for(TeamPolicy)");
   }
 };
@@ -399,8 +439,13 @@ class ParallelReduce<CombinedFunctorReducerType, Kokkos::TeamPolicy<Properties..
   struct Closure : GB300ValueOps<ReducerType> {
     FunctorType f;
     int shmem;
+    char* l1;          // level-1 slices, one per CTA
+    size_t l1_size;    // a team's level-1 bytes
+    size_t l1_stride;  // slice stride
     __device__ void exec_team(int64_t lr, int64_t league, unsigned char* sm, void* v) const {
-      gb300_call<WorkTag>(f, GB300TeamMember(sm, shmem, (int)lr, (int)league),
+      gb300_call<WorkTag>(f,
+                          GB300TeamMember(sm, shmem, (int)lr, (int)league,
+                                          l1 ? l1 + (size_t)blockIdx.x * l1_stride : nullptr, l1_size),
                           this->r.reference(static_cast<pointer_type>(v)));
     }
   };
@@ -421,15 +466,21 @@ class ParallelReduce<CombinedFunctorReducerType, Kokkos::TeamPolicy<Properties..
     const auto& exec = m_policy.space();
     int64_t g = 1;
     int shmem = 0;
-    gb300_team_shape(m_policy, (const void*)gbk_skel::k_team_reduce<VB, Closure>, int64_t(1) << 16, &g, &shmem);
+    size_t l1 = 0, l1s = 0;
+    gb300_team_shape(m_policy, (const void*)gbk_skel::k_team_reduce<VB, Closure>, int64_t(1) << 16, &g, &shmem,
+                     &l1, &l1s,
+                     FunctorTeamShmemSize<FunctorType>::value(m_functor_reducer.get_functor(), m_policy.team_size()));
     const int64_t league = m_policy.league_size() > 0 ? m_policy.league_size() : 0;
-    Closure c{{m_functor_reducer.get_reducer()}, m_functor_reducer.get_functor(), shmem};
+    Closure c{{m_functor_reducer.get_reducer()}, m_functor_reducer.get_functor(), shmem, nullptr, l1, l1s};
     const int ts = m_policy.team_size();
+    // the level-1 slices follow the reduce's partials in the stream's workspace
     gb300_run_reduce<VB>(exec, m_functor_reducer.get_reducer(), g, m_result_ptr, m_result_ptr_device_accessible,
-                         [&](gbk_skel::Val<VB>* part, unsigned* ctr, gbk_skel::Val<VB>* out, int* err) {
+                         [&](gbk_skel::Val<VB>* part, unsigned* ctr, gbk_skel::Val<VB>* out, int* err, char* extra) {
+                           if (l1s) c.l1 = extra;
                            gbk_skel::k_team_reduce<VB, Closure><<<(unsigned)g, ts, shmem, exec.stream()>>>(
                                c, league, part, ctr, out, err);
-                         });
+                         },
+                         (size_t)g * l1s);
   }
 };
 
@@ -548,9 +599,13 @@ KOKKOS_INLINE_FUNCTION Impl::VectorSingleStruct<Impl::GB300TeamMember> PerThread
     (void)b;                                                                                                        \
     (void)closure;                                                                                                  \
     (void)reducer;                                                                                                  \
-    KOKKOS_IF_ON_DEVICE((typename ReducerType::value_type v; reducer.init(v);                                       \
+    KOKKOS_IF_ON_DEVICE((using value_type = typename ReducerType::value_type;                                      \
+                         using WR = typename Kokkos::Impl::FunctorAnalysis<                                         \
+                             Kokkos::Impl::FunctorPatternInterface::REDUCE,                                         \
+                             Kokkos::TeamPolicy<Kokkos::Experimental::GB300>, ReducerType, value_type>::Reducer;    \
+                         WR wr(reducer); value_type v; wr.init(&v);                                                 \
                          Impl::gb300_team_walk(b, [&](iType i) { closure(i, v); });                                 \
-                         b.member.team_reduce(reducer, v);))                                                        \
+                         b.member.impl_team_reduce_wrapped(wr, v); wr.final(&v); reducer.reference() = v;))         \
   }                                                                                                                 \
   template <typename iType, class Closure, class ValueType>                                                        \
   KOKKOS_INLINE_FUNCTION std::enable_if_t<!Kokkos::is_reducer<ValueType>::value> parallel_reduce(                  \
@@ -558,8 +613,13 @@ KOKKOS_INLINE_FUNCTION Impl::VectorSingleStruct<Impl::GB300TeamMember> PerThread
     (void)b;                                                                                                        \
     (void)closure;                                                                                                  \
     (void)result;                                                                                                   \
-    KOKKOS_IF_ON_DEVICE((ValueType v = ValueType(); Impl::gb300_team_walk(b, [&](iType i) { closure(i, v); });      \
-                         Kokkos::Sum<ValueType> r(result); b.member.team_reduce(r, v);))                            \
+    KOKKOS_IF_ON_DEVICE((using WR = typename Kokkos::Impl::FunctorAnalysis<                                         \
+                             Kokkos::Impl::FunctorPatternInterface::REDUCE,                                         \
+                             Kokkos::TeamPolicy<Kokkos::Experimental::GB300>, Closure, ValueType>::Reducer;         \
+                         using value_type = typename WR::value_type;                                                \
+                         WR wr(closure); value_type v{}; wr.init(&v);                                               \
+                         Impl::gb300_team_walk(b, [&](iType i) { closure(i, v); });                                 \
+                         b.member.impl_team_reduce_wrapped(wr, v); wr.final(&v); result = v;))                      \
   }                                                                                                                 \
   /* scan: the team's indices in order; each thread folds its own strided */                                      \
   /* indices, so the scan runs in rounds of team_size consecutive indices */                                       \
@@ -605,17 +665,32 @@ template <typename iType, class Closure, class ReducerType>
 KOKKOS_INLINE_FUNCTION std::enable_if_t<Kokkos::is_reducer<ReducerType>::value> parallel_reduce(
     const Impl::ThreadVectorRangeBoundariesStruct<iType, Impl::GB300TeamMember>& b, const Closure& closure,
     const ReducerType& reducer) {
-  typename ReducerType::value_type v;
-  reducer.init(v);
+  using value_type = typename ReducerType::value_type;
+  using WR = typename Kokkos::Impl::FunctorAnalysis<Kokkos::Impl::FunctorPatternInterface::REDUCE,
+                                                    Kokkos::TeamPolicy<Kokkos::Experimental::GB300>, ReducerType,
+                                                    value_type>::Reducer;
+  WR wr(reducer);
+  value_type v;
+  wr.init(&v);
   for (iType i = b.start; i < b.end; ++i) closure(i, v);
+  wr.final(&v);
   reducer.reference() = v;
 }
 template <typename iType, class Closure, class ValueType>
 KOKKOS_INLINE_FUNCTION std::enable_if_t<!Kokkos::is_reducer<ValueType>::value> parallel_reduce(
     const Impl::ThreadVectorRangeBoundariesStruct<iType, Impl::GB300TeamMember>& b, const Closure& closure,
     ValueType& result) {
-  ValueType v = ValueType();
+  // a closure with its own join / init / final reduces with them (vector
+  // length 1: init, the loop, final)
+  using WR = typename Kokkos::Impl::FunctorAnalysis<Kokkos::Impl::FunctorPatternInterface::REDUCE,
+                                                    Kokkos::TeamPolicy<Kokkos::Experimental::GB300>, Closure,
+                                                    ValueType>::Reducer;
+  using value_type = typename WR::value_type;
+  WR wr(closure);
+  value_type v{};
+  wr.init(&v);
   for (iType i = b.start; i < b.end; ++i) closure(i, v);
+  wr.final(&v);
   result = v;
 }
 template <typename iType, class Closure, class ReducerType>
