@@ -275,29 +275,38 @@ class TeamPolicyInternal<Kokkos::Experimental::GB300, Properties...> : public Po
   TeamPolicyInternal(int league_size_request, int team_size_request, int vector_length_request = 1)
       : TeamPolicyInternal(execution_space(), league_size_request, team_size_request, vector_length_request) {}
 
+  // The largest team the pattern's kernel can launch with (its registers
+  // per thread bound the threads of a CTA), at most 1024; the pattern types
+  // are those the reference's CUDA policy names for the same query.
   template <class FunctorType>
   int team_size_max(const FunctorType&, const ParallelForTag&) const {
-    return 1024;
+    return ParallelFor<FunctorType, Kokkos::TeamPolicy<Properties...>, Kokkos::Experimental::GB300>::max_team_threads();
   }
   template <class FunctorType>
   int team_size_max(const FunctorType&, const ParallelReduceTag&) const {
-    return 1024;
+    using FA = FunctorAnalysis<FunctorPatternInterface::REDUCE, TeamPolicyInternal, FunctorType, void>;
+    return ParallelReduce<CombinedFunctorReducer<FunctorType, typename FA::Reducer>, Kokkos::TeamPolicy<Properties...>,
+                          Kokkos::Experimental::GB300>::max_team_threads();
   }
   template <class FunctorType, class ReducerType>
   int team_size_max(const FunctorType&, const ReducerType&, const ParallelReduceTag&) const {
-    return 1024;
+    return ParallelReduce<CombinedFunctorReducer<FunctorType, ReducerType>, Kokkos::TeamPolicy<Properties...>,
+                          Kokkos::Experimental::GB300>::max_team_threads();
   }
   template <class FunctorType>
-  int team_size_recommended(const FunctorType&, const ParallelForTag&) const {
-    return kDefaultTeam;
+  int team_size_recommended(const FunctorType& f, const ParallelForTag& t) const {
+    const int m = team_size_max(f, t);
+    return m < kDefaultTeam ? m : kDefaultTeam;
   }
   template <class FunctorType>
-  int team_size_recommended(const FunctorType&, const ParallelReduceTag&) const {
-    return kDefaultTeam;
+  int team_size_recommended(const FunctorType& f, const ParallelReduceTag& t) const {
+    const int m = team_size_max(f, t);
+    return m < kDefaultTeam ? m : kDefaultTeam;
   }
   template <class FunctorType, class ReducerType>
-  int team_size_recommended(const FunctorType&, const ReducerType&, const ParallelReduceTag&) const {
-    return kDefaultTeam;
+  int team_size_recommended(const FunctorType& f, const ReducerType& r, const ParallelReduceTag& t) const {
+    const int m = team_size_max(f, r, t);
+    return m < kDefaultTeam ? m : kDefaultTeam;
   }
 
   int team_size() const { return m_team_size; }
@@ -340,6 +349,15 @@ class TeamPolicyInternal<Kokkos::Experimental::GB300, Properties...> : public Po
     return *this;
   }
 };
+
+// Threads a CTA of this kernel can have (its registers per thread), at most
+// 1024, whole warps.
+inline int gb300_kernel_max_threads(const void* kernel) {
+  cudaFuncAttributes a{};
+  gb300_check_cuda(cudaFuncGetAttributes(&a, kernel), "TeamPolicy::team_size_max");
+  const int t = a.maxThreadsPerBlock < 1024 ? a.maxThreadsPerBlock : 1024;
+  return t >= 32 ? t / 32 * 32 : t;
+}
 
 // Grid and dynamic shared memory of a team launch.
 template <class Policy>
@@ -397,6 +415,7 @@ class ParallelFor<FunctorType, Kokkos::TeamPolicy<Properties...>, Kokkos::Experi
   };
 
   Policy const& get_policy() const { return m_policy; }
+  static int max_team_threads() { return gb300_kernel_max_threads((const void*)gbk_skel::k_team_for<Closure>); }
   ParallelFor(const FunctorType& arg_functor, const Policy& arg_policy)
       : m_functor(arg_functor), m_policy(arg_policy) {}
 
@@ -451,6 +470,9 @@ class ParallelReduce<CombinedFunctorReducerType, Kokkos::TeamPolicy<Properties..
   };
 
   Policy const& get_policy() const { return m_policy; }
+  static int max_team_threads() {
+    return gb300_kernel_max_threads((const void*)gbk_skel::k_team_reduce<gb300_value_bytes<ReducerType>(), Closure>);
+  }
 
   template <class ViewType>
   ParallelReduce(const CombinedFunctorReducerType& arg_functor_reducer, const Policy& arg_policy,

@@ -1,0 +1,3 @@
+// The reference's core/unit_test/TestMDRange_e.hpp on the GB300 space.
+#include <TestGB300_Category.hpp>
+#include <TestMDRange_e.hpp>
