@@ -196,6 +196,14 @@ struct MemorySpaceAccess<Kokkos::Experimental::GB300Space, Kokkos::HostSpace> {
   enum : bool { accessible = false };
   enum : bool { deepcopy = true };
 };
+// A team's scratch is reachable from the code of the space that owns it (a
+// managed View over ScratchMemorySpace<GB300> asks this of the space).
+template <>
+struct MemorySpaceAccess<Kokkos::Experimental::GB300Space, Kokkos::ScratchMemorySpace<Kokkos::Experimental::GB300>> {
+  enum : bool { assignable = false };
+  enum : bool { accessible = true };
+  enum : bool { deepcopy = false };
+};
 
 // ---- deep_copy: host<->device and device<->device through the library ----
 void gb300_deep_copy(void* dst, const void* src, size_t n);                      // synchronous
