@@ -52,3 +52,20 @@ def test_backend_builds_against_kokkos_and_registers():
     r = subprocess.run([b, "--no-device"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
     assert r.returncode == 0, r.stdout
     assert r.stdout.startswith("registered: Kokkos::Experimental::GB300: initialize"), r.stdout
+
+
+def test_reference_unit_test_compiles_for_the_space():
+    """One of the reference's own unit-test headers (core/unit_test/
+    TestReduce.hpp) compiles for the GB300 space through the test category
+    of tests/backend/unit, with the reference's googletest; the whole set
+    runs on a GPU machine from a copy of the Kokkos sources."""
+    if not os.path.isdir(os.path.join(REF, "core", "unit_test")) or \
+            not os.path.isdir(os.path.join(REF, "tpls", "gtest")):
+        pytest.skip("Kokkos unit-test sources not present")
+    build()
+    target = "tests/backend/_build/unit/gb300_Reduce.o"  # the Makefile's default OUT, relative to the repository
+    obj = os.path.join(ROOT, target)
+    r = subprocess.run(["make", "-s", "-f", "tests/backend/Makefile", f"REF={os.path.abspath(REF)}", target],
+                       cwd=ROOT, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout[-6000:]
+    assert os.path.getsize(obj) > 0
